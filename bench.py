@@ -1,0 +1,321 @@
+"""Benchmark: Monte Carlo transient of an RLC ladder, batched mixed precision.
+
+Workload (one "step" = one full pass): 2048 instances of a 200-section RLC ladder
+(R 50 Ohm, L 10 nH, C 1 pF, each x (1 + 0.1 N(0,1)), seeded), 0-1 V pulse with
+100 ps rise and 5 ns width, trapezoidal rule, fixed 1 ps step, 10000 steps; every
+unknown (602) is written at every step.  Metric: circuit-timesteps/sec.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's CPU algorithm (the C restatement in oracle/,
+rebuilding and refactoring the matrix every step as krets does) on the host cores.
+Prints ONE JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_INST = 2048
+SECTIONS = 200
+H = 1e-12
+N_STEPS = 10000
+SEED = 3
+METRIC = "circuit-timesteps/sec batched vs plain GPU form at <=1e-9 rel err vs FP64"
+UNIT = "circuit-timesteps/s"
+WORKLOAD = "mc_transient_rlc_ladder_2048x200sec_tr_1ps_10000steps"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def workload():
+    from krets_gb300.generators import monte_carlo_values, rlc_ladder
+    from krets_gb300.table import element_table
+    c = rlc_ladder(SECTIONS)
+    t = element_table(c)
+    vals = monte_carlo_values(c, N_INST, sigma=0.1, seed=SEED)
+    return c, t, vals
+
+
+def rel_err(x, ref, cur_mask):
+    worst = 0.0
+    for m in (cur_mask, ~cur_mask):
+        r = np.abs(ref[..., m]).max()
+        d = np.abs(x[..., m] - ref[..., m]).max()
+        worst = max(worst, d / r if r > 0 else d)
+    return worst
+
+
+# ------------------------------------------------------------------ CPU timing (oracle)
+def cpu_rate(t, vals, n, idxs, steps, faithful, threads):
+    """Time the oracle's TR transient on `idxs` instances over `steps` steps with a
+    thread pool (ctypes releases the GIL).  Returns circuit-timesteps/s."""
+    from oracle import oracle as O
+    O.lib()
+
+    def one(i):
+        ti = t.copy()
+        ti["value"] = vals[i]
+        O.tran(ti, n, H, steps, method="tr", lag=False, faithful=faithful)
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(one, idxs))
+    dt = time.perf_counter() - t0
+    return len(idxs) * steps / dt, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    c, t, vals = workload()
+    threads = os.cpu_count() or 1
+    steps_per_sample = 1000
+    idxs = list(range(threads))
+    for _ in range(args.warmup):
+        cpu_rate(t, vals, c.size, idxs[:1], 50, True, 1)
+    rates, times = [], []
+    for _ in range(args.steps):
+        r, dt = cpu_rate(t, vals, c.size, idxs, steps_per_sample, True, threads)
+        rates.append(r)
+        times.append(dt)
+    value = len(idxs) * steps_per_sample * args.steps / sum(times)
+    sample = (f"{len(idxs)} instances x {steps_per_sample} TR steps per step (of {N_INST} x {N_STEPS}), "
+              "matrix rebuilt and refactored every step as the reference does")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded splitmix64 Monte Carlo values)",
+        "config": {"workload": WORKLOAD, "instances": N_INST, "sections": SECTIONS, "h": H, "n_steps": N_STEPS,
+                   "method": "trapezoidal", "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the Rust reference cannot be built here (no cargo, no crate registry); the C "
+                "restatement of its algorithm in oracle/ stands in for it",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_ours(args, rank, world):
+    from krets_gb300 import _lib
+    from krets_gb300.table import is_current_mask
+
+    c, t, vals = workload()
+    n = c.size
+    g = _lib.GpuCircuit(t, n)
+    d_vals = _lib.DeviceArray(vals.shape).upload(vals)
+    out_shape = (N_INST, N_STEPS + 1, n)
+    d_out = _lib.DeviceArray(out_shape)
+    out_bytes = d_out.nbytes
+
+    def step():
+        g.batch_tran(d_vals, H, N_STEPS, "tr", lag=False, precision=_lib.PREC_MIXED, out=d_out, n_inst=N_INST)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+        g.flush_l2()
+    call_ms, kern_ms = [], []
+    l0 = _lib.launch_count()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        for _ in range(args.steps):
+            _lib.lib().krets_device_synchronize()
+            step()
+            _lib.lib().krets_device_synchronize()
+            k, cm = g.timing()
+            call_ms.append(cm)
+            kern_ms.append(k)
+            g.flush_l2()
+    launches = _lib.launch_count() - l0 - 0
+    hist, fallbacks = g.refine_stats()
+    total_s = sum(call_ms) / 1e3
+    ctsteps = N_INST * N_STEPS
+    value = ctsteps * args.steps * world / total_s
+
+    # accuracy: sampled instances against the FP64 oracle over the full 10000 steps
+    from oracle import oracle as O
+    mask = is_current_mask(c)
+    sample_idx = [0, N_INST // 2, N_INST - 1]
+    errs = []
+    for i in sample_idx:
+        host = np.empty((N_STEPS + 1, n))
+        off = i * (N_STEPS + 1) * n * 8
+        _lib.check(_lib.lib().krets_memcpy_d2h(host.ctypes.data_as(_lib.ctypes.c_void_p),
+                                               _lib.ctypes.c_void_p(d_out.ptr + off), host.nbytes))
+        ti = t.copy()
+        ti["value"] = vals[i]
+        ref = O.tran(ti, n, H, N_STEPS, method="tr", lag=False)
+        errs.append(rel_err(host, ref, mask))
+
+    # plain GPU form: one instance, FP64, level-scheduled single-CTA kernels per step
+    plain_steps = 2000
+    g1 = _lib.GpuCircuit(t, n)
+    g1.tran(H, 100, "tr", lag=False)
+    t0 = time.perf_counter()
+    g1.tran(H, plain_steps, "tr", lag=False)
+    _, plain_ms = g1.timing()
+    plain_rate = plain_steps / (plain_ms / 1e3)
+
+    # roofline of the dominant kernel (the batched transient)
+    alg_bytes = out_bytes - N_INST * n * 8 + vals.nbytes + N_INST * n * 8  # rows 1..N written, inputs read
+    k_s = statistics.mean(kern_ms) / 1e3
+    peak, peak_kind = measured_peak_hbm()
+    achieved = alg_bytes / k_s / 1e9
+
+    # CPU baseline: optimised oracle (factor once) on the host cores, bounded sample
+    threads = os.cpu_count() or 1
+    r1, dt1 = cpu_rate(t, vals, n, [0], 500, False, 1)
+    per_inst_s = N_STEPS / r1
+    n_sample = max(threads, min(8 * threads, int(15.0 * threads / max(per_inst_s, 1e-3))))
+    cpu_val, cpu_dt = cpu_rate(t, vals, n, list(range(n_sample)), N_STEPS, False, threads)
+
+    # end to end: host values in, host waveforms out, through the C ABI
+    del d_out
+    e2e_inst = N_INST
+    try:
+        with open("/proc/meminfo") as f:
+            avail_kb = int([ln for ln in f if ln.startswith("MemAvailable")][0].split()[1])
+        while e2e_inst > 64 and e2e_inst * (N_STEPS + 1) * n * 8 > 0.45 * avail_kb * 1024:
+            e2e_inst //= 2
+    except Exception:
+        e2e_inst = 256
+    host_out = np.empty((e2e_inst, N_STEPS + 1, n))
+    host_vals = np.ascontiguousarray(vals[:e2e_inst])
+    e2e_ms = []
+    for r in range(1 + max(1, min(args.steps, 2))):
+        _lib.lib().krets_device_synchronize()
+        g.batch_tran(host_vals, H, N_STEPS, "tr", lag=False, precision=_lib.PREC_MIXED, out=host_out)
+        _lib.lib().krets_device_synchronize()
+        if r > 0:
+            e2e_ms.append(g.timing()[1])
+    e2e_val = e2e_inst * N_STEPS * len(e2e_ms) / (sum(e2e_ms) / 1e3)
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": statistics.mean(call_ms), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32-factor+f64-refine",
+        "data": "synthetic (seeded splitmix64 Monte Carlo values)",
+        "config": {"workload": WORKLOAD, "instances": N_INST, "sections": SECTIONS, "unknowns": n, "h": H,
+                   "n_steps": N_STEPS, "method": "trapezoidal", "precision": "fp32 LU + fp64 refinement",
+                   "l2": "flushed between timed steps (512 MB write); outputs 98.6 GB >> L2",
+                   "parallelism": "replicas only (instances sharded per GPU)"},
+        "max_rel_err_vs_fp64": max(errs),
+        "refinement_histogram": [int(v) for v in hist], "fp64_fallbacks": int(fallbacks),
+        "plain_form": {"value": plain_rate, "unit": UNIT, "what": "1 instance, FP64, per-step kernels (CUDA graph)"},
+        "batched_over_plain": value / plain_rate,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "k_tran_batch<1>", "algorithmic_bytes_per_launch": alg_bytes},
+        "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n_sample} instances x {N_STEPS} TR steps, factor once, oracle/ C restatement"},
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(host_vals.nbytes),
+                "d2h_bytes_per_step": int(host_out.nbytes), "instances": e2e_inst},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if world > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,221 @@
+/*
+ * krets_gpu.h — C ABI of the GB300 (sm_103a) MNA solve path.
+ *
+ * This is the drop-in boundary for krets's solver crate.  Each entry point replaces one
+ * reference interface (paths inside prokie/krets):
+ *
+ *   krets_circuit_create   Solver::new(circuit, config)          crates/krets-solver/src/solver.rs:22-25
+ *                          + parse-time index layout             crates/krets-parser/src/parser.rs:105-125
+ *   krets_op               op::solve                             crates/krets-solver/src/solver/op.rs:15-86
+ *   krets_dc               dc::solve                             crates/krets-solver/src/solver/dc.rs:14-124
+ *   krets_ac               ac::solve                             crates/krets-solver/src/solver/ac.rs:17-109
+ *   krets_tran             transient::solve                      crates/krets-solver/src/solver/transient.rs:14-114
+ *   krets_batch_*          (no counterpart: many instances of one topology per launch)
+ *   krets_adjoint_tran     (no counterpart: adjoint sensitivities)
+ *   krets_status_string /  Display of krets_solver::Error        crates/krets-solver/src/error.rs:4-36
+ *   krets_last_error_message
+ *
+ * Conventions
+ *   - All functions are `extern "C"`, never throw, and return a krets_status (0 = OK).
+ *   - Unknown numbering is the reference's: in element file order, I(<id>) first for
+ *     Group-2 elements, then each first-seen non-ground node as V(<node>).
+ *   - Output buffers are caller-owned.  A pointer may be host memory (pageable or pinned)
+ *     or device memory; the library detects which and copies only when it must.
+ *   - A krets_circuit owns its device memory and one CUDA stream.  A handle is not
+ *     thread-safe; distinct handles are.
+ *   - No CPU fallback: every solve runs on the GPU, and an absent or unusable GPU is
+ *     reported as KRETS_ERR_CUDA.
+ */
+#ifndef KRETS_GPU_H
+#define KRETS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------------- status codes */
+typedef int32_t krets_status;
+#define KRETS_OK 0
+#define KRETS_ERR_ELEMENT_NOT_FOUND 1    /* Error::ElementNotFound            error.rs:8-9   */
+#define KRETS_ERR_MAX_ITERATIONS 2       /* Error::MaximumIterationsExceeded  error.rs:12-13 */
+#define KRETS_ERR_INVALID_ELEMENT 3      /* Error::InvalidElementFormat       error.rs:16-17 */
+#define KRETS_ERR_UNEXPECTED 4           /* Error::Unexpected                 error.rs:20-21 */
+#define KRETS_ERR_DECOMPOSITION_FAILED 5 /* Error::DecompositionFailed        error.rs:24-25 */
+#define KRETS_ERR_MATRIX_BUILD 6         /* Error::MatrixBuild                error.rs:28-29 */
+#define KRETS_ERR_MATRIX_DECOMPOSITION 7 /* Error::MatrixDecomposition        error.rs:32-33 */
+#define KRETS_ERR_NOT_IMPLEMENTED 8      /* the reference panics with todo!() (BJT, NMOS AC) */
+#define KRETS_ERR_TIMEOUT 9              /* a bounded device wait ran out                    */
+#define KRETS_ERR_CUDA 10                /* a CUDA runtime call failed / no GPU              */
+#define KRETS_ERR_INVALID_ARGUMENT 11
+#define KRETS_ERR_OUT_OF_MEMORY 12
+#define KRETS_ERR_PIVOT_UNSTABLE 13      /* static pivot growth above the limit              */
+
+/* ----------------------------------------------------------------- elements */
+#define KRETS_ELEM_R 1 /* resistor          value = ohms                                   */
+#define KRETS_ELEM_C 2 /* capacitor         value = farads, flags may hold KRETS_FLAG_G2   */
+#define KRETS_ELEM_L 3 /* inductor          value = henries                                */
+#define KRETS_ELEM_V 4 /* voltage source    value = dc value, ac = AC amplitude, wave/wp   */
+#define KRETS_ELEM_I 5 /* current source    value = amperes                                */
+#define KRETS_ELEM_D 6 /* diode             value = saturation current, wp[0] = emission n */
+#define KRETS_ELEM_M 7 /* NMOS level 1      wp = {vto, kp, lambda, w, l}; stamps nothing,
+                          as the reference's bare-name index lookups never match           */
+#define KRETS_ELEM_Q 8 /* BJT               parsed only; solving reports NOT_IMPLEMENTED   */
+
+#define KRETS_FLAG_G2 1
+
+#define KRETS_WAVE_NONE 0
+#define KRETS_WAVE_PULSE 1 /* wp = {v1, v2, td, tr, tf, pw, per}  voltage_source.rs:70-93 */
+#define KRETS_WAVE_SIN 2   /* wp = {off, amp, freq, td, damp, phase_deg}  :52-65          */
+
+/* One flattened element (104 bytes).  p/m/b/g hold MNA unknown indices or -1 (ground, or
+ * absent from the index map — the reference then skips that stamp entry). */
+typedef struct krets_element {
+  int32_t kind;
+  int32_t p;     /* V(plus)  (NMOS: drain)  */
+  int32_t m;     /* V(minus) (NMOS: source) */
+  int32_t b;     /* I(<id>) for Group-2 elements */
+  int32_t g;     /* NMOS gate */
+  int32_t flags;
+  int32_t wave;
+  int32_t reserved;
+  double value;
+  double ac;
+  double wp[7];
+} krets_element;
+
+/* SolverConfig (crates/krets-solver/src/config.rs:4-36). */
+typedef struct krets_config {
+  double relative_tolerance;         /* 1e-3  */
+  double current_absolute_tolerance; /* 1e-12 */
+  double voltage_absolute_tolerance; /* 1e-6  */
+  int32_t maximum_iterations;        /* 300   */
+  int32_t reserved;
+} krets_config;
+
+#define KRETS_METHOD_BE 0 /* backward Euler, as the reference */
+#define KRETS_METHOD_TR 1 /* trapezoidal (extension) */
+
+/* Precision of the batched transient/AC engines. */
+#define KRETS_PREC_FP64 0  /* FP64 factor and solves (the plain form's arithmetic)          */
+#define KRETS_PREC_MIXED 1 /* FP32 factor + solves, FP64 residual/state, iterative refinement */
+
+typedef struct krets_circuit krets_circuit;
+
+/* Compile the topology (host symbolic pass: fill-reducing ordering, static pivot
+ * sequence, fill pattern, stamp-to-slot maps, level schedules) and upload it.
+ * `elems` holds nominal values, used to choose pivots.  cfg may be NULL (defaults). */
+krets_status krets_circuit_create(const krets_element *elems, int32_t n_elem, int32_t n_unknowns,
+                                  const krets_config *cfg, krets_circuit **out);
+krets_status krets_circuit_destroy(krets_circuit *c);
+krets_status krets_circuit_info(const krets_circuit *c, int32_t mode, int32_t *n, int32_t *nnz_a,
+                                int32_t *nnz_lu, int32_t *n_levels, int32_t *n_ulevels);
+
+/* ------------------------------------------------- single-instance analyses (plain form)
+ * FP64 throughout, one instance, level-scheduled single-CTA kernels.  These mirror the
+ * reference's per-analysis functions; results use the reference unknown numbering. */
+
+/* x_out[n]; iters_out (optional) = Newton iterations. */
+krets_status krets_op(krets_circuit *c, double *x_out, int32_t *iters_out);
+
+/* DC sweep of element index `sweep_elem` (must be a V or I source).
+ * Points: |(stop-start)/step| + 1 (truncated), x_out[max_points][n]. */
+krets_status krets_dc(krets_circuit *c, int32_t sweep_elem, double start, double stop, double step,
+                      double *x_out, int32_t max_points, int32_t *n_points);
+
+/* AC sweep: operating point first, frequencies <= 0 skipped.
+ * x_out: complex, interleaved re/im, [n_freq][n][2]; *n_kept = points solved. */
+krets_status krets_ac(krets_circuit *c, const double *freqs, int32_t n_freq, double *x_out,
+                      int32_t *n_kept);
+
+/* Transient: t=0 operating point, then n_steps fixed steps of size h.
+ * method KRETS_METHOD_BE/TR; source_lag 1 = the reference's source timing (first Newton
+ * iteration sees t_{n-1}), 0 = sources at t_n.  refactor_each_step 1 refactors the
+ * matrix every step even for linear circuits (the reference's cost model).
+ * x_out[n_steps+1][n]. */
+krets_status krets_tran(krets_circuit *c, double h, int32_t n_steps, int32_t method, int32_t source_lag,
+                        int32_t refactor_each_step, double *x_out);
+
+/* ------------------------------------------------- batched (persistent) engines
+ * `values` [n_inst][n_elem] replaces each element's `value` per instance (Monte Carlo).
+ * The engine runs one instance per CTA drawn from a device work queue, keeps the
+ * factors and state in shared memory for the whole run, and writes every unknown at
+ * every step.  stats_out (optional, host) receives per-instance refinement counts. */
+krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *values, double h,
+                              int32_t n_steps, int32_t method, int32_t source_lag, int32_t precision,
+                              double *x_out /* [n_inst][n_steps+1][n] */,
+                              int32_t *inst_status /* [n_inst] or NULL */);
+
+/* Batched AC over frequency points of one instance (values NULL) or of several
+ * instances: each work item is one (instance, frequency) complex system.
+ * precision: FP64 = complex128 factor; MIXED = complex64 factor + complex128 refinement.
+ * x_out: [n_inst][n_freq][n][2]; frequencies must be > 0. */
+krets_status krets_batch_ac(krets_circuit *c, int32_t n_inst, const double *values, const double *freqs,
+                            int32_t n_freq, int32_t precision, double *x_out, int32_t *item_status);
+
+/* Batched operating points: x_out[n_inst][n]. */
+krets_status krets_batch_op(krets_circuit *c, int32_t n_inst, const double *values, double *x_out,
+                            int32_t *inst_status);
+
+/* ------------------------------------------------- diagnostics and timing */
+const char *krets_status_string(krets_status s);
+const char *krets_last_error_message(void);
+/* Device time (CUDA events on the handle's stream) of the last call's main kernel and of
+ * the whole last call (copies included), in milliseconds. */
+krets_status krets_last_timing(const krets_circuit *c, float *kernel_ms, float *call_ms);
+/* Kernel launches issued by this library since load. */
+int64_t krets_launch_count(void);
+/* Refinement statistics of the last mixed-precision batched call: histogram[k] = number
+ * of (instance, step) solves that took k refinement iterations (k < 8), fallbacks =
+ * instances that switched to an FP64 refactor, max_rel_correction = largest final
+ * correction / |x| seen. */
+krets_status krets_last_refine_stats(const krets_circuit *c, int64_t histogram[8], int32_t *fallbacks);
+
+/* Device memory helpers so a caller without a CUDA runtime binding can hold device-
+ * resident inputs/outputs (used by the benchmark). */
+krets_status krets_device_alloc(size_t bytes, void **ptr);
+krets_status krets_device_free(void *ptr);
+krets_status krets_memcpy_h2d(void *dst, const void *src, size_t bytes);
+krets_status krets_memcpy_d2h(void *dst, const void *src, size_t bytes);
+/* Write a scratch buffer larger than L2 (on the given circuit's stream). */
+krets_status krets_flush_l2(krets_circuit *c);
+krets_status krets_device_synchronize(void);
+
+/* ------------------------------------------------- symbolic-pass introspection
+ * Builds the static program of a topology for one mode on the host (no GPU needed) and
+ * copies array `which` (KRETS_PROG_*) into out[cap]; *len receives its length.  Used by
+ * tests to check the ordering, pivot sequence, fill and schedules. */
+#define KRETS_PROG_Q 0
+#define KRETS_PROG_PROW 1
+#define KRETS_PROG_LU_ROWPTR 2
+#define KRETS_PROG_LU_COL 3
+#define KRETS_PROG_LU_DIAG 4
+#define KRETS_PROG_A_ROWPTR 5
+#define KRETS_PROG_A_COL 6
+#define KRETS_PROG_A_SLOT 7
+#define KRETS_PROG_A_CPTR 8
+#define KRETS_PROG_A_CONTRIB 9
+#define KRETS_PROG_B_CPTR 10
+#define KRETS_PROG_B_CONTRIB 11
+#define KRETS_PROG_PIV_PTR 12
+#define KRETS_PROG_PIV 13
+#define KRETS_PROG_UPD 14
+#define KRETS_PROG_LEV_PTR 15
+#define KRETS_PROG_LEV_ROWS 16
+#define KRETS_PROG_ULEV_PTR 17
+#define KRETS_PROG_ULEV_ROWS 18
+#define KRETS_PROG_EL_POS 19
+#define KRETS_PROG_META 20 /* {ordering, n, nnz_a, nnz_lu, n_levels, n_ulevels, factor_flops} */
+#define KRETS_MODE_DC 0
+#define KRETS_MODE_AC 1
+#define KRETS_MODE_TRAN 2
+krets_status krets_symbolic_export(const krets_element *elems, int32_t n_elem, int32_t n_unknowns, int32_t mode,
+                                   int32_t method, double h, double freq, int32_t ordering /* -1 = autotune */,
+                                   int32_t which, int64_t *out, int64_t cap, int64_t *len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KRETS_GPU_H */

@@ -1,0 +1,290 @@
+"""ctypes binding of libkrets_gpu.so (the C ABI in include/krets_gpu.h).
+
+The library is built in-tree (krets_gb300/build.py).  There is no CPU fallback:
+when the library is missing, `lib()` raises, and every solve reports a CUDA
+error when no GPU is present.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from . import errors as E
+from .table import ELEM_DTYPE
+
+LIB_PATH = Path(__file__).resolve().parent / "libkrets_gpu.so"
+
+OK = 0
+ELEMENT_NOT_FOUND, MAX_ITERATIONS, INVALID_ELEMENT, UNEXPECTED = 1, 2, 3, 4
+DECOMPOSITION_FAILED, MATRIX_BUILD, MATRIX_DECOMPOSITION, NOT_IMPLEMENTED = 5, 6, 7, 8
+TIMEOUT, CUDA, INVALID_ARGUMENT, OUT_OF_MEMORY, PIVOT_UNSTABLE = 9, 10, 11, 12, 13
+
+METHOD = {"be": 0, "tr": 1}
+PREC_FP64, PREC_MIXED = 0, 1
+MODE_DC, MODE_AC, MODE_TRAN = 0, 1, 2
+
+PROG_ARRAYS = ["q", "prow", "lu_rowptr", "lu_col", "lu_diag", "a_rowptr", "a_col", "a_slot", "a_cptr",
+               "a_contrib", "b_cptr", "b_contrib", "piv_ptr", "piv", "upd", "lev_ptr", "lev_rows",
+               "ulev_ptr", "ulev_rows", "el_pos", "meta"]
+
+_EXC = {
+    ELEMENT_NOT_FOUND: E.ElementNotFound, MAX_ITERATIONS: E.MaximumIterationsExceeded,
+    INVALID_ELEMENT: E.InvalidElementFormat, UNEXPECTED: E.Unexpected,
+    DECOMPOSITION_FAILED: E.DecompositionFailed, MATRIX_BUILD: E.MatrixBuild,
+    MATRIX_DECOMPOSITION: E.MatrixDecomposition, NOT_IMPLEMENTED: E.NotImplementedInReference,
+    TIMEOUT: E.DeviceTimeout, CUDA: E.CudaError, INVALID_ARGUMENT: E.KretsError,
+    OUT_OF_MEMORY: E.CudaError, PIVOT_UNSTABLE: E.PivotUnstable,
+}
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("relative_tolerance", ctypes.c_double), ("current_absolute_tolerance", ctypes.c_double),
+                ("voltage_absolute_tolerance", ctypes.c_double), ("maximum_iterations", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+_lib = None
+_P = ctypes.c_void_p
+_I = ctypes.c_int32
+_D = ctypes.c_double
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise E.CudaError(f"{LIB_PATH} is not built (run krets_gb300.build.build()); "
+                              "there is no CPU fallback")
+        L = ctypes.CDLL(str(LIB_PATH))
+        sig = {
+            "krets_circuit_create": [_P, _I, _I, _P, _P],
+            "krets_circuit_destroy": [_P],
+            "krets_circuit_info": [_P, _I, _P, _P, _P, _P, _P],
+            "krets_op": [_P, _P, _P],
+            "krets_dc": [_P, _I, _D, _D, _D, _P, _I, _P],
+            "krets_ac": [_P, _P, _I, _P, _P],
+            "krets_tran": [_P, _D, _I, _I, _I, _I, _P],
+            "krets_batch_tran": [_P, _I, _P, _D, _I, _I, _I, _I, _P, _P],
+            "krets_batch_ac": [_P, _I, _P, _P, _I, _I, _P, _P],
+            "krets_batch_op": [_P, _I, _P, _P, _P],
+            "krets_last_timing": [_P, _P, _P],
+            "krets_last_refine_stats": [_P, _P, _P],
+            "krets_device_alloc": [ctypes.c_size_t, _P],
+            "krets_device_free": [_P],
+            "krets_memcpy_h2d": [_P, _P, ctypes.c_size_t],
+            "krets_memcpy_d2h": [_P, _P, ctypes.c_size_t],
+            "krets_flush_l2": [_P],
+            "krets_device_synchronize": [],
+            "krets_symbolic_export": [_P, _I, _I, _I, _I, _D, _D, _I, _I, _P, ctypes.c_int64, _P],
+        }
+        for name, args in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int32
+        L.krets_status_string.argtypes = [_I]
+        L.krets_status_string.restype = ctypes.c_char_p
+        L.krets_last_error_message.argtypes = []
+        L.krets_last_error_message.restype = ctypes.c_char_p
+        L.krets_launch_count.argtypes = []
+        L.krets_launch_count.restype = ctypes.c_int64
+        _lib = L
+    return _lib
+
+
+def check(status: int, what: str = ""):
+    if status == OK:
+        return
+    L = lib()
+    msg = L.krets_last_error_message().decode(errors="replace")
+    cls = _EXC.get(status, E.KretsError)
+    raise cls(f"{what}: {L.krets_status_string(status).decode()} ({msg})")
+
+
+def ptr(a) -> ctypes.c_void_p:
+    if a is None:
+        return None
+    if isinstance(a, DeviceArray):
+        return ctypes.c_void_p(a.ptr)
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class DeviceArray:
+    """Device memory owned through the library (for callers without a CUDA binding)."""
+
+    def __init__(self, shape, dtype=np.float64):
+        self.shape = tuple(shape) if isinstance(shape, (tuple, list)) else (int(shape),)
+        self.dtype = np.dtype(dtype)
+        self.nbytes = int(np.prod(self.shape)) * self.dtype.itemsize
+        p = ctypes.c_void_p()
+        check(lib().krets_device_alloc(max(self.nbytes, 16), ctypes.byref(p)), "device alloc")
+        self.ptr = p.value
+
+    def upload(self, host: np.ndarray):
+        h = np.ascontiguousarray(host, dtype=self.dtype)
+        assert h.nbytes == self.nbytes
+        check(lib().krets_memcpy_h2d(ctypes.c_void_p(self.ptr), h.ctypes.data_as(ctypes.c_void_p), self.nbytes))
+        return self
+
+    def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        out = np.empty(self.shape, self.dtype) if out is None else out
+        check(lib().krets_memcpy_d2h(out.ctypes.data_as(ctypes.c_void_p), ctypes.c_void_p(self.ptr), self.nbytes))
+        return out
+
+    def free(self):
+        if self.ptr:
+            lib().krets_device_free(ctypes.c_void_p(self.ptr))
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class GpuCircuit:
+    """Owns a krets_circuit handle (compiled topology on the device)."""
+
+    def __init__(self, table: np.ndarray, n: int, config=None):
+        self.table = np.ascontiguousarray(table, dtype=ELEM_DTYPE)
+        self.n = int(n)
+        self.ne = len(self.table)
+        cfg = None
+        if config is not None:
+            cfg = Config(config.relative_tolerance, config.current_absolute_tolerance,
+                         config.voltage_absolute_tolerance, config.maximum_iterations, 0)
+        h = ctypes.c_void_p()
+        check(lib().krets_circuit_create(ptr(self.table), self.ne, self.n,
+                                         ctypes.byref(cfg) if cfg is not None else None, ctypes.byref(h)),
+              "krets_circuit_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().krets_circuit_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -------------------------------------------------------------- analyses
+    def op(self):
+        x = np.zeros(self.n)
+        it = ctypes.c_int32(0)
+        check(lib().krets_op(self.h, ptr(x), ctypes.byref(it)), "op")
+        return x, it.value
+
+    def dc(self, sweep_index, start, stop, step):
+        npts = int(abs((stop - start) / step)) + 1
+        x = np.zeros((npts, self.n))
+        got = ctypes.c_int32(0)
+        check(lib().krets_dc(self.h, sweep_index, start, stop, step, ptr(x), npts, ctypes.byref(got)), "dc")
+        return x[:got.value]
+
+    def ac(self, freqs):
+        f = np.ascontiguousarray(freqs, dtype=np.float64)
+        x = np.zeros((max(len(f), 1), self.n, 2))
+        kept = ctypes.c_int32(0)
+        check(lib().krets_ac(self.h, ptr(f), len(f), ptr(x), ctypes.byref(kept)), "ac")
+        return x[:kept.value, :, 0] + 1j * x[:kept.value, :, 1]
+
+    def tran(self, h, n_steps, method="be", lag=None, refactor_each_step=False):
+        m = METHOD[method]
+        if lag is None:
+            lag = m == 0
+        x = np.zeros((n_steps + 1, self.n))
+        check(lib().krets_tran(self.h, h, n_steps, m, int(bool(lag)), int(bool(refactor_each_step)), ptr(x)),
+              "tran")
+        return x
+
+    def batch_op(self, values):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        ni = v.shape[0]
+        x = np.zeros((ni, self.n))
+        st = np.zeros(ni, dtype=np.int32)
+        check(lib().krets_batch_op(self.h, ni, ptr(v), ptr(x), ptr(st)), "batch_op")
+        return x
+
+    def batch_tran(self, values, h, n_steps, method="tr", lag=None, precision=PREC_MIXED, out=None,
+                   n_inst=None):
+        m = METHOD[method]
+        if lag is None:
+            lag = m == 0
+        if isinstance(values, DeviceArray):
+            ni = values.shape[0] if n_inst is None else n_inst
+        elif values is None:
+            ni = 1 if n_inst is None else n_inst
+        else:
+            values = np.ascontiguousarray(values, dtype=np.float64)
+            ni = values.shape[0]
+        if out is None:
+            out = np.zeros((ni, n_steps + 1, self.n))
+        st = np.zeros(ni, dtype=np.int32)
+        check(lib().krets_batch_tran(self.h, ni, ptr(values), h, n_steps, m, int(bool(lag)), precision, ptr(out),
+                                     ptr(st)), "batch_tran")
+        return out
+
+    def batch_ac(self, values, freqs, precision=PREC_MIXED, out=None):
+        f = np.ascontiguousarray(freqs, dtype=np.float64)
+        if values is None:
+            ni = 1
+        elif isinstance(values, DeviceArray):
+            ni = values.shape[0]
+        else:
+            values = np.ascontiguousarray(values, dtype=np.float64)
+            ni = values.shape[0]
+        host_out = out is None
+        if host_out:
+            out = np.zeros((ni, len(f), self.n, 2))
+        st = np.zeros(ni * len(f), dtype=np.int32)
+        check(lib().krets_batch_ac(self.h, ni, ptr(values), ptr(f), len(f), precision, ptr(out), ptr(st)),
+              "batch_ac")
+        if host_out:
+            return out[..., 0] + 1j * out[..., 1]
+        return out
+
+    # -------------------------------------------------------------- diagnostics
+    def timing(self):
+        k = ctypes.c_float()
+        c = ctypes.c_float()
+        check(lib().krets_last_timing(self.h, ctypes.byref(k), ctypes.byref(c)))
+        return k.value, c.value
+
+    def refine_stats(self):
+        hist = np.zeros(8, dtype=np.int64)
+        fb = ctypes.c_int32()
+        check(lib().krets_last_refine_stats(self.h, ptr(hist), ctypes.byref(fb)))
+        return hist, fb.value
+
+    def info(self, mode):
+        vals = [ctypes.c_int32() for _ in range(5)]
+        check(lib().krets_circuit_info(self.h, mode, *[ctypes.byref(v) for v in vals]))
+        return dict(zip(["n", "nnz_a", "nnz_lu", "n_levels", "n_ulevels"], [v.value for v in vals]))
+
+    def flush_l2(self):
+        check(lib().krets_flush_l2(self.h))
+
+
+def launch_count() -> int:
+    return int(lib().krets_launch_count())
+
+
+def symbolic_export(table, n, mode, method="be", h=1e-9, freq=1e3, ordering=-1):
+    """Host symbolic pass arrays (no GPU needed): dict name -> int64 array."""
+    t = np.ascontiguousarray(table, dtype=ELEM_DTYPE)
+    out = {}
+    m = METHOD[method] if isinstance(method, str) else method
+    for which, name in enumerate(PROG_ARRAYS):
+        ln = ctypes.c_int64(0)
+        check(lib().krets_symbolic_export(ptr(t), len(t), n, mode, m, h, freq, ordering, which, None, 0,
+                                          ctypes.byref(ln)), "symbolic_export")
+        arr = np.zeros(max(ln.value, 1), dtype=np.int64)
+        check(lib().krets_symbolic_export(ptr(t), len(t), n, mode, m, h, freq, ordering, which, ptr(arr),
+                                          ln.value, ctypes.byref(ln)), "symbolic_export")
+        out[name] = arr[:ln.value]
+    return out

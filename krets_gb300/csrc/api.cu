@@ -1,0 +1,821 @@
+// C ABI (include/krets_gpu.h): handle management, program upload, workspace layout,
+// launches, CUDA-graph replay of the plain transient, timing and error reporting.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "krets_gpu.h"
+#include "symbolic.h"
+
+using namespace krets;
+
+namespace {
+
+thread_local std::string g_last_error;
+std::atomic<long long> g_launches{0};
+
+krets_status fail(krets_status s, const std::string &msg) {
+  g_last_error = msg;
+  return s;
+}
+
+#define CU(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(KRETS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+struct LayBuilder {
+  Lay L{};
+  size_t cur = 0;
+  int idx = 0;
+  void add(int slot, size_t bytes) {
+    L.off[slot] = (int)cur;
+    cur = align16(cur + bytes);
+  }
+  Lay done() {
+    L.bytes = align16(cur ? cur : 16);
+    return L;
+  }
+};
+
+// Uploaded program: one device buffer holding every index array.
+struct DevProgram {
+  Program host;
+  DevProg view{};
+  void *buf = nullptr;
+  ~DevProgram() { if (buf) cudaFree(buf); }
+};
+
+int device_sm_count() {
+  static int sms = -1;
+  if (sms < 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      sms = 1;
+  }
+  return sms;
+}
+
+size_t max_smem_optin() {
+  static int v = -1;
+  if (v < 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+      v = 48 * 1024;
+  }
+  return (size_t)v;
+}
+
+bool is_device_ptr(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+struct krets_circuit {
+  std::vector<krets_element> el;
+  int n = 0, ne = 0;
+  KCfg cfg{};
+  bool nonlinear = false;
+  krets_element *d_el = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {};
+  float kernel_ms = 0.f, call_ms = 0.f;
+  std::map<std::string, std::unique_ptr<DevProgram>> progs;
+  int *d_is_cur_tmp = nullptr;
+  // scratch
+  void *scratch = nullptr;
+  size_t scratch_bytes = 0;
+  int *d_small = nullptr;  // counters / status words
+  unsigned long long *d_hist = nullptr;
+  long long hist[8] = {};
+  int fallbacks = 0;
+  void *l2buf = nullptr;
+
+  ~krets_circuit() {
+    if (d_el) cudaFree(d_el);
+    if (scratch) cudaFree(scratch);
+    if (d_small) cudaFree(d_small);
+    if (d_hist) cudaFree(d_hist);
+    if (l2buf) cudaFree(l2buf);
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  krets_status ensure_scratch(size_t bytes) {
+    if (bytes <= scratch_bytes) return KRETS_OK;
+    if (scratch) cudaFree(scratch);
+    scratch = nullptr;
+    scratch_bytes = 0;
+    CU(cudaMalloc(&scratch, bytes));
+    scratch_bytes = bytes;
+    return KRETS_OK;
+  }
+};
+
+namespace {
+
+krets_status upload_program(krets_circuit *c, Program &&P, DevProgram &D) {
+  D.host = std::move(P);
+  Program &H = D.host;
+  // compute lu_src: A entry index per LU slot
+  std::vector<int> lu_src(H.lu_col.size(), -1);
+  for (size_t t = 0; t < H.a_slot.size(); ++t) lu_src[H.a_slot[t]] = (int)t;
+  std::vector<int> is_cur(H.n, 0);
+  for (int e = 0; e < H.ne; ++e)
+    if (H.el_pos[4 * e + 2] >= 0) is_cur[H.el_pos[4 * e + 2]] = 1;
+  struct Part { const void *src; size_t bytes; size_t off; };
+  std::vector<Part> parts;
+  size_t total = 0;
+  auto add = [&](const void *src, size_t bytes) {
+    parts.push_back({src, bytes, total});
+    total = align16(total + (bytes ? bytes : 4));
+    return parts.size() - 1;
+  };
+  auto vi = [&](const std::vector<int> &v) { return add(v.data(), v.size() * sizeof(int)); };
+  size_t i_q = vi(H.q), i_rp = vi(H.lu_rowptr), i_col = vi(H.lu_col), i_dg = vi(H.lu_diag), i_src = vi(lu_src);
+  size_t i_arp = vi(H.a_rowptr), i_acol = vi(H.a_col), i_acp = vi(H.a_cptr), i_acn = vi(H.a_contrib);
+  size_t i_bcp = vi(H.b_cptr), i_bcn = vi(H.b_contrib), i_pp = vi(H.piv_ptr), i_pv = vi(H.piv), i_up = vi(H.upd);
+  size_t i_lp = vi(H.lev_ptr), i_lr = vi(H.lev_rows), i_ulp = vi(H.ulev_ptr), i_ulr = vi(H.ulev_rows);
+  size_t i_ep = vi(H.el_pos), i_ic = vi(is_cur);
+  CU(cudaMalloc(&D.buf, total));
+  std::vector<char> staging(total, 0);
+  for (auto &p : parts)
+    if (p.bytes) memcpy(staging.data() + p.off, p.src, p.bytes);
+  CU(cudaMemcpy(D.buf, staging.data(), total, cudaMemcpyHostToDevice));
+  char *b = (char *)D.buf;
+  auto ptr = [&](size_t i) { return (const void *)(b + parts[i].off); };
+  DevProg &V = D.view;
+  V.n = H.n;
+  V.ne = H.ne;
+  V.nnz_a = (int)H.a_col.size();
+  V.nnz_lu = (int)H.lu_col.size();
+  V.nlev = (int)H.lev_ptr.size() - 1;
+  V.nulev = (int)H.ulev_ptr.size() - 1;
+  V.mode = H.mode;
+  V.method = H.method;
+  V.q = (const int *)ptr(i_q);
+  V.lu_rowptr = (const int *)ptr(i_rp);
+  V.lu_col = (const int *)ptr(i_col);
+  V.lu_diag = (const int *)ptr(i_dg);
+  V.lu_src = (const int *)ptr(i_src);
+  V.a_rowptr = (const int *)ptr(i_arp);
+  V.a_col = (const int *)ptr(i_acol);
+  V.a_cptr = (const int *)ptr(i_acp);
+  V.a_contrib = (const int *)ptr(i_acn);
+  V.b_cptr = (const int *)ptr(i_bcp);
+  V.b_contrib = (const int *)ptr(i_bcn);
+  V.piv_ptr = (const int *)ptr(i_pp);
+  V.piv = (const int4 *)ptr(i_pv);
+  V.upd = (const int2 *)ptr(i_up);
+  V.lev_ptr = (const int *)ptr(i_lp);
+  V.lev_rows = (const int *)ptr(i_lr);
+  V.ulev_ptr = (const int *)ptr(i_ulp);
+  V.ulev_rows = (const int *)ptr(i_ulr);
+  V.el_pos = (const int4 *)ptr(i_ep);
+  V.is_cur = (const int *)ptr(i_ic);
+  V.el = c->d_el;
+  bool nl = false;
+  for (int e = 0; e < H.ne; ++e) {
+    int k = c->el[e].kind;
+    if (H.mode == MODE_DC && k == KRETS_ELEM_C) continue;
+    if (k == KRETS_ELEM_D || k == KRETS_ELEM_M || k == KRETS_ELEM_Q) nl = true;
+  }
+  V.nonlinear = nl;
+  return KRETS_OK;
+}
+
+krets_status get_program(krets_circuit *c, int mode, int method, double h, double f, DevProgram **out) {
+  char key[128];
+  snprintf(key, sizeof key, "%d/%d/%.17g/%.17g", mode, method, mode == MODE_TRAN ? h : 0.0, mode == MODE_AC ? f : 0.0);
+  auto it = c->progs.find(key);
+  if (it != c->progs.end()) {
+    *out = it->second.get();
+    return KRETS_OK;
+  }
+  Program P;
+  std::string msg;
+  int st = build_program(c->el.data(), c->ne, c->n, mode, method, h, f, -1, P, msg);
+  if (st != KRETS_OK) return fail(st, msg);
+  auto D = std::make_unique<DevProgram>();
+  krets_status s2 = upload_program(c, std::move(P), *D);
+  if (s2 != KRETS_OK) return s2;
+  *out = D.get();
+  c->progs[key] = std::move(D);
+  return KRETS_OK;
+}
+
+Lay layout_op(const DevProg &P) {
+  LayBuilder B;
+  B.add(0, sizeof(double) * P.nnz_lu);
+  B.add(1, sizeof(double) * P.n);
+  B.add(2, sizeof(double) * P.n);
+  B.add(3, sizeof(double) * P.n);
+  B.add(4, sizeof(double) * P.ne);
+  B.add(5, sizeof(double) * P.ne);
+  B.add(6, sizeof(int) * 4);
+  B.add(7, sizeof(double) * P.ne);
+  return B.done();
+}
+
+Lay layout_tran(const DevProg &P, bool mixed) {
+  LayBuilder B;
+  B.add(0, sizeof(double) * P.ne);
+  B.add(1, mixed ? sizeof(double) * P.nnz_a : 0);
+  B.add(2, (mixed ? sizeof(float) : sizeof(double)) * P.nnz_lu);
+  B.add(3, sizeof(double) * P.n);
+  B.add(4, P.nonlinear ? sizeof(double) * P.n : 0);
+  B.add(5, P.nonlinear ? sizeof(double) * P.n : 0);
+  B.add(6, sizeof(double) * P.n);
+  B.add(7, mixed ? sizeof(float) * P.n : 0);
+  B.add(8, sizeof(double) * P.ne);
+  B.add(9, sizeof(double) * P.ne);
+  B.add(10, sizeof(double) * P.ne);
+  B.add(11, sizeof(double) * 32);
+  B.add(12, sizeof(int) * 4);
+  B.add(13, sizeof(int) * 4);
+  return B.done();
+}
+
+Lay layout_ac(const DevProg &P, bool mixed) {
+  LayBuilder B;
+  B.add(0, sizeof(double) * P.ne);
+  B.add(1, mixed ? 16 * (size_t)P.nnz_a : 0);
+  B.add(2, (mixed ? 8 : 16) * (size_t)P.nnz_lu);
+  B.add(3, 16 * (size_t)P.n);
+  B.add(4, 16 * (size_t)P.n);
+  B.add(5, mixed ? 8 * (size_t)P.n : 0);
+  B.add(6, sizeof(double) * P.ne);
+  B.add(7, sizeof(double) * P.ne);
+  B.add(8, sizeof(double) * P.ne);
+  B.add(9, sizeof(double) * P.n);
+  B.add(10, sizeof(double) * 32);
+  B.add(11, sizeof(int) * 4);
+  B.add(12, sizeof(int) * 4);
+  return B.done();
+}
+
+// Decide shared vs global placement and the grid for a per-CTA workspace.
+template <typename K>
+krets_status plan_launch(krets_circuit *c, K kernel, const Lay &L, int threads, int items, int &grid,
+                         size_t &smem, char *&gws) {
+  if (L.bytes <= max_smem_optin()) {
+    smem = L.bytes;
+    gws = nullptr;
+    CU(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
+    if (per_sm < 1) per_sm = 1;
+    grid = std::max(1, std::min(items, per_sm * device_sm_count()));
+  } else {
+    smem = 0;
+    grid = std::max(1, std::min(items, 2 * device_sm_count()));
+    krets_status s = c->ensure_scratch(L.bytes * (size_t)grid);
+    if (s != KRETS_OK) return s;
+    gws = (char *)c->scratch;
+  }
+  return KRETS_OK;
+}
+
+krets_status map_status(int bits, int mode_for_decomp) {
+  if (bits & KS_NOTIMPL) return fail(KRETS_ERR_NOT_IMPLEMENTED, "stamp is not implemented in the reference (todo!())");
+  if (bits & (KS_SINGULAR | KS_NONFINITE))
+    return fail(mode_for_decomp == 0 ? KRETS_ERR_MATRIX_DECOMPOSITION : KRETS_ERR_DECOMPOSITION_FAILED,
+                "zero or non-finite pivot during factorisation");
+  if (bits & KS_MAXITER) return fail(KRETS_ERR_MAX_ITERATIONS, "maximum Newton iterations exceeded");
+  if (bits & KS_STALL) return fail(KRETS_ERR_PIVOT_UNSTABLE, "iterative refinement stalled");
+  return KRETS_OK;
+}
+
+struct DevBuf {
+  void *p = nullptr;
+  ~DevBuf() { if (p) cudaFree(p); }
+};
+
+// Device view of a caller buffer: use it directly when it is device memory, otherwise a
+// temporary device buffer (copied in when `in` is set).
+krets_status dev_view(const void *user, size_t bytes, bool in, cudaStream_t s, DevBuf &tmp, void **dptr) {
+  if (!user || bytes == 0) {
+    *dptr = nullptr;
+    return KRETS_OK;
+  }
+  if (is_device_ptr(user)) {
+    *dptr = const_cast<void *>(user);
+    return KRETS_OK;
+  }
+  CU(cudaMalloc(&tmp.p, bytes));
+  if (in) CU(cudaMemcpyAsync(tmp.p, user, bytes, cudaMemcpyHostToDevice, s));
+  *dptr = tmp.p;
+  return KRETS_OK;
+}
+
+krets_status run_op(krets_circuit *c, DevProgram *D, int n_inst, const double *d_values, double *d_x,
+                    size_t out_stride, int *d_status, int *d_iters, int threads) {
+  Lay L = layout_op(D->view);
+  int grid;
+  size_t smem;
+  char *gws;
+  krets_status s = plan_launch(c, k_op, L, threads, n_inst, grid, smem, gws);
+  if (s != KRETS_OK) return s;
+  k_op<<<grid, threads, smem, c->stream>>>(D->view, c->cfg, L, gws, d_values, d_x, out_stride, d_status, d_iters,
+                                          n_inst);
+  g_launches++;
+  CU(cudaGetLastError());
+  return KRETS_OK;
+}
+
+int plain_threads(const DevProg &P) {
+  int t = 128;
+  while (t < 512 && t < P.n / 2) t *= 2;
+  return t;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+krets_status krets_circuit_create(const krets_element *elems, int32_t n_elem, int32_t n_unknowns,
+                                  const krets_config *cfg, krets_circuit **out) {
+  if (!out || (!elems && n_elem > 0) || n_elem < 0 || n_unknowns <= 0)
+    return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments to krets_circuit_create");
+  *out = nullptr;
+  for (int e = 0; e < n_elem; ++e) {
+    const krets_element &x = elems[e];
+    if (x.kind < KRETS_ELEM_R || x.kind > KRETS_ELEM_Q)
+      return fail(KRETS_ERR_INVALID_ELEMENT, "unknown element kind at index " + std::to_string(e));
+    const int idx[4] = {x.p, x.m, x.b, x.g};
+    for (int v : idx)
+      if (v < -1 || v >= n_unknowns)
+        return fail(KRETS_ERR_INVALID_ARGUMENT, "element " + std::to_string(e) + " has an unknown index out of range");
+  }
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
+    cudaGetLastError();
+    return fail(KRETS_ERR_CUDA, "no CUDA device is available (this library has no CPU fallback)");
+  }
+  auto c = std::make_unique<krets_circuit>();
+  c->el.assign(elems, elems + n_elem);
+  c->n = n_unknowns;
+  c->ne = n_elem;
+  krets_config d{0.001, 1e-12, 1e-6, 300, 0};
+  const krets_config &k = cfg ? *cfg : d;
+  c->cfg = KCfg{k.relative_tolerance, k.current_absolute_tolerance, k.voltage_absolute_tolerance,
+                k.maximum_iterations};
+  CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  for (auto &e : c->ev) CU(cudaEventCreate(&e));
+  CU(cudaMalloc(&c->d_el, sizeof(krets_element) * std::max(1, n_elem)));
+  if (n_elem) CU(cudaMemcpy(c->d_el, elems, sizeof(krets_element) * n_elem, cudaMemcpyHostToDevice));
+  CU(cudaMalloc(&c->d_small, 4096));
+  CU(cudaMalloc(&c->d_hist, 8 * sizeof(unsigned long long)));
+  *out = c.release();
+  return KRETS_OK;
+}
+
+krets_status krets_circuit_destroy(krets_circuit *c) {
+  delete c;
+  return KRETS_OK;
+}
+
+krets_status krets_circuit_info(const krets_circuit *cc, int32_t mode, int32_t *n, int32_t *nnz_a, int32_t *nnz_lu,
+                                int32_t *n_levels, int32_t *n_ulevels) {
+  krets_circuit *c = const_cast<krets_circuit *>(cc);
+  if (!c) return fail(KRETS_ERR_INVALID_ARGUMENT, "null circuit");
+  DevProgram *D;
+  krets_status s = get_program(c, mode, KRETS_METHOD_TR, 1e-12, 1e3, &D);
+  if (s != KRETS_OK) return s;
+  if (n) *n = D->view.n;
+  if (nnz_a) *nnz_a = D->view.nnz_a;
+  if (nnz_lu) *nnz_lu = D->view.nnz_lu;
+  if (n_levels) *n_levels = D->view.nlev;
+  if (n_ulevels) *n_ulevels = D->view.nulev;
+  return KRETS_OK;
+}
+
+krets_status krets_op(krets_circuit *c, double *x_out, int32_t *iters_out) {
+  if (!c || !x_out) return fail(KRETS_ERR_INVALID_ARGUMENT, "null argument");
+  DevProgram *D;
+  krets_status s = get_program(c, MODE_DC, 0, 0, 0, &D);
+  if (s != KRETS_OK) return s == KRETS_ERR_DECOMPOSITION_FAILED ? KRETS_ERR_MATRIX_DECOMPOSITION : s;
+  DevBuf tx;
+  void *dx;
+  CU(cudaEventRecord(c->ev[0], c->stream));
+  s = dev_view(x_out, sizeof(double) * c->n, false, c->stream, tx, &dx);
+  if (s) return s;
+  int *d_status = c->d_small, *d_iters = c->d_small + 1;
+  CU(cudaMemsetAsync(c->d_small, 0, 16, c->stream));
+  CU(cudaEventRecord(c->ev[2], c->stream));
+  s = run_op(c, D, 1, nullptr, (double *)dx, c->n, d_status, d_iters, plain_threads(D->view));
+  if (s) return s;
+  CU(cudaEventRecord(c->ev[3], c->stream));
+  if (tx.p) CU(cudaMemcpyAsync(x_out, dx, sizeof(double) * c->n, cudaMemcpyDeviceToHost, c->stream));
+  int h[2];
+  CU(cudaMemcpyAsync(h, c->d_small, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaEventRecord(c->ev[1], c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  cudaEventElapsedTime(&c->kernel_ms, c->ev[2], c->ev[3]);
+  cudaEventElapsedTime(&c->call_ms, c->ev[0], c->ev[1]);
+  if (iters_out) *iters_out = h[1];
+  return map_status(h[0], 0);
+}
+
+krets_status krets_batch_op(krets_circuit *c, int32_t n_inst, const double *values, double *x_out,
+                            int32_t *inst_status) {
+  if (!c || !x_out || n_inst <= 0) return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments");
+  DevProgram *D;
+  krets_status s = get_program(c, MODE_DC, 0, 0, 0, &D);
+  if (s != KRETS_OK) return s;
+  CU(cudaEventRecord(c->ev[0], c->stream));
+  DevBuf tv, tx, ts;
+  void *dv, *dx, *dst;
+  s = dev_view(values, sizeof(double) * c->ne * (size_t)n_inst, true, c->stream, tv, &dv);
+  if (s) return s;
+  s = dev_view(x_out, sizeof(double) * c->n * (size_t)n_inst, false, c->stream, tx, &dx);
+  if (s) return s;
+  CU(cudaMalloc(&ts.p, sizeof(int) * n_inst));
+  dst = ts.p;
+  CU(cudaMemsetAsync(dst, 0, sizeof(int) * n_inst, c->stream));
+  CU(cudaEventRecord(c->ev[2], c->stream));
+  s = run_op(c, D, n_inst, (const double *)dv, (double *)dx, c->n, (int *)dst, nullptr, 128);
+  if (s) return s;
+  CU(cudaEventRecord(c->ev[3], c->stream));
+  if (tx.p) CU(cudaMemcpyAsync(x_out, dx, sizeof(double) * c->n * (size_t)n_inst, cudaMemcpyDeviceToHost, c->stream));
+  std::vector<int> st(n_inst);
+  CU(cudaMemcpyAsync(st.data(), dst, sizeof(int) * n_inst, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaEventRecord(c->ev[1], c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  cudaEventElapsedTime(&c->kernel_ms, c->ev[2], c->ev[3]);
+  cudaEventElapsedTime(&c->call_ms, c->ev[0], c->ev[1]);
+  int any = 0;
+  for (int i = 0; i < n_inst; ++i) {
+    if (inst_status) inst_status[i] = st[i];
+    any |= st[i];
+  }
+  return map_status(any, 0);
+}
+
+krets_status krets_dc(krets_circuit *c, int32_t sweep_elem, double start, double stop, double step, double *x_out,
+                      int32_t max_points, int32_t *n_points) {
+  if (!c || !x_out) return fail(KRETS_ERR_INVALID_ARGUMENT, "null argument");
+  if (sweep_elem < 0 || sweep_elem >= c->ne) return fail(KRETS_ERR_ELEMENT_NOT_FOUND, "sweep element not found");
+  int kind = c->el[sweep_elem].kind;
+  if (kind != KRETS_ELEM_V && kind != KRETS_ELEM_I)
+    return fail(KRETS_ERR_INVALID_ELEMENT, "DC sweep element must be a voltage or current source");
+  double np_d = std::fabs((stop - start) / step);
+  if (!(np_d < 1e9)) return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid sweep range");
+  int np = (int)np_d + 1;  // dc.rs:153-154 (truncation)
+  if (n_points) *n_points = np;
+  if (np > max_points) return fail(KRETS_ERR_INVALID_ARGUMENT, "x_out too small for the sweep");
+  DevProgram *D;
+  krets_status s = get_program(c, MODE_DC, 0, 0, 0, &D);
+  if (s != KRETS_OK) return s;
+  CU(cudaEventRecord(c->ev[0], c->stream));
+  DevBuf tx;
+  void *dx;
+  s = dev_view(x_out, sizeof(double) * c->n * (size_t)np, false, c->stream, tx, &dx);
+  if (s) return s;
+  Lay L = layout_op(D->view);
+  int threads = plain_threads(D->view), grid;
+  size_t smem;
+  char *gws;
+  s = plan_launch(c, k_dc_sweep, L, threads, 1, grid, smem, gws);
+  if (s) return s;
+  CU(cudaEventRecord(c->ev[2], c->stream));
+  k_dc_sweep<<<1, threads, smem, c->stream>>>(D->view, c->cfg, L, gws, sweep_elem, start, step, np, (double *)dx,
+                                              c->d_small);
+  g_launches++;
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(c->ev[3], c->stream));
+  if (tx.p) CU(cudaMemcpyAsync(x_out, dx, sizeof(double) * c->n * (size_t)np, cudaMemcpyDeviceToHost, c->stream));
+  int h = 0;
+  CU(cudaMemcpyAsync(&h, c->d_small, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaEventRecord(c->ev[1], c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  cudaEventElapsedTime(&c->kernel_ms, c->ev[2], c->ev[3]);
+  cudaEventElapsedTime(&c->call_ms, c->ev[0], c->ev[1]);
+  return map_status(h, 1);
+}
+
+krets_status krets_batch_ac(krets_circuit *c, int32_t n_inst, const double *values, const double *freqs,
+                            int32_t n_freq, int32_t precision, double *x_out, int32_t *item_status) {
+  if (!c || !freqs || !x_out || n_inst <= 0 || n_freq <= 0) return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments");
+  std::vector<double> hf(n_freq);
+  if (is_device_ptr(freqs)) CU(cudaMemcpy(hf.data(), freqs, sizeof(double) * n_freq, cudaMemcpyDeviceToHost));
+  else memcpy(hf.data(), freqs, sizeof(double) * n_freq);
+  double lo = 1e300, hi = 0;
+  for (double f : hf) {
+    if (!(f > 0)) return fail(KRETS_ERR_INVALID_ARGUMENT, "batched AC frequencies must be > 0");
+    lo = std::min(lo, f);
+    hi = std::max(hi, f);
+  }
+  DevProgram *Ddc, *Dac;
+  krets_status s = get_program(c, MODE_DC, 0, 0, 0, &Ddc);
+  if (s != KRETS_OK) return s;
+  double frep = std::sqrt(lo * hi);
+  s = get_program(c, MODE_AC, 0, 0, frep, &Dac);
+  if (s != KRETS_OK) return s;
+  CU(cudaEventRecord(c->ev[0], c->stream));
+  DevBuf tv, tf, tx, top, ts;
+  void *dv, *df, *dx;
+  s = dev_view(values, sizeof(double) * c->ne * (size_t)n_inst, true, c->stream, tv, &dv);
+  if (s) return s;
+  s = dev_view(freqs, sizeof(double) * n_freq, true, c->stream, tf, &df);
+  if (s) return s;
+  size_t out_bytes = sizeof(double) * 2 * c->n * (size_t)n_freq * n_inst;
+  s = dev_view(x_out, out_bytes, false, c->stream, tx, &dx);
+  if (s) return s;
+  CU(cudaMalloc(&top.p, sizeof(double) * c->n * (size_t)n_inst));
+  size_t items = (size_t)n_inst * n_freq;
+  CU(cudaMalloc(&ts.p, sizeof(int) * (items + n_inst)));
+  int *d_item_st = (int *)ts.p, *d_op_st = d_item_st + items;
+  CU(cudaMemsetAsync(ts.p, 0, sizeof(int) * (items + n_inst), c->stream));
+  s = run_op(c, Ddc, n_inst, (const double *)dv, (double *)top.p, c->n, d_op_st, nullptr, 128);
+  if (s) return s;
+  bool mixed = precision == KRETS_PREC_MIXED;
+  Lay L = layout_ac(Dac->view, mixed);
+  int threads = 128, grid;
+  size_t smem;
+  char *gws;
+  auto kern = mixed ? k_ac_batch<1> : k_ac_batch<0>;
+  s = plan_launch(c, kern, L, threads, (int)std::min<size_t>(items, 1 << 30), grid, smem, gws);
+  if (s) return s;
+  int *queue = c->d_small + 8;
+  CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
+  CU(cudaEventRecord(c->ev[2], c->stream));
+  kern<<<grid, threads, smem, c->stream>>>(Dac->view, L, gws, (const double *)dv, (const double *)top.p, n_inst,
+                                           (const double *)df, n_freq, (double *)dx, d_item_st, queue);
+  g_launches++;
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(c->ev[3], c->stream));
+  if (tx.p) CU(cudaMemcpyAsync(x_out, dx, out_bytes, cudaMemcpyDeviceToHost, c->stream));
+  std::vector<int> st(items + n_inst);
+  CU(cudaMemcpyAsync(st.data(), d_item_st, sizeof(int) * (items + n_inst), cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaEventRecord(c->ev[1], c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  cudaEventElapsedTime(&c->kernel_ms, c->ev[2], c->ev[3]);
+  cudaEventElapsedTime(&c->call_ms, c->ev[0], c->ev[1]);
+  int any_op = 0, any = 0;
+  for (size_t i = 0; i < items; ++i) {
+    if (item_status) item_status[i] = st[i];
+    any |= st[i];
+  }
+  for (int i = 0; i < n_inst; ++i) any_op |= st[items + i];
+  if (any_op) return map_status(any_op, 0);
+  return map_status(any, 1);
+}
+
+krets_status krets_ac(krets_circuit *c, const double *freqs, int32_t n_freq, double *x_out, int32_t *n_kept) {
+  if (!c || (!freqs && n_freq > 0) || !x_out) return fail(KRETS_ERR_INVALID_ARGUMENT, "null argument");
+  std::vector<double> kept;
+  for (int i = 0; i < n_freq; ++i)
+    if (freqs[i] > 0.0) kept.push_back(freqs[i]);  // ac.rs:40-45
+  if (n_kept) *n_kept = (int)kept.size();
+  if (kept.empty()) {
+    // the reference still computes the operating point first (ac.rs:25)
+    std::vector<double> xop(c->n);
+    return krets_op(c, xop.data(), nullptr);
+  }
+  return krets_batch_ac(c, 1, nullptr, kept.data(), (int)kept.size(), KRETS_PREC_FP64, x_out, nullptr);
+}
+
+krets_status krets_tran(krets_circuit *c, double h, int32_t n_steps, int32_t method, int32_t source_lag,
+                        int32_t refactor_each_step, double *x_out) {
+  if (!c || !x_out || n_steps < 0 || !(h > 0)) return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments");
+  DevProgram *Ddc, *Dtr;
+  krets_status s = get_program(c, MODE_DC, 0, 0, 0, &Ddc);
+  if (s != KRETS_OK) return s;
+  s = get_program(c, MODE_TRAN, method, h, 0, &Dtr);
+  if (s != KRETS_OK) return s;
+  CU(cudaEventRecord(c->ev[0], c->stream));
+  size_t out_bytes = sizeof(double) * c->n * ((size_t)n_steps + 1);
+  DevBuf tx, stbuf;
+  void *dx;
+  s = dev_view(x_out, out_bytes, false, c->stream, tx, &dx);
+  if (s) return s;
+  const DevProg &P = Dtr->view;
+  size_t nd = 8 * (size_t)P.n + 3 * (size_t)P.ne + P.nnz_lu + 64;
+  CU(cudaMalloc(&stbuf.p, nd * sizeof(double)));
+  CU(cudaMemsetAsync(stbuf.p, 0, nd * sizeof(double), c->stream));
+  double *d = (double *)stbuf.p;
+  TranState st;
+  st.x = d; d += P.n;
+  st.prev = d; d += P.n;
+  st.guess = d; d += P.n;
+  st.b = d; d += P.n;
+  st.ca = d; d += P.ne;
+  st.cb = d; d += P.ne;
+  st.icap = d; d += P.ne;
+  st.lu = d; d += P.nnz_lu;
+  int *ints = (int *)d;
+  st.status = ints;
+  st.step = ints + 2;
+  st.factored = ints + 4;
+  int *op_status = ints + 6;
+  CU(cudaEventRecord(c->ev[2], c->stream));
+  s = run_op(c, Ddc, 1, nullptr, (double *)dx, c->n, op_status, nullptr, plain_threads(Ddc->view));
+  if (s) return s;
+  // TRAN state starts from the operating point (position space of the TRAN program)
+  k_gather<<<(P.n + 255) / 256, 256, 0, c->stream>>>(st.x, (const double *)dx, P.q, P.n);
+  g_launches++;
+  int threads = plain_threads(P);
+  if (n_steps > 0) {
+    // a CUDA graph of up to 256 step launches, replayed; each launch advances one step
+    int chunk = std::min(n_steps, 256);
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < chunk; ++i)
+      k_tran_step<<<1, threads, 0, c->stream>>>(P, c->cfg, st, h, method, source_lag, refactor_each_step, n_steps,
+                                               (double *)dx);
+    CU(cudaStreamEndCapture(c->stream, &graph));
+    CU(cudaGraphInstantiate(&exec, graph, 0));
+    int reps = (n_steps + chunk - 1) / chunk;
+    for (int r = 0; r < reps; ++r) CU(cudaGraphLaunch(exec, c->stream));
+    g_launches += (long long)reps * chunk;
+    CU(cudaStreamSynchronize(c->stream));
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+  }
+  CU(cudaEventRecord(c->ev[3], c->stream));
+  if (tx.p) CU(cudaMemcpyAsync(x_out, dx, out_bytes, cudaMemcpyDeviceToHost, c->stream));
+  int h2[8];
+  CU(cudaMemcpyAsync(h2, ints, sizeof h2, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaEventRecord(c->ev[1], c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  cudaEventElapsedTime(&c->kernel_ms, c->ev[2], c->ev[3]);
+  cudaEventElapsedTime(&c->call_ms, c->ev[0], c->ev[1]);
+  if (h2[6]) return map_status(h2[6], 0);
+  return map_status(h2[0], 1);
+}
+
+krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *values, double h, int32_t n_steps,
+                              int32_t method, int32_t source_lag, int32_t precision, double *x_out,
+                              int32_t *inst_status) {
+  if (!c || !x_out || n_inst <= 0 || n_steps < 0 || !(h > 0)) return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments");
+  DevProgram *Ddc, *Dtr;
+  krets_status s = get_program(c, MODE_DC, 0, 0, 0, &Ddc);
+  if (s != KRETS_OK) return s;
+  s = get_program(c, MODE_TRAN, method, h, 0, &Dtr);
+  if (s != KRETS_OK) return s;
+  CU(cudaEventRecord(c->ev[0], c->stream));
+  size_t stride = (size_t)c->n * ((size_t)n_steps + 1);
+  DevBuf tv, tx, ts, tfb;
+  void *dv, *dx;
+  s = dev_view(values, sizeof(double) * c->ne * (size_t)n_inst, true, c->stream, tv, &dv);
+  if (s) return s;
+  s = dev_view(x_out, sizeof(double) * stride * n_inst, false, c->stream, tx, &dx);
+  if (s) return s;
+  CU(cudaMalloc(&ts.p, sizeof(int) * 2 * (size_t)n_inst));
+  int *d_st = (int *)ts.p, *d_opst = d_st + n_inst;
+  CU(cudaMemsetAsync(ts.p, 0, sizeof(int) * 2 * (size_t)n_inst, c->stream));
+  s = run_op(c, Ddc, n_inst, (const double *)dv, (double *)dx, stride, d_opst, nullptr, 128);
+  if (s) return s;
+  bool mixed = precision == KRETS_PREC_MIXED;
+  const DevProg &P = Dtr->view;
+  Lay L = layout_tran(P, mixed);
+  int threads = 128, grid;
+  size_t smem;
+  char *gws;
+  auto kern = mixed ? k_tran_batch<1> : k_tran_batch<0>;
+  s = plan_launch(c, kern, L, threads, n_inst, grid, smem, gws);
+  if (s) return s;
+  double *fb = nullptr;
+  if (mixed) {
+    CU(cudaMalloc(&tfb.p, sizeof(double) * (size_t)P.nnz_lu * grid));
+    fb = (double *)tfb.p;
+  }
+  int *queue = c->d_small + 8;
+  int *d_fallbacks = c->d_small + 12;
+  CU(cudaMemsetAsync(c->d_small + 8, 0, 8 * sizeof(int), c->stream));
+  CU(cudaMemsetAsync(c->d_hist, 0, 8 * sizeof(unsigned long long), c->stream));
+  CU(cudaEventRecord(c->ev[2], c->stream));
+  kern<<<grid, threads, smem, c->stream>>>(P, c->cfg, L, gws, (const double *)dv, n_inst, h, n_steps, method,
+                                           source_lag, (double *)dx, d_st, queue, c->d_hist, d_fallbacks, fb);
+  g_launches++;
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(c->ev[3], c->stream));
+  if (tx.p) CU(cudaMemcpyAsync(x_out, dx, sizeof(double) * stride * n_inst, cudaMemcpyDeviceToHost, c->stream));
+  std::vector<int> st(2 * (size_t)n_inst);
+  CU(cudaMemcpyAsync(st.data(), ts.p, sizeof(int) * 2 * (size_t)n_inst, cudaMemcpyDeviceToHost, c->stream));
+  unsigned long long hist[8];
+  CU(cudaMemcpyAsync(hist, c->d_hist, sizeof hist, cudaMemcpyDeviceToHost, c->stream));
+  int fbk = 0;
+  CU(cudaMemcpyAsync(&fbk, d_fallbacks, sizeof fbk, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaEventRecord(c->ev[1], c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  cudaEventElapsedTime(&c->kernel_ms, c->ev[2], c->ev[3]);
+  cudaEventElapsedTime(&c->call_ms, c->ev[0], c->ev[1]);
+  for (int k = 0; k < 8; ++k) c->hist[k] = (long long)hist[k];
+  c->fallbacks = fbk;
+  int any = 0, any_op = 0;
+  for (int i = 0; i < n_inst; ++i) {
+    int v = st[i] | st[n_inst + i];
+    if (inst_status) inst_status[i] = v;
+    any |= st[i];
+    any_op |= st[n_inst + i];
+  }
+  if (any_op) return map_status(any_op, 0);
+  return map_status(any, 1);
+}
+
+const char *krets_status_string(krets_status s) {
+  switch (s) {
+    case KRETS_OK: return "ok";
+    case KRETS_ERR_ELEMENT_NOT_FOUND: return "element not found in the netlist";
+    case KRETS_ERR_MAX_ITERATIONS: return "maximum iterations exceeded";
+    case KRETS_ERR_INVALID_ELEMENT: return "invalid element format";
+    case KRETS_ERR_UNEXPECTED: return "unexpected error";
+    case KRETS_ERR_DECOMPOSITION_FAILED: return "decomposition failed";
+    case KRETS_ERR_MATRIX_BUILD: return "matrix build failed";
+    case KRETS_ERR_MATRIX_DECOMPOSITION: return "matrix decomposition failed";
+    case KRETS_ERR_NOT_IMPLEMENTED: return "not implemented in the reference";
+    case KRETS_ERR_TIMEOUT: return "device wait timed out";
+    case KRETS_ERR_CUDA: return "CUDA error";
+    case KRETS_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case KRETS_ERR_OUT_OF_MEMORY: return "out of memory";
+    case KRETS_ERR_PIVOT_UNSTABLE: return "pivot unstable / refinement stalled";
+  }
+  return "unknown status";
+}
+
+const char *krets_last_error_message(void) { return g_last_error.c_str(); }
+
+krets_status krets_last_timing(const krets_circuit *c, float *kernel_ms, float *call_ms) {
+  if (!c) return fail(KRETS_ERR_INVALID_ARGUMENT, "null circuit");
+  if (kernel_ms) *kernel_ms = c->kernel_ms;
+  if (call_ms) *call_ms = c->call_ms;
+  return KRETS_OK;
+}
+
+int64_t krets_launch_count(void) { return g_launches.load(); }
+
+krets_status krets_last_refine_stats(const krets_circuit *c, int64_t histogram[8], int32_t *fallbacks) {
+  if (!c) return fail(KRETS_ERR_INVALID_ARGUMENT, "null circuit");
+  if (histogram)
+    for (int k = 0; k < 8; ++k) histogram[k] = c->hist[k];
+  if (fallbacks) *fallbacks = c->fallbacks;
+  return KRETS_OK;
+}
+
+krets_status krets_device_alloc(size_t bytes, void **ptr) {
+  if (!ptr) return fail(KRETS_ERR_INVALID_ARGUMENT, "null pointer");
+  cudaError_t e = cudaMalloc(ptr, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(e == cudaErrorMemoryAllocation ? KRETS_ERR_OUT_OF_MEMORY : KRETS_ERR_CUDA, cudaGetErrorString(e));
+  }
+  return KRETS_OK;
+}
+
+krets_status krets_device_free(void *ptr) {
+  CU(cudaFree(ptr));
+  return KRETS_OK;
+}
+
+krets_status krets_memcpy_h2d(void *dst, const void *src, size_t bytes) {
+  CU(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+  return KRETS_OK;
+}
+
+krets_status krets_memcpy_d2h(void *dst, const void *src, size_t bytes) {
+  CU(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+  return KRETS_OK;
+}
+
+krets_status krets_flush_l2(krets_circuit *c) {
+  if (!c) return fail(KRETS_ERR_INVALID_ARGUMENT, "null circuit");
+  const size_t n = (size_t)64 << 20;  // 512 MB of doubles, several times the L2
+  if (!c->l2buf) CU(cudaMalloc(&c->l2buf, n * sizeof(double)));
+  k_fill<<<4 * device_sm_count(), 256, 0, c->stream>>>((double *)c->l2buf, n, 1.0);
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(c->stream));
+  return KRETS_OK;
+}
+
+krets_status krets_device_synchronize(void) {
+  CU(cudaDeviceSynchronize());
+  return KRETS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,344 @@
+// Device engine: the per-instance MNA operations, written once and used by every kernel
+// (plain single-instance form and batched persistent forms).
+//
+// One CTA processes one instance.  All operations walk the static program built by the
+// host symbolic pass (symbolic.cpp):
+//   stamp   - deterministic segmented sums of element contributions into each matrix /
+//             rhs entry, in the reference's emission order (solver.rs:59-70 semantics,
+//             no atomics)
+//   factor  - up-looking (IKJ) LU, rows of one level in parallel, static pivots
+//   lsolve  - unit-lower solve, level by level
+//   usolve  - upper solve, level by level (reverse dependency levels)
+// Arrays passed in may live in shared or global memory.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "krets_gpu.h"
+
+namespace krets {
+
+// ------------------------------------------------------------------ complex scalar
+template <typename R>
+struct cx {
+  R re, im;
+  __host__ __device__ cx() : re(0), im(0) {}
+  __host__ __device__ cx(R r) : re(r), im(0) {}
+  __host__ __device__ cx(R r, R i) : re(r), im(i) {}
+  template <typename S>
+  __host__ __device__ explicit cx(const cx<S> &o) : re((R)o.re), im((R)o.im) {}
+};
+template <typename R> __device__ __forceinline__ cx<R> operator+(cx<R> a, cx<R> b) { return {a.re + b.re, a.im + b.im}; }
+template <typename R> __device__ __forceinline__ cx<R> operator-(cx<R> a, cx<R> b) { return {a.re - b.re, a.im - b.im}; }
+template <typename R> __device__ __forceinline__ cx<R> operator-(cx<R> a) { return {-a.re, -a.im}; }
+template <typename R> __device__ __forceinline__ cx<R> operator*(cx<R> a, cx<R> b) {
+  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <typename R> __device__ __forceinline__ cx<R> operator/(cx<R> a, cx<R> b) {
+  // Smith's algorithm (robust to large |b| components)
+  if (fabs(b.re) >= fabs(b.im)) {
+    R r = b.im / b.re, d = b.re + b.im * r;
+    return {(a.re + a.im * r) / d, (a.im - a.re * r) / d};
+  }
+  R r = b.re / b.im, d = b.re * r + b.im;
+  return {(a.re * r + a.im) / d, (a.im * r - a.re) / d};
+}
+
+template <typename T> struct scal;
+template <> struct scal<double> {
+  using real = double;
+  __device__ static double mag(double x) { return fabs(x); }
+  __device__ static bool finite(double x) { return isfinite(x); }
+  __device__ static double neg(double x) { return -x; }
+};
+template <> struct scal<float> {
+  using real = float;
+  __device__ static float mag(float x) { return fabsf(x); }
+  __device__ static bool finite(float x) { return isfinite(x); }
+};
+template <> struct scal<cx<double>> {
+  using real = double;
+  __device__ static double mag(cx<double> x) { return hypot(x.re, x.im); }
+  __device__ static bool finite(cx<double> x) { return isfinite(x.re) && isfinite(x.im); }
+};
+template <> struct scal<cx<float>> {
+  using real = float;
+  __device__ static float mag(cx<float> x) { return hypotf(x.re, x.im); }
+  __device__ static bool finite(cx<float> x) { return isfinite(x.re) && isfinite(x.im); }
+};
+
+// ------------------------------------------------------------------ program view
+struct DevProg {
+  int n, ne, nnz_a, nnz_lu, nlev, nulev, mode, method;
+  const int *q;          // [n]  position -> unknown
+  const int *lu_rowptr;  // [n+1]
+  const int *lu_col;     // [nnz_lu]
+  const int *lu_diag;    // [n]
+  const int *lu_src;     // [nnz_lu] A entry feeding this slot, or -1 (fill)
+  const int *a_rowptr;   // [n+1]
+  const int *a_col;      // [nnz_a]
+  const int *a_cptr;     // [nnz_a+1]
+  const int *a_contrib;  // packed elem<<2 | unit<<1 | neg
+  const int *b_cptr;     // [n+1]
+  const int *b_contrib;  // packed elem<<1 | neg
+  const int *piv_ptr;    // [n+1]
+  const int4 *piv;       // {slot, j, upd_begin, upd_end}
+  const int2 *upd;       // {dst, src}
+  const int *lev_ptr, *lev_rows, *ulev_ptr, *ulev_rows;
+  const int4 *el_pos;    // p, m, b, g in position space
+  const int *is_cur;     // [n] 1 when the unknown at this position is a branch current
+  const krets_element *el;
+  int nonlinear;         // any diode / MOSFET / BJT among the stamped elements
+};
+
+// status bits written by the engine
+#define KS_SINGULAR 1
+#define KS_MAXITER 2
+#define KS_NONFINITE 4
+#define KS_NOTIMPL 8
+#define KS_STALL 16
+#define KS_GROWTH 32
+
+static constexpr double kPiD = 3.14159265358979323846;
+static constexpr double kVtD = 1.380649e-23 * 300.0 / 1.602176634e-19;
+static constexpr double kDblMax = 1.7976931348623157e308;
+
+// ------------------------------------------------------------------ waveforms
+// Pulse and sine sources, voltage_source.rs:52-93 (same operation order; fmod and the
+// divisions are IEEE-exact, so the pulse value is bit-identical to the reference's).
+__device__ __forceinline__ double wave_value(const krets_element &E, double value, double t) {
+  if (E.wave == KRETS_WAVE_PULSE) {
+    const double *w = E.wp;
+    double v1 = w[0], v2 = w[1], td = w[2], tr = w[3], tf = w[4], pw = w[5], per = w[6];
+    if (t < td) return v1;
+    double tt = fmod(t - td, per);
+    if (tt < tr) return v1 + (v2 - v1) * (tt / tr);
+    if (tt < tr + pw) return v2;
+    if (tt < tr + pw + tf) return v2 + (v1 - v2) * ((tt - tr - pw) / tf);
+    return v1;
+  }
+  if (E.wave == KRETS_WAVE_SIN) {
+    const double *w = E.wp;
+    if (t < w[3]) return w[0];
+    double omega = 2.0 * kPiD * w[2];
+    double ph = w[5] * (kPiD / 180.0);
+    double tt = t - w[3];
+    return w[0] + w[1] * exp(-w[4] * tt) * sin(omega * tt + ph);
+  }
+  return value;
+}
+
+// Diode linearisation (diode.rs:26-70): V(+) defaults to 0.5 V and V(-) to 0 when the
+// solution map lacks them (empty map on the first OP iteration, or a ground terminal).
+__device__ __forceinline__ void diode_lin(const krets_element &E, double is, int4 pos, const double *guess,
+                                          bool empty, double &g, double &ieq) {
+  double vp = (!empty && pos.x >= 0) ? guess[pos.x] : 0.5;
+  double vm = (!empty && pos.y >= 0) ? guess[pos.y] : 0.0;
+  double vd = vp - vm;
+  double n = E.wp[0];
+  double vc = n * kVtD * log(kDblMax * n * kVtD / is);
+  double vl = vd;  // f64::clamp(-vc, vc); NaN stays NaN
+  if (vd < -vc) vl = -vc;
+  if (vd > vc) vl = vc;
+  double nvt = n * kVtD;
+  g = (is / nvt) * exp(vl / nvt);
+  double cur = is * (exp(vl / nvt) - 1.0);
+  ieq = cur - g * vd;
+}
+
+struct PassCtx {
+  int mode, method;
+  double h, freq;
+  double t_src;          // time at which transient sources are evaluated
+  const double *guess;   // Newton guess (position space)
+  bool guess_empty;      // the reference's map is empty (first OP iteration)
+  const double *prev;    // previous time step (position space)
+  const double *icap;    // TR capacitor currents at t_n, per element
+};
+
+// Per-element coefficients of one stamping pass: ca = matrix coefficient (real part in
+// ca_re, imaginary in ca_im), cb = rhs coefficient.  Expressions and operation order follow
+// stampable.rs so the summed entries match the reference's bit for bit (up to exp/sin).
+__device__ __forceinline__ void elem_coefs(const krets_element &E, int e, int4 pos, double val,
+                                           const PassCtx &c, double &ca_re, double &ca_im, double &cb,
+                                           int &err) {
+  ca_re = 0.0;
+  ca_im = 0.0;
+  cb = 0.0;
+  switch (E.kind) {
+    case KRETS_ELEM_R:
+      ca_re = (E.flags & KRETS_FLAG_G2) ? val : 1.0 / val;
+      break;
+    case KRETS_ELEM_C:
+      if (c.mode == 1) {
+        ca_im = 2.0 * kPiD * c.freq * val;
+      } else if (c.mode == 2) {
+        double vp = pos.x >= 0 ? c.prev[pos.x] : 0.0, vm = pos.y >= 0 ? c.prev[pos.y] : 0.0;
+        double vprev = vp - vm;
+        if (c.method == KRETS_METHOD_TR) {
+          ca_re = 2.0 * val / c.h;
+          cb = ca_re * vprev + c.icap[e];
+        } else {
+          ca_re = val / c.h;
+          double ieq = -(val / c.h) * vprev;
+          cb = -ieq;
+        }
+      }
+      break;
+    case KRETS_ELEM_L:
+      if (c.mode == 1) {
+        ca_im = 2.0 * kPiD * c.freq * val;
+      } else if (c.mode == 2) {
+        double iprev = pos.z >= 0 ? c.prev[pos.z] : 0.0;
+        if (c.method == KRETS_METHOD_TR) {
+          double lh = 2.0 * val / c.h;
+          double vl = (pos.x >= 0 ? c.prev[pos.x] : 0.0) - (pos.y >= 0 ? c.prev[pos.y] : 0.0);
+          ca_re = lh;
+          cb = -lh * iprev - vl;
+        } else {
+          ca_re = val / c.h;
+          cb = -(val / c.h) * iprev;
+        }
+      }
+      break;
+    case KRETS_ELEM_V:
+      cb = c.mode == 0 ? val : (c.mode == 1 ? E.ac : wave_value(E, val, c.t_src));
+      break;
+    case KRETS_ELEM_I:
+      cb = val;
+      break;
+    case KRETS_ELEM_D: {
+      double g, ieq;
+      diode_lin(E, val, pos, c.guess, c.guess_empty, g, ieq);
+      ca_re = g;
+      cb = ieq;
+      break;
+    }
+    case KRETS_ELEM_M:
+      if (c.mode == 1) err |= KS_NOTIMPL;
+      break;
+    default:
+      err |= KS_NOTIMPL;
+  }
+}
+
+// ------------------------------------------------------------------ block helpers
+__device__ __forceinline__ double block_max(double v, double *red) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
+    if (threadIdx.x == 0) red[0] = t;
+  }
+  __syncthreads();
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// ------------------------------------------------------------------ stamping
+// Sum of one A entry's contributions (emission order).
+template <typename T>
+__device__ __forceinline__ T sum_entry(const DevProg &P, int t, const double *ca_re, const double *ca_im);
+
+template <>
+__device__ __forceinline__ double sum_entry<double>(const DevProg &P, int t, const double *ca_re, const double *) {
+  double s = 0.0;
+  for (int u = P.a_cptr[t]; u < P.a_cptr[t + 1]; ++u) {
+    int code = P.a_contrib[u];
+    double v = (code & 2) ? 1.0 : ca_re[code >> 2];
+    s += (code & 1) ? -v : v;
+  }
+  return s;
+}
+
+template <>
+__device__ __forceinline__ cx<double> sum_entry<cx<double>>(const DevProg &P, int t, const double *ca_re,
+                                                            const double *ca_im) {
+  double sr = 0.0, si = 0.0;
+  for (int u = P.a_cptr[t]; u < P.a_cptr[t + 1]; ++u) {
+    int code = P.a_contrib[u];
+    double vr = (code & 2) ? 1.0 : ca_re[code >> 2];
+    double vi = (code & 2) ? 0.0 : ca_im[code >> 2];
+    if (code & 1) { vr = -vr; vi = -vi; }
+    sr += vr;
+    si += vi;
+  }
+  return cx<double>(sr, si);
+}
+
+// rhs row k (position space)
+__device__ __forceinline__ double sum_rhs(const DevProg &P, int k, const double *cb) {
+  double s = 0.0;
+  for (int u = P.b_cptr[k]; u < P.b_cptr[k + 1]; ++u) {
+    int code = P.b_contrib[u];
+    double v = cb[code >> 1];
+    s += (code & 1) ? -v : v;
+  }
+  return s;
+}
+
+// ------------------------------------------------------------------ factor / solves
+// In-place static-pivot LU of lu[] (values in position space).  Returns status bits.
+// Status bits are OR-ed into *status (shared or global) by the threads that see them.
+template <typename T>
+__device__ void factor(const DevProg &P, T *lu, int *status) {
+  int bad = 0;
+  for (int l = 0; l < P.nlev; ++l) {
+    int r0 = P.lev_ptr[l], r1 = P.lev_ptr[l + 1];
+    for (int t = r0 + threadIdx.x; t < r1; t += blockDim.x) {
+      int k = P.lev_rows[t];
+      for (int pi = P.piv_ptr[k]; pi < P.piv_ptr[k + 1]; ++pi) {
+        int4 pv = P.piv[pi];
+        T l_kj = lu[pv.x] / lu[P.lu_diag[pv.y]];
+        lu[pv.x] = l_kj;
+        for (int u = pv.z; u < pv.w; ++u) {
+          int2 d = P.upd[u];
+          lu[d.x] = lu[d.x] - l_kj * lu[d.y];
+        }
+      }
+      T dk = lu[P.lu_diag[k]];
+      if (!(scal<T>::mag(dk) > 0)) bad |= KS_SINGULAR;
+      else if (!scal<T>::finite(dk)) bad |= KS_NONFINITE;
+    }
+    __syncthreads();
+  }
+  if (bad) atomicOr(status, bad);
+  __syncthreads();
+}
+
+template <typename T, typename V>
+__device__ void lsolve(const DevProg &P, const T *lu, V *y) {
+  for (int l = 1; l < P.nlev; ++l) {  // level 0 rows have no L entries
+    int r0 = P.lev_ptr[l], r1 = P.lev_ptr[l + 1];
+    for (int t = r0 + threadIdx.x; t < r1; t += blockDim.x) {
+      int k = P.lev_rows[t];
+      V s = y[k];
+      for (int u = P.lu_rowptr[k]; u < P.lu_diag[k]; ++u) s = s - V(lu[u]) * y[P.lu_col[u]];
+      y[k] = s;
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, typename V>
+__device__ void usolve(const DevProg &P, const T *lu, V *y) {
+  for (int l = 0; l < P.nulev; ++l) {
+    int r0 = P.ulev_ptr[l], r1 = P.ulev_ptr[l + 1];
+    for (int t = r0 + threadIdx.x; t < r1; t += blockDim.x) {
+      int k = P.ulev_rows[t];
+      V s = y[k];
+      int dg = P.lu_diag[k];
+      for (int u = dg + 1; u < P.lu_rowptr[k + 1]; ++u) s = s - V(lu[u]) * y[P.lu_col[u]];
+      y[k] = s / V(lu[dg]);
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace krets

@@ -1,0 +1,658 @@
+// Host symbolic pass (see symbolic.h).
+//
+// Stamp emission follows crates/krets-solver/src/stampable.rs element by element and
+// entry by entry, so that the device's segmented sums add duplicate (row, col) entries in
+// the same order as the reference's HashMap `+=` (crates/krets-solver/src/solver.rs:59-70).
+#include "symbolic.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <numeric>
+#include <queue>
+#include <unordered_map>
+
+namespace krets {
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kVt = 1.380649e-23 * 300.0 / 1.602176634e-19;
+
+struct MEntry { int r, c, code; };  // code = packed contribution (pack_a)
+struct BEntry { int r, code; };     // code = packed contribution (pack_b)
+
+// Emit the matrix and rhs stamp entries of element e for the mode, in the reference's
+// order.  Returns false for stamps the reference leaves as todo!().
+bool emit(const krets_element &x, int e, int mode, std::vector<MEntry> &M, std::vector<BEntry> &B) {
+  const int ip = x.p, im = x.m, ic = x.b;
+  auto A = [&](int r, int c, bool unit, bool neg) { M.push_back({r, c, pack_a(e, unit, neg)}); };
+  auto R = [&](int r, bool neg) { B.push_back({r, pack_b(e, neg)}); };
+  switch (x.kind) {
+    case KRETS_ELEM_R:  // stampable.rs:203-246
+      if (x.flags & KRETS_FLAG_G2) {
+        if (ip >= 0 && ic >= 0) { A(ip, ic, true, false); A(ic, ip, true, false); }
+        if (im >= 0 && ic >= 0) { A(im, ic, true, true); A(ic, im, true, true); }
+        if (ic >= 0) A(ic, ic, false, true);  // -R
+      } else {
+        if (ip >= 0) A(ip, ip, false, false);
+        if (im >= 0) A(im, im, false, false);
+        if (ip >= 0 && im >= 0) { A(ip, im, false, true); A(im, ip, false, true); }
+      }
+      return true;
+    case KRETS_ELEM_C:  // stampable.rs:360-506
+      if (mode == MODE_DC) return true;
+      if (mode == MODE_AC && (x.flags & KRETS_FLAG_G2)) {
+        if (ip >= 0 && ic >= 0) A(ic, ip, false, true);
+        if (im >= 0 && ic >= 0) A(ic, im, false, false);
+        if (ic >= 0) A(ic, ic, true, false);
+        return true;
+      }
+      if (ip >= 0) A(ip, ip, false, false);
+      if (im >= 0) A(im, im, false, false);
+      if (ip >= 0 && im >= 0) { A(ip, im, false, true); A(im, ip, false, true); }
+      if (mode == MODE_TRAN) {
+        // BE: (p, -ieq), (m, ieq) with ieq = -(C/h) v_prev.  TR: (p, ihist), (m, -ihist).
+        // The per-pass rhs coefficient is -ieq (BE) or ihist (TR): + at p, - at m.
+        if (ip >= 0) R(ip, false);
+        if (im >= 0) R(im, true);
+      }
+      return true;
+    case KRETS_ELEM_I:  // stampable.rs:508-585
+      if (mode == MODE_AC) {
+        if (ip >= 0 && ic >= 0) A(ip, ic, true, false);
+        if (im >= 0 && ic >= 0) A(im, ic, true, true);
+      } else {
+        if (ic >= 0) A(ic, ic, true, false);
+        if (ip >= 0 && ic >= 0) A(ip, ic, true, false);
+        if (im >= 0 && ic >= 0) A(im, ic, true, true);
+      }
+      if (ic >= 0) R(ic, false);
+      return true;
+    case KRETS_ELEM_D:  // stampable.rs:587-674
+      if (ip >= 0) A(ip, ip, false, false);
+      if (im >= 0) A(im, im, false, false);
+      if (ip >= 0 && im >= 0) { A(ip, im, false, true); A(im, ip, false, true); }
+      if (mode != MODE_AC) {
+        // (p, -ieq), (m, ieq): per-pass rhs coefficient = ieq
+        if (ip >= 0) R(ip, true);
+        if (im >= 0) R(im, false);
+      }
+      return true;
+    case KRETS_ELEM_L:  // stampable.rs:676-817
+      if (mode == MODE_TRAN) {
+        if (ic >= 0) A(ic, ic, false, true);
+        if (ip >= 0 && ic >= 0) { A(ip, ic, true, false); A(ic, ip, true, false); }
+        if (im >= 0 && ic >= 0) { A(im, ic, true, true); A(ic, im, true, true); }
+        if (ic >= 0) R(ic, false);
+        return true;
+      }
+      if (ip >= 0 && ic >= 0) A(ip, ic, true, false);
+      if (im >= 0 && ic >= 0) A(im, ic, true, true);
+      if (ip >= 0 && ic >= 0) A(ic, ip, true, false);
+      if (im >= 0 && ic >= 0) A(ic, im, true, true);
+      if (mode == MODE_AC && ic >= 0) A(ic, ic, false, true);
+      return true;
+    case KRETS_ELEM_V:  // stampable.rs:960-1050
+      if (ip >= 0 && ic >= 0) { A(ip, ic, true, false); A(ic, ip, true, false); }
+      if (im >= 0 && ic >= 0) { A(im, ic, true, true); A(ic, im, true, true); }
+      if (ic >= 0) R(ic, false);
+      return true;
+    case KRETS_ELEM_M:  // stampable.rs:819-922: index lookups by bare node name never match
+      return mode != MODE_AC;
+    default:
+      return false;
+  }
+}
+
+// Representative value of an element's matrix coefficient (for pivot selection only).
+std::complex<double> rep_coef(const krets_element &x, int mode, int method, double h, double f) {
+  switch (x.kind) {
+    case KRETS_ELEM_R:
+      return (x.flags & KRETS_FLAG_G2) ? x.value : 1.0 / x.value;
+    case KRETS_ELEM_C:
+      if (mode == MODE_AC) return std::complex<double>(0.0, 2.0 * kPi * f * x.value);
+      return (method == KRETS_METHOD_TR ? 2.0 : 1.0) * x.value / h;
+    case KRETS_ELEM_L:
+      if (mode == MODE_AC) return std::complex<double>(0.0, 2.0 * kPi * f * x.value);
+      return (method == KRETS_METHOD_TR ? 2.0 : 1.0) * x.value / h;
+    case KRETS_ELEM_D: {
+      double n = x.wp[0] > 0 ? x.wp[0] : 1.0;
+      return (x.value / (n * kVt)) * std::exp(std::min(0.5 / (n * kVt), 700.0));
+    }
+    default:
+      return 1.0;
+  }
+}
+
+// ------------------------------------------------------------ Gilbert-Peierls LU
+// Left-looking LU with threshold partial pivoting (diagonal preferred), used on the
+// representative values to fix the pivot sequence and the static fill pattern.
+struct GP {
+  int n;
+  std::vector<int> lp, li, up, ui, pinv;
+  double min_ratio = 1.0;
+};
+
+template <typename T>
+int gp_factor(int n, const std::vector<int> &ap, const std::vector<int> &ai, const std::vector<T> &ax,
+              const std::vector<int> &q, double tau, GP &F) {
+  F.n = n;
+  F.lp.assign(n + 1, 0);
+  F.up.assign(n + 1, 0);
+  F.li.clear();
+  F.ui.clear();
+  F.pinv.assign(n, -1);
+  std::vector<T> lx, xv(n, T(0));
+  std::vector<int> mark(n, -1), stack(n), pstack(n), reach(n);
+  for (int k = 0; k < n; ++k) {
+    F.lp[k] = (int)F.li.size();
+    F.up[k] = (int)F.ui.size();
+    int col = q[k];
+    int top = n;
+    for (int p = ap[col]; p < ap[col + 1]; ++p) {
+      int r0 = ai[p];
+      if (mark[r0] == k) continue;
+      int head = 0;
+      stack[0] = r0;
+      while (head >= 0) {
+        int j = stack[head];
+        int jp = F.pinv[j];
+        if (mark[j] != k) {
+          mark[j] = k;
+          pstack[head] = jp < 0 ? 0 : F.lp[jp];
+        }
+        bool done = true;
+        if (jp >= 0) {
+          int end = F.lp[jp + 1];
+          for (int pp = pstack[head]; pp < end; ++pp) {
+            int i = F.li[pp];
+            if (mark[i] == k) continue;
+            pstack[head] = pp + 1;
+            stack[++head] = i;
+            done = false;
+            break;
+          }
+        }
+        if (done) {
+          --head;
+          reach[--top] = j;
+        }
+      }
+    }
+    for (int p = top; p < n; ++p) xv[reach[p]] = T(0);
+    for (int p = ap[col]; p < ap[col + 1]; ++p) xv[ai[p]] += ax[p];
+    for (int p = top; p < n; ++p) {
+      int j = reach[p];
+      int jp = F.pinv[j];
+      if (jp < 0) continue;
+      T xj = xv[j];
+      for (int pp = F.lp[jp]; pp < F.lp[jp + 1]; ++pp) xv[F.li[pp]] -= lx[pp] * xj;
+    }
+    int ipiv = -1;
+    double amax = -1.0;
+    for (int p = top; p < n; ++p) {
+      int i = reach[p];
+      if (F.pinv[i] < 0) {
+        double a = std::abs(xv[i]);
+        if (a > amax) { amax = a; ipiv = i; }
+      } else {
+        F.ui.push_back(F.pinv[i]);
+      }
+    }
+    if (ipiv < 0) return KRETS_ERR_DECOMPOSITION_FAILED;  // structurally singular column
+    if (!(amax > 0.0) || !std::isfinite(amax)) return KRETS_ERR_DECOMPOSITION_FAILED;
+    // diagonal preference: keep the row paired with this column if it is large enough
+    if (F.pinv[col] < 0 && mark[col] == k && std::abs(xv[col]) >= tau * amax) ipiv = col;
+    F.min_ratio = std::min(F.min_ratio, std::abs(xv[ipiv]) / amax);
+    T piv = xv[ipiv];
+    F.ui.push_back(k);
+    F.pinv[ipiv] = k;
+    for (int p = top; p < n; ++p) {
+      int i = reach[p];
+      if (F.pinv[i] < 0) {
+        F.li.push_back(i);
+        lx.push_back(xv[i] / piv);
+      }
+      xv[i] = T(0);
+    }
+  }
+  F.lp[n] = (int)F.li.size();
+  F.up[n] = (int)F.ui.size();
+  return KRETS_OK;
+}
+
+uint64_t fnv1a(uint64_t h, uint64_t v) {
+  for (int k = 0; k < 8; ++k) {
+    h ^= (v >> (8 * k)) & 0xff;
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ orderings
+std::vector<int> order_min_degree(int n, const std::vector<std::vector<int>> &adj0) {
+  std::vector<std::vector<int>> adj = adj0;
+  std::vector<char> gone(n, 0);
+  std::vector<int> order;
+  order.reserve(n);
+  for (int step = 0; step < n; ++step) {
+    int best = -1;
+    size_t bd = 0;
+    for (int v = 0; v < n; ++v)
+      if (!gone[v] && (best < 0 || adj[v].size() < bd)) { best = v; bd = adj[v].size(); }
+    gone[best] = 1;
+    order.push_back(best);
+    const std::vector<int> nb = adj[best];
+    for (int u : nb) {
+      std::vector<int> merged;
+      merged.reserve(adj[u].size() + nb.size());
+      std::set_union(adj[u].begin(), adj[u].end(), nb.begin(), nb.end(), std::back_inserter(merged));
+      merged.erase(std::remove_if(merged.begin(), merged.end(), [&](int w) { return w == u || w == best; }),
+                   merged.end());
+      adj[u].swap(merged);
+    }
+    adj[best].clear();
+  }
+  return order;
+}
+
+std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<int>> &adj) {
+  std::vector<int> order;
+  order.reserve(n);
+  std::vector<int> in_set(n, -1), level(n, -1);
+  int stamp = 0;
+  const int kLeaf = 4;
+  // explicit stack of vertex sets to avoid deep recursion
+  std::function<void(std::vector<int> &)> nd = [&](std::vector<int> &V) {
+    if ((int)V.size() <= kLeaf) {
+      std::sort(V.begin(), V.end());
+      order.insert(order.end(), V.begin(), V.end());
+      return;
+    }
+    int id = ++stamp;
+    for (int v : V) in_set[v] = id;
+    // connected components of V
+    std::vector<std::vector<int>> comps;
+    int cid = ++stamp;
+    for (int s : V) {
+      if (in_set[s] != id) continue;
+      std::vector<int> comp{s};
+      in_set[s] = cid;
+      for (size_t h = 0; h < comp.size(); ++h)
+        for (int w : adj[comp[h]])
+          if (in_set[w] == id) { in_set[w] = cid; comp.push_back(w); }
+      comps.push_back(std::move(comp));
+    }
+    for (auto &C : comps) {
+      if ((int)C.size() <= kLeaf) {
+        std::sort(C.begin(), C.end());
+        order.insert(order.end(), C.begin(), C.end());
+        continue;
+      }
+      int mid = ++stamp;
+      for (int v : C) in_set[v] = mid;
+      auto bfs = [&](int root, std::vector<std::vector<int>> &levels) {
+        levels.clear();
+        int bid = ++stamp;
+        std::vector<int> cur{root};
+        in_set[root] = bid;
+        while (!cur.empty()) {
+          levels.push_back(cur);
+          std::vector<int> nxt;
+          for (int v : cur)
+            for (int w : adj[v])
+              if (in_set[w] == mid) { in_set[w] = bid; nxt.push_back(w); }
+          cur.swap(nxt);
+        }
+        for (int v : C) in_set[v] = mid;
+      };
+      std::vector<std::vector<int>> levels;
+      int root = *std::min_element(C.begin(), C.end());
+      for (int rep = 0; rep < 3; ++rep) {  // pseudo-peripheral root
+        bfs(root, levels);
+        const auto &last = levels.back();
+        int cand = last[0];
+        for (int v : last)
+          if (adj[v].size() < adj[cand].size()) cand = v;
+        if (cand == root) break;
+        root = cand;
+      }
+      bfs(root, levels);
+      int L = (int)levels.size();
+      if (L < 3) {
+        std::sort(C.begin(), C.end());
+        order.insert(order.end(), C.begin(), C.end());
+        continue;
+      }
+      // separator: smallest level in the middle third (by vertex count)
+      std::vector<int> cum(L + 1, 0);
+      for (int l = 0; l < L; ++l) cum[l + 1] = cum[l] + (int)levels[l].size();
+      int total = cum[L], best = -1;
+      for (int l = 1; l < L - 1; ++l) {
+        if (cum[l] < total / 4 || cum[l + 1] > total - total / 4) continue;
+        if (best < 0 || levels[l].size() < levels[best].size()) best = l;
+      }
+      if (best < 0) {
+        best = 1;
+        while (best < L - 2 && cum[best + 1] < total / 2) ++best;
+      }
+      std::vector<int> A, B;
+      for (int l = 0; l < best; ++l) A.insert(A.end(), levels[l].begin(), levels[l].end());
+      for (int l = best + 1; l < L; ++l) B.insert(B.end(), levels[l].begin(), levels[l].end());
+      std::vector<int> S = levels[best];
+      nd(A);
+      nd(B);
+      std::sort(S.begin(), S.end());
+      order.insert(order.end(), S.begin(), S.end());
+    }
+  };
+  std::vector<int> all(n);
+  std::iota(all.begin(), all.end(), 0);
+  nd(all);
+  return order;
+}
+
+// ------------------------------------------------------------------ program
+static int build_with_order(const krets_element *el, int ne, int n, int mode, int method, double h, double f,
+                            const std::vector<MEntry> &M, const std::vector<BEntry> &B,
+                            const std::vector<int> &q, Program &P, std::string &msg) {
+  P = Program();
+  P.mode = mode;
+  P.method = method;
+  P.n = n;
+  P.ne = ne;
+  // ---- representative numeric matrix (CSC, summed), for pivot selection
+  std::vector<std::complex<double>> coef(ne);
+  for (int e = 0; e < ne; ++e) coef[e] = rep_coef(el[e], mode, method, h, f);
+  std::vector<std::pair<long long, std::complex<double>>> ent;
+  ent.reserve(M.size());
+  for (auto &m : M) {
+    int e = m.code >> 2;
+    std::complex<double> v = (m.code & 2) ? std::complex<double>(1.0) : coef[e];
+    if (m.code & 1) v = -v;
+    ent.push_back({(long long)m.c * n + m.r, v});
+  }
+  std::stable_sort(ent.begin(), ent.end(), [](auto &a, auto &b) { return a.first < b.first; });
+  std::vector<int> ap(n + 1, 0), ai;
+  std::vector<std::complex<double>> axz;
+  for (size_t k = 0; k < ent.size();) {
+    size_t k2 = k;
+    std::complex<double> s = 0;
+    while (k2 < ent.size() && ent[k2].first == ent[k].first) s += ent[k2++].second;
+    int c = (int)(ent[k].first / n), r = (int)(ent[k].first % n);
+    ai.push_back(r);
+    axz.push_back(s);
+    ap[c + 1]++;
+    k = k2;
+  }
+  for (int c = 0; c < n; ++c) ap[c + 1] += ap[c];
+  GP F;
+  int st;
+  const double tau = 1e-3;  // threshold partial pivoting (diagonal kept when >= tau * column max)
+  if (mode == MODE_AC) {
+    st = gp_factor<std::complex<double>>(n, ap, ai, axz, q, tau, F);
+  } else {
+    std::vector<double> axr(axz.size());
+    for (size_t k = 0; k < axz.size(); ++k) axr[k] = axz[k].real();
+    st = gp_factor<double>(n, ap, ai, axr, q, tau, F);
+  }
+  if (st != KRETS_OK) {
+    msg = "matrix is singular for the representative element values (no usable pivot)";
+    return st;
+  }
+  P.pivot_min_ratio = F.min_ratio;
+  P.q = q;
+  P.qinv.assign(n, 0);
+  for (int k = 0; k < n; ++k) P.qinv[q[k]] = k;
+  P.pinv = F.pinv;
+  P.prow.assign(n, 0);
+  for (int r = 0; r < n; ++r) P.prow[F.pinv[r]] = r;
+  // ---- static LU pattern in position space
+  std::vector<std::vector<int>> rows(n);
+  for (int k = 0; k < n; ++k) {
+    for (int p = F.lp[k]; p < F.lp[k + 1]; ++p) rows[F.pinv[F.li[p]]].push_back(k);  // L(i,k)
+    for (int p = F.up[k]; p < F.up[k + 1]; ++p) rows[F.ui[p]].push_back(k);           // U(i,k), diag
+  }
+  P.lu_rowptr.assign(n + 1, 0);
+  P.lu_diag.assign(n, -1);
+  for (int k = 0; k < n; ++k) {
+    std::sort(rows[k].begin(), rows[k].end());
+    P.lu_rowptr[k + 1] = P.lu_rowptr[k] + (int)rows[k].size();
+    P.max_row_lu = std::max(P.max_row_lu, (int)rows[k].size());
+  }
+  P.lu_col.resize(P.lu_rowptr[n]);
+  std::vector<std::unordered_map<int, int>> slot(n);
+  for (int k = 0; k < n; ++k) {
+    for (size_t t = 0; t < rows[k].size(); ++t) {
+      int s = P.lu_rowptr[k] + (int)t;
+      P.lu_col[s] = rows[k][t];
+      slot[k][rows[k][t]] = s;
+      if (rows[k][t] == k) P.lu_diag[k] = s;
+    }
+    if (P.lu_diag[k] < 0) {
+      msg = "internal: missing diagonal in static pattern";
+      return KRETS_ERR_UNEXPECTED;
+    }
+  }
+  // ---- factorisation program (IKJ)
+  P.piv_ptr.assign(n + 1, 0);
+  for (int k = 0; k < n; ++k) {
+    for (int s = P.lu_rowptr[k]; s < P.lu_diag[k]; ++s) {
+      int j = P.lu_col[s];
+      int ub = (int)P.upd.size() / 2;
+      for (int t = P.lu_diag[j] + 1; t < P.lu_rowptr[j + 1]; ++t) {
+        int c = P.lu_col[t];
+        auto it = slot[k].find(c);
+        if (it == slot[k].end()) {
+          msg = "internal: fill entry missing from static pattern";
+          return KRETS_ERR_UNEXPECTED;
+        }
+        P.upd.push_back(it->second);
+        P.upd.push_back(t);
+        P.factor_flops += 2;
+      }
+      P.piv.insert(P.piv.end(), {s, j, ub, (int)P.upd.size() / 2});
+      P.factor_flops += 1;
+    }
+    P.piv_ptr[k + 1] = (int)P.piv.size() / 4;
+  }
+  // ---- level schedules
+  std::vector<int> lev(n, 0), ulev(n, 0);
+  int nl = 0, nu = 0;
+  for (int k = 0; k < n; ++k) {
+    int l = 0;
+    for (int s = P.lu_rowptr[k]; s < P.lu_diag[k]; ++s) l = std::max(l, lev[P.lu_col[s]] + 1);
+    lev[k] = l;
+    nl = std::max(nl, l + 1);
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    int l = 0;
+    for (int s = P.lu_diag[k] + 1; s < P.lu_rowptr[k + 1]; ++s) l = std::max(l, ulev[P.lu_col[s]] + 1);
+    ulev[k] = l;
+    nu = std::max(nu, l + 1);
+  }
+  auto bucket = [&](const std::vector<int> &lv, int nlev, std::vector<int> &ptr, std::vector<int> &rws) {
+    ptr.assign(nlev + 1, 0);
+    for (int k = 0; k < n; ++k) ptr[lv[k] + 1]++;
+    for (int l = 0; l < nlev; ++l) ptr[l + 1] += ptr[l];
+    rws.assign(n, 0);
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    for (int k = 0; k < n; ++k) rws[fill[lv[k]]++] = k;
+  };
+  if (n == 0) { nl = nu = 0; }
+  bucket(lev, nl, P.lev_ptr, P.lev_rows);
+  bucket(ulev, nu, P.ulev_ptr, P.ulev_rows);
+  // ---- stamp maps: A entries (position space) with contributions in emission order
+  std::vector<std::pair<long long, int>> am;  // key (row pos * n + col pos), emission index
+  am.reserve(M.size());
+  for (size_t t = 0; t < M.size(); ++t)
+    am.push_back({(long long)P.pinv[M[t].r] * n + P.qinv[M[t].c], (int)t});
+  std::stable_sort(am.begin(), am.end(), [](auto &a, auto &b) { return a.first < b.first; });
+  P.a_rowptr.assign(n + 1, 0);
+  P.a_cptr.push_back(0);
+  for (size_t t = 0; t < am.size();) {
+    size_t t2 = t;
+    int r = (int)(am[t].first / n), c = (int)(am[t].first % n);
+    while (t2 < am.size() && am[t2].first == am[t].first) P.a_contrib.push_back(M[am[t2++].second].code);
+    P.a_cptr.push_back((int)P.a_contrib.size());
+    P.a_col.push_back(c);
+    auto it = slot[r].find(c);
+    if (it == slot[r].end()) {
+      msg = "internal: A entry outside the LU pattern";
+      return KRETS_ERR_UNEXPECTED;
+    }
+    P.a_slot.push_back(it->second);
+    P.a_rowptr[r + 1]++;
+    t = t2;
+  }
+  for (int r = 0; r < n; ++r) P.a_rowptr[r + 1] += P.a_rowptr[r];
+  std::vector<std::vector<int>> brow(n);
+  for (auto &b : B) brow[P.pinv[b.r]].push_back(b.code);  // emission order kept
+  P.b_cptr.assign(n + 1, 0);
+  for (int r = 0; r < n; ++r) {
+    P.b_contrib.insert(P.b_contrib.end(), brow[r].begin(), brow[r].end());
+    P.b_cptr[r + 1] = (int)P.b_contrib.size();
+  }
+  P.el_pos.assign(4 * ne, -1);
+  for (int e = 0; e < ne; ++e) {
+    const int idx[4] = {el[e].p, el[e].m, el[e].b, el[e].g};
+    for (int t = 0; t < 4; ++t) P.el_pos[4 * e + t] = idx[t] >= 0 ? P.qinv[idx[t]] : -1;
+  }
+  uint64_t sig = 1469598103934665603ull;
+  sig = fnv1a(sig, (uint64_t)mode);
+  sig = fnv1a(sig, (uint64_t)n);
+  for (auto &m : M) sig = fnv1a(sig, (uint64_t)m.r * 0x9E3779B1u + (uint64_t)m.c);
+  P.signature = sig;
+  return KRETS_OK;
+}
+
+// Estimated per-instance device cost of a program (arbitrary units): per level, the
+// longest row divided over the CTA plus a fixed synchronisation cost, for the L and U
+// solves and the factorisation.
+static double program_cost(const Program &P) {
+  const int T = 128;
+  const double sync = 24.0;
+  double c = 0;
+  auto levels = [&](const std::vector<int> &ptr, const std::vector<int> &rws, bool lower) {
+    for (size_t l = 0; l + 1 < ptr.size(); ++l) {
+      int cnt = ptr[l + 1] - ptr[l];
+      int mx = 0;
+      for (int t = ptr[l]; t < ptr[l + 1]; ++t) {
+        int k = rws[t];
+        int len = lower ? P.lu_diag[k] - P.lu_rowptr[k] : P.lu_rowptr[k + 1] - P.lu_diag[k];
+        mx = std::max(mx, len);
+      }
+      c += ((cnt + T - 1) / T) * (2.0 * mx + 4.0) + sync;
+    }
+  };
+  levels(P.lev_ptr, P.lev_rows, true);
+  levels(P.ulev_ptr, P.ulev_rows, false);
+  c *= 3.0;  // solves dominate (several per step) relative to one factorisation
+  c += (double)P.factor_flops / T;
+  return c;
+}
+
+int build_program(const krets_element *el, int ne, int n, int mode, int method, double h, double f,
+                  int forced_ordering, Program &out, std::string &msg) {
+  if (n <= 0) {
+    msg = "circuit has no unknowns";
+    return KRETS_ERR_MATRIX_BUILD;
+  }
+  std::vector<MEntry> M;
+  std::vector<BEntry> B;
+  for (int e = 0; e < ne; ++e) {
+    const krets_element &x = el[e];
+    if (x.p >= n || x.m >= n || x.b >= n || x.g >= n) {
+      msg = "element " + std::to_string(e) + " references an unknown index >= n";
+      return KRETS_ERR_INVALID_ARGUMENT;
+    }
+    if (mode == MODE_DC && x.kind == KRETS_ELEM_C) continue;  // op.rs:20-24
+    if (!emit(x, e, mode, M, B)) {
+      if (x.kind == KRETS_ELEM_Q || x.kind == KRETS_ELEM_M) {
+        msg = x.kind == KRETS_ELEM_Q ? "BJT stamps are not implemented in the reference (todo!())"
+                                     : "NMOS AC stamp is not implemented in the reference (todo!())";
+        return KRETS_ERR_NOT_IMPLEMENTED;
+      }
+      msg = "unknown element kind " + std::to_string(x.kind);
+      return KRETS_ERR_INVALID_ELEMENT;
+    }
+  }
+  // symmetric adjacency of the pattern (without diagonal)
+  std::vector<std::vector<int>> adj(n);
+  for (auto &m : M)
+    if (m.r != m.c) { adj[m.r].push_back(m.c); adj[m.c].push_back(m.r); }
+  for (auto &a : adj) {
+    std::sort(a.begin(), a.end());
+    a.erase(std::unique(a.begin(), a.end()), a.end());
+  }
+  std::vector<int> cands = forced_ordering >= 0 ? std::vector<int>{forced_ordering}
+                                                : std::vector<int>{ORDER_NESTED, ORDER_MINDEG, ORDER_NATURAL};
+  double best_cost = 0;
+  int best_st = KRETS_ERR_DECOMPOSITION_FAILED;
+  std::string best_msg;
+  for (int o : cands) {
+    std::vector<int> q;
+    if (o == ORDER_NATURAL) {
+      q.resize(n);
+      std::iota(q.begin(), q.end(), 0);
+    } else if (o == ORDER_MINDEG) {
+      if (n > 20000) continue;
+      q = order_min_degree(n, adj);
+    } else {
+      q = order_nested_dissection(n, adj);
+    }
+    Program P;
+    std::string m2;
+    int st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2);
+    if (st != KRETS_OK) {
+      if (best_st != KRETS_OK) { best_st = st; best_msg = m2; }
+      continue;
+    }
+    P.ordering = o;
+    double c = program_cost(P);
+    if (best_st != KRETS_OK || c < best_cost) {
+      best_cost = c;
+      best_st = KRETS_OK;
+      out = std::move(P);
+    }
+  }
+  if (best_st != KRETS_OK) msg = best_msg;
+  return best_st;
+}
+
+}  // namespace krets
+
+// --------------------------------------------------------------- C ABI: introspection
+extern "C" krets_status krets_symbolic_export(const krets_element *elems, int32_t n_elem, int32_t n_unknowns,
+                                              int32_t mode, int32_t method, double h, double freq,
+                                              int32_t ordering, int32_t which, int64_t *out, int64_t cap,
+                                              int64_t *len) {
+  using namespace krets;
+  if (!elems || n_elem < 0 || n_unknowns <= 0 || !len) return KRETS_ERR_INVALID_ARGUMENT;
+  Program P;
+  std::string msg;
+  int st = build_program(elems, n_elem, n_unknowns, mode, method, h, freq, ordering, P, msg);
+  if (st != KRETS_OK) return st;
+  std::vector<long long> meta{P.ordering, P.n, (long long)P.a_col.size(), (long long)P.lu_col.size(),
+                              (long long)P.lev_ptr.size() - 1, (long long)P.ulev_ptr.size() - 1, P.factor_flops};
+  const std::vector<int> *arrs[] = {&P.q, &P.prow, &P.lu_rowptr, &P.lu_col, &P.lu_diag, &P.a_rowptr, &P.a_col,
+                                    &P.a_slot, &P.a_cptr, &P.a_contrib, &P.b_cptr, &P.b_contrib, &P.piv_ptr,
+                                    &P.piv, &P.upd, &P.lev_ptr, &P.lev_rows, &P.ulev_ptr, &P.ulev_rows,
+                                    &P.el_pos};
+  if (which < 0 || which > KRETS_PROG_META) return KRETS_ERR_INVALID_ARGUMENT;
+  if (which == KRETS_PROG_META) {
+    *len = (int64_t)meta.size();
+    if (out)
+      for (int64_t k = 0; k < std::min<int64_t>(cap, *len); ++k) out[k] = meta[k];
+    return KRETS_OK;
+  }
+  const std::vector<int> &v = *arrs[which];
+  *len = (int64_t)v.size();
+  if (out)
+    for (int64_t k = 0; k < std::min<int64_t>(cap, *len); ++k) out[k] = v[k];
+  return KRETS_OK;
+}

@@ -1,0 +1,68 @@
+// Host symbolic pass: turns a flattened netlist into a static "program" that the device
+// kernels execute without further decisions (ordering, pivot sequence, fill pattern,
+// stamp-to-slot maps, level schedules).
+//
+// The reference re-derives all of this every Newton iteration (a fresh faer
+// SparseColMat + sp_lu per iteration: crates/krets-solver/src/solver/op.rs:48-58,
+// transient.rs:74-83, ac.rs:67-70, dc.rs:81-84).  Here it runs once per (topology, mode).
+#pragma once
+
+#include <complex>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "krets_gpu.h"
+
+namespace krets {
+
+enum Mode { MODE_DC = 0, MODE_AC = 1, MODE_TRAN = 2 };
+
+// A matrix stamp contribution, packed as  elem << 2 | unit << 1 | neg:
+//   unit = 1 -> the value is the constant 1 (KCL/KVL incidence), else the element's
+//   per-pass matrix coefficient; neg = 1 -> negated.
+// A right-hand-side contribution, packed as elem << 1 | neg (value = element's
+// per-pass rhs coefficient).
+inline int pack_a(int e, bool unit, bool neg) { return (e << 2) | (unit ? 2 : 0) | (neg ? 1 : 0); }
+inline int pack_b(int e, bool neg) { return (e << 1) | (neg ? 1 : 0); }
+
+enum Ordering { ORDER_NATURAL = 0, ORDER_MINDEG = 1, ORDER_NESTED = 2 };
+
+struct Program {
+  int mode = 0, method = 0, n = 0, ne = 0;
+  int ordering = 0;
+  // position k factors unknown column q[k] with pivot row prow[k]
+  std::vector<int> q, qinv, prow, pinv;
+  // LU pattern in position space, row-wise: [L part | diag | U part], columns ascending
+  std::vector<int> lu_rowptr, lu_col, lu_diag;
+  // A entries in position space (subset of the LU pattern), row-wise
+  std::vector<int> a_rowptr, a_col, a_slot;
+  std::vector<int> a_cptr, a_contrib;  // contributions of each A entry, emission order
+  std::vector<int> b_cptr, b_contrib;  // rhs contributions per position row
+  // factorisation program (row-oriented, up-looking):
+  //   row k: piv entries [piv_ptr[k], piv_ptr[k+1]), each {slot(k,j), j, upd_begin, upd_end}
+  //   upd pairs {dst slot(k,c), src slot(j,c)}:  lu[dst] -= l_kj * lu[src]
+  std::vector<int> piv_ptr;
+  std::vector<int> piv;  // 4 ints per entry
+  std::vector<int> upd;  // 2 ints per entry
+  // level schedules: rows of the L solve / factorisation, and of the U solve
+  std::vector<int> lev_ptr, lev_rows, ulev_ptr, ulev_rows;
+  // per element: p, m, b, g in POSITION space (-1 = absent)
+  std::vector<int> el_pos;
+  // per element: 1 when it is a capacitor whose TR history current is state
+  long long factor_flops = 0;
+  int max_row_lu = 0;
+  uint64_t signature = 0;
+  double pivot_min_ratio = 1.0;  // smallest |pivot| / column max seen while pivoting
+};
+
+// Build the program for one mode.  h / freq: representative step and frequency used to
+// evaluate values for pivot selection.  Returns KRETS_OK or an error code (msg filled).
+int build_program(const krets_element *el, int ne, int n, int mode, int method, double h, double freq,
+                  int forced_ordering, Program &out, std::string &msg);
+
+// Exposed for tests of the symbolic pass itself.
+std::vector<int> order_min_degree(int n, const std::vector<std::vector<int>> &adj);
+std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<int>> &adj);
+
+}  // namespace krets

@@ -1,0 +1,129 @@
+"""Seeded synthetic workloads (netlists and Monte Carlo values) for the five
+benchmark configurations and the tests.
+
+All randomness comes from a counter-based splitmix64 stream (seed -> u64 ->
+uniform in (0, 1]); normals use Box-Muller on consecutive uniform pairs.  The
+generators are pure numpy and produce identical values on every machine.
+
+Configurations (sizes as in the benchmark definitions):
+  1  resistor ladder: V1 1 0 1; R_k k->k+1 (k < N), R_N N->0, all 1 kOhm, plus a
+     1 kOhm shunt from every node to ground; N = 1000 gives 1001 unknowns
+  2  RC low-pass ladder, 500 sections, R log-uniform 100 Ohm-10 kOhm, C
+     log-uniform 1 pF-1 uF, AC 1 V source; 4096 log-spaced points 1 Hz-1 GHz
+  3  RLC ladder Monte Carlo: 2048 instances x 200 sections (R 50 Ohm, L 10 nH,
+     C 1 pF, each x (1 + 0.1 N(0,1))), 0-1 V pulse, 100 ps rise, 5 ns width
+  4  uneven batch of random connected netlists (see random_netlist)
+  5  RC ladder for adjoint sensitivities, 1000 sections
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .netlist import Circuit, parse_circuit_description
+from .table import element_table
+
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def splitmix64(seed: int, count: int) -> np.ndarray:
+    """`count` consecutive splitmix64 outputs of the stream started at `seed`."""
+    with np.errstate(over="ignore"):
+        idx = np.arange(1, count + 1, dtype=np.uint64)
+        z = (np.uint64(seed) + idx * np.uint64(0x9E3779B97F4A7C15))
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+def uniform(seed: int, count: int) -> np.ndarray:
+    """Uniform doubles in (0, 1]: ((u >> 11) + 1) * 2^-53."""
+    u = splitmix64(seed, count)
+    return ((u >> np.uint64(11)).astype(np.float64) + 1.0) * (2.0 ** -53)
+
+
+def normal(seed: int, count: int) -> np.ndarray:
+    """Standard normals by Box-Muller on consecutive uniform pairs."""
+    m = (count + 1) // 2
+    u = uniform(seed, 2 * m)
+    u1, u2 = u[0::2], u[1::2]
+    r = np.sqrt(-2.0 * np.log(u1))
+    z = np.empty(2 * m)
+    z[0::2] = r * np.cos(2.0 * np.pi * u2)
+    z[1::2] = r * np.sin(2.0 * np.pi * u2)
+    return z[:count]
+
+
+def log_uniform(seed: int, count: int, lo: float, hi: float) -> np.ndarray:
+    return np.exp(np.log(lo) + (np.log(hi) - np.log(lo)) * uniform(seed, count))
+
+
+# --------------------------------------------------------------------------- netlists
+def resistor_ladder_netlist(n: int, shunts: bool = False) -> str:
+    """The reference's resistor_ladder_<n>.cir element lines (plus optional shunts)."""
+    lines = ["% N-sized resistor ladder", "V1 1 0 1"]
+    for k in range(1, n):
+        lines.append(f"R{k} {k} {k + 1} 1000")
+    lines.append(f"R{n} {n} 0 1000")
+    if shunts:
+        for k in range(1, n + 1):
+            lines.append(f"Rs{k} {k} 0 1000")
+    return "\n".join(lines) + "\n"
+
+
+def config1_circuit() -> Circuit:
+    """Plain OP workload: 1000-section ladder with a shunt per node, 1001 unknowns."""
+    return parse_circuit_description(resistor_ladder_netlist(1000, shunts=True))
+
+
+def rc_ladder_ac(sections: int = 500, seed: int = 2) -> Circuit:
+    """AC workload: V1 in 0 0 AC 1, R_k n_{k-1}->n_k, C_k n_k->0 (seeded values)."""
+    r = log_uniform(seed, sections, 100.0, 1e4)
+    c = log_uniform(seed + 1000003, sections, 1e-12, 1e-6)
+    lines = ["* RC low-pass ladder", "V1 in 0 0 AC 1"]
+    prev = "in"
+    for k in range(1, sections + 1):
+        lines.append(f"R{k} {prev} n{k} {float(r[k - 1])!r}")
+        lines.append(f"C{k} n{k} 0 {float(c[k - 1])!r}")
+        prev = f"n{k}"
+    return parse_circuit_description("\n".join(lines) + "\n")
+
+
+def rlc_ladder(sections: int = 200, rise: str = "100p", width: str = "5n") -> Circuit:
+    """Nominal RLC ladder: R 50 Ohm n_{k-1}->m_k, L 10 nH m_k->n_k, C 1 pF n_k->0,
+    driven by V1 in 0 dc 0 PULSE(0 1 0 <rise> <rise> <width> 1)."""
+    lines = ["* RLC ladder", f"V1 in 0 dc 0 PULSE(0 1 0 {rise} {rise} {width} 1)"]
+    prev = "in"
+    for k in range(1, sections + 1):
+        lines.append(f"R{k} {prev} m{k} 50")
+        lines.append(f"L{k} m{k} n{k} 10n")
+        lines.append(f"C{k} n{k} 0 1p")
+        prev = f"n{k}"
+    return parse_circuit_description("\n".join(lines) + "\n")
+
+
+def monte_carlo_values(circuit: Circuit, n_inst: int, sigma: float = 0.1, seed: int = 3,
+                       kinds=(1, 2, 3)) -> np.ndarray:
+    """[n_inst][n_elem] element values: nominal x (1 + sigma N(0,1)) for R, C, L."""
+    t = element_table(circuit)
+    nominal = t["value"].copy()
+    ne = len(t)
+    z = normal(seed, n_inst * ne).reshape(n_inst, ne)
+    mask = np.isin(t["kind"], kinds)
+    vals = np.tile(nominal, (n_inst, 1))
+    vals[:, mask] = nominal[mask] * (1.0 + sigma * z[:, mask])
+    return vals
+
+
+def rc_ladder_step(sections: int = 1000, seed: int = 5) -> Circuit:
+    """Adjoint workload: R log-uniform 100 Ohm-10 kOhm, C log-uniform 1 pF-100 pF,
+    1 V step input PULSE(0 1 0 1p 1p 1 2)."""
+    r = log_uniform(seed, sections, 100.0, 1e4)
+    c = log_uniform(seed + 1000003, sections, 1e-12, 1e-10)
+    lines = ["* RC ladder, step input", "V1 in 0 dc 0 PULSE(0 1 0 1p 1p 1 2)"]
+    prev = "in"
+    for k in range(1, sections + 1):
+        lines.append(f"R{k} {prev} n{k} {float(r[k - 1])!r}")
+        lines.append(f"C{k} n{k} 0 {float(c[k - 1])!r}")
+        prev = f"n{k}"
+    return parse_circuit_description("\n".join(lines) + "\n")

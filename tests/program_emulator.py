@@ -1,0 +1,122 @@
+"""CPU emulation (numpy) of the static program the host symbolic pass emits.
+
+Test infrastructure: it executes the exported index arrays exactly the way the
+device engine walks them (segmented stamp sums -> IKJ factor program -> level
+ordered solves), so a mismatch against the oracle points at the symbolic pass
+rather than at the CUDA code.  No solve path of the product calls this.
+"""
+import numpy as np
+
+from krets_gb300 import _lib
+
+PI = 3.14159265358979323846
+
+
+def element_coefs(table, mode, method="be", h=1.0, freq=0.0, prev=None, t_src=0.0, icap=None):
+    """Per-element (matrix coefficient, rhs coefficient), original unknown numbering."""
+    ne = len(table)
+    ca = np.zeros(ne, dtype=complex)
+    cb = np.zeros(ne)
+    tr = method == "tr"
+    for e, el in enumerate(table):
+        k, v = int(el["kind"]), float(el["value"])
+        p, m, b = int(el["p"]), int(el["m"]), int(el["b"])
+        if k == 1:
+            ca[e] = v if el["flags"] & 1 else 1.0 / v
+        elif k == 2:
+            if mode == 1:
+                ca[e] = 1j * (2.0 * PI * freq * v)
+            elif mode == 2:
+                vp = prev[p] if p >= 0 else 0.0
+                vm = prev[m] if m >= 0 else 0.0
+                if tr:
+                    ca[e] = 2.0 * v / h
+                    cb[e] = ca[e].real * (vp - vm) + icap[e]
+                else:
+                    ca[e] = v / h
+                    cb[e] = -(-(v / h) * (vp - vm))
+        elif k == 3:
+            if mode == 1:
+                ca[e] = 1j * (2.0 * PI * freq * v)
+            elif mode == 2:
+                ip = prev[b]
+                if tr:
+                    lh = 2.0 * v / h
+                    vl = (prev[p] if p >= 0 else 0.0) - (prev[m] if m >= 0 else 0.0)
+                    ca[e] = lh
+                    cb[e] = -lh * ip - vl
+                else:
+                    ca[e] = v / h
+                    cb[e] = -(v / h) * ip
+        elif k == 4:
+            if mode == 0:
+                cb[e] = v
+            elif mode == 1:
+                cb[e] = float(el["ac"])
+            else:
+                from oracle import oracle as O
+                w = el["wp"]
+                cb[e] = O.pulse(w, t_src) if el["wave"] == 1 else (O.sin(w, t_src) if el["wave"] == 2 else v)
+        elif k == 5:
+            cb[e] = v
+    return ca, cb
+
+
+def emulate(prog, table, n, ca, cb, complex_=False):
+    """Stamp, factor and solve with the program arrays; returns x in unknown order."""
+    dt = complex if complex_ else float
+    cav = ca if complex_ else ca.real
+    nnz_lu = len(prog["lu_col"])
+    lu = np.zeros(nnz_lu, dtype=dt)
+    a_cptr, a_contrib = prog["a_cptr"], prog["a_contrib"]
+    for t in range(len(prog["a_col"])):
+        s = dt(0)
+        for u in range(a_cptr[t], a_cptr[t + 1]):
+            code = int(a_contrib[u])
+            val = dt(1.0) if code & 2 else cav[code >> 2]
+            s += -val if code & 1 else val
+        lu[prog["a_slot"][t]] = s
+    b = np.zeros(n, dtype=dt)
+    for k in range(n):
+        s = 0.0
+        for u in range(prog["b_cptr"][k], prog["b_cptr"][k + 1]):
+            code = int(prog["b_contrib"][u])
+            s += -cb[code >> 1] if code & 1 else cb[code >> 1]
+        b[k] = s
+    piv = prog["piv"].reshape(-1, 4)
+    upd = prog["upd"].reshape(-1, 2)
+    diag = prog["lu_diag"]
+    lev_ptr, lev_rows = prog["lev_ptr"], prog["lev_rows"]
+    done = np.zeros(n, dtype=bool)
+    for lv in range(len(lev_ptr) - 1):
+        rows = lev_rows[lev_ptr[lv]:lev_ptr[lv + 1]]
+        for k in rows:
+            for pi in range(prog["piv_ptr"][k], prog["piv_ptr"][k + 1]):
+                s, j, u0, u1 = piv[pi]
+                assert done[j], "factor level order violated"
+                l = lu[s] / lu[diag[j]]
+                lu[s] = l
+                for dst, src in upd[u0:u1]:
+                    lu[dst] -= l * lu[src]
+        for k in rows:
+            done[k] = True
+    rp, col = prog["lu_rowptr"], prog["lu_col"]
+    y = b.copy()
+    for lv in range(1, len(lev_ptr) - 1):
+        for k in lev_rows[lev_ptr[lv]:lev_ptr[lv + 1]]:
+            for u in range(rp[k], diag[k]):
+                y[k] -= lu[u] * y[col[u]]
+    ulp, ulr = prog["ulev_ptr"], prog["ulev_rows"]
+    for lv in range(len(ulp) - 1):
+        for k in ulr[ulp[lv]:ulp[lv + 1]]:
+            s = y[k]
+            for u in range(diag[k] + 1, rp[k + 1]):
+                s -= lu[u] * y[col[u]]
+            y[k] = s / lu[diag[k]]
+    x = np.zeros(n, dtype=dt)
+    x[prog["q"]] = y
+    return x
+
+
+def export(table, n, mode, method="be", h=1.0, freq=1e3, ordering=-1):
+    return _lib.symbolic_export(table, n, mode, method, h, freq, ordering)

@@ -1,0 +1,184 @@
+"""GPU parity: every analysis through the C ABI against the CPU oracle on the same
+inputs.  Tolerance: 1e-9 norm-wise relative error per quantity class (node voltages,
+branch currents), the precision target of the mixed-precision path; the FP64 plain
+form is held to the same bound.  Also the reference's own known answers."""
+import numpy as np
+import pytest
+
+from conftest import analysis_from_case, circuit_from_case
+from krets_gb300 import AnalysisSpec, Solver, generate_frequencies, parse_circuit_description
+from krets_gb300 import _lib
+from krets_gb300.generators import (config1_circuit, monte_carlo_values, rc_ladder_ac, rc_ladder_step,
+                                    rlc_ladder)
+from krets_gb300.table import element_table, is_current_mask
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-9
+
+
+def rel_err(x, ref, cur_mask):
+    """max over {voltages, currents} of max|x - ref| / max|ref| (arrays [..., n])."""
+    x = np.asarray(x)
+    ref = np.asarray(ref)
+    worst = 0.0
+    for m in (cur_mask, ~cur_mask):
+        if not m.any():
+            continue
+        r = np.abs(ref[..., m]).max()
+        d = np.abs(x[..., m] - ref[..., m]).max()
+        worst = max(worst, d / r if r > 0 else d)
+    return worst
+
+
+def _oracle(O, case):
+    from test_oracle_golden import _run_oracle
+    return _run_oracle(O, case)
+
+
+@pytest.mark.parametrize("group", ["op", "ac", "dc", "tran"])
+def test_reference_cases_through_solver(oracle_lib, golden, group):
+    from test_oracle_golden import _check
+    for case in golden[group]:
+        c = circuit_from_case(case)
+        res = Solver(c).solve(analysis_from_case(case))
+        maps = res.data if isinstance(res.data, list) else [res.data]
+        _check(maps, case["expect"])
+        _, ref = _oracle(oracle_lib, case)
+        assert len(ref) == len(maps)
+        names = list(c.index_map)
+        got = np.array([[m[k] for k in names] for m in maps])
+        exp = np.array([[m[k] for k in names] for m in ref])
+        mask = np.array([k.startswith("I") for k in names])
+        assert rel_err(got, exp, mask) < TOL, case["name"]
+
+
+def test_low_pass_ac_parquet(golden):
+    fx = golden["parquet"]["low_pass_ac"]
+    spec = AnalysisSpec.from_str(fx["toml"])
+    c = parse_circuit_description(fx["netlist"])
+    res = Solver(c).solve(spec.analysis)
+    cols = fx["columns"]
+    for key, idx in c.index_map.items():
+        z = res.array[:, idx]
+        np.testing.assert_allclose(np.abs(z), cols[key + "_mag"], rtol=1e-12)
+        np.testing.assert_allclose(np.degrees(np.arctan2(z.imag, z.real)), cols[key + "_phase_deg"], rtol=1e-10,
+                                   atol=1e-10)
+
+
+def test_inverter_dc_parquet(golden):
+    fx = golden["parquet"]["inverter_dc"]
+    spec = AnalysisSpec.from_str(fx["toml"])
+    c = parse_circuit_description(fx["netlist"])
+    res = Solver(c).solve(spec.analysis)
+    for key, v in c.index_map.items():
+        np.testing.assert_allclose(res.array[:, v], fx["columns"][key], rtol=1e-12, atol=1e-15)
+
+
+def test_config1_plain_op(oracle_lib):
+    c = config1_circuit()
+    t = element_table(c)
+    g = _lib.GpuCircuit(t, c.size)
+    x, it = g.op()
+    ref = oracle_lib.op(t, c.size)
+    assert it == 1
+    assert rel_err(x, ref, is_current_mask(c)) < TOL
+
+
+def test_plain_transient_refactor_matches_reuse(oracle_lib):
+    c = rlc_ladder(40)
+    t = element_table(c)
+    g = _lib.GpuCircuit(t, c.size)
+    a = g.tran(1e-12, 400, "tr", lag=False, refactor_each_step=True)
+    b = g.tran(1e-12, 400, "tr", lag=False, refactor_each_step=False)
+    np.testing.assert_array_equal(a, b)      # identical factors -> identical results
+    ref = oracle_lib.tran(t, c.size, 1e-12, 400, method="tr", lag=False)
+    assert rel_err(a, ref, is_current_mask(c)) < TOL
+
+
+@pytest.mark.parametrize("precision", [_lib.PREC_FP64, _lib.PREC_MIXED])
+def test_batched_mc_transient_matches_oracle(oracle_lib, precision):
+    c = rlc_ladder(200)
+    t = element_table(c)
+    vals = monte_carlo_values(c, 6, seed=11)
+    g = _lib.GpuCircuit(t, c.size)
+    steps = 1500
+    x = g.batch_tran(vals, 1e-12, steps, "tr", lag=False, precision=precision)
+    mask = is_current_mask(c)
+    for i in range(len(vals)):
+        ti = t.copy()
+        ti["value"] = vals[i]
+        ref = oracle_lib.tran(ti, c.size, 1e-12, steps, method="tr", lag=False)
+        assert rel_err(x[i], ref, mask) < TOL, i
+    if precision == _lib.PREC_MIXED:
+        hist, fb = g.refine_stats()
+        assert hist.sum() == len(vals) * steps and fb == 0
+
+
+def test_batched_be_with_source_lag(oracle_lib):
+    net = "V1 in 0 dc 0 PULSE (0 1 1u 1u 1u 1 1)\nR1 in out 1000\nC1 out 0 1u\n"
+    c = parse_circuit_description(net)
+    t = element_table(c)
+    g = _lib.GpuCircuit(t, c.size)
+    x = g.batch_tran(None, 50e-6, 400, "be", lag=True, precision=_lib.PREC_MIXED, n_inst=1)
+    assert abs(x[0, 42, c.index_map["V(out)"]] - 0.8647) < 1e-3
+    ref = oracle_lib.tran(t, c.size, 50e-6, 400, method="be", lag=True)
+    assert rel_err(x[0], ref, is_current_mask(c)) < TOL
+
+
+def test_batched_nonlinear_rectifier(oracle_lib, golden):
+    case = next(cc for cc in golden["tran"] if cc["name"] == "rectifier_tran")
+    c = circuit_from_case(case)
+    t = element_table(c)
+    g = _lib.GpuCircuit(t, c.size)
+    ref = oracle_lib.tran(t, c.size, 50e-6, 300, method="be", lag=True)
+    for prec in (_lib.PREC_FP64, _lib.PREC_MIXED):
+        x = g.batch_tran(None, 50e-6, 300, "be", lag=True, precision=prec, n_inst=1)
+        assert rel_err(x[0], ref, is_current_mask(c)) < 1e-8, prec
+
+
+@pytest.mark.parametrize("precision", [_lib.PREC_FP64, _lib.PREC_MIXED])
+def test_batched_ac_sweep_matches_oracle(oracle_lib, precision):
+    from krets_gb300.analyses import AcAnalysis, Decade
+    c = rc_ladder_ac()
+    t = element_table(c)
+    f = np.array(generate_frequencies(AcAnalysis(Decade(455), 1.0, 1e9)))[::16]
+    g = _lib.GpuCircuit(t, c.size)
+    z = g.batch_ac(None, f, precision=precision)[0]
+    ref = oracle_lib.ac(t, c.size, f)
+    mask = is_current_mask(c)
+    for i in range(len(f)):   # per frequency point (each is its own system)
+        assert rel_err(z[i], ref[i], mask) < TOL, (i, f[i])
+
+
+def test_batch_op_monte_carlo(oracle_lib):
+    c = config1_circuit()
+    t = element_table(c)
+    vals = monte_carlo_values(c, 8, seed=4)
+    g = _lib.GpuCircuit(t, c.size)
+    x = g.batch_op(vals)
+    for i in range(len(vals)):
+        ti = t.copy()
+        ti["value"] = vals[i]
+        assert rel_err(x[i], oracle_lib.op(ti, c.size), is_current_mask(c)) < TOL
+
+
+def test_batched_transient_is_deterministic():
+    c = rlc_ladder(100)
+    t = element_table(c)
+    vals = monte_carlo_values(c, 32, seed=1)
+    g = _lib.GpuCircuit(t, c.size)
+    a = g.batch_tran(vals, 1e-12, 300, "tr", precision=_lib.PREC_MIXED)
+    b = g.batch_tran(vals, 1e-12, 300, "tr", precision=_lib.PREC_MIXED)
+    np.testing.assert_array_equal(a, b)
+
+
+def test_errors_are_reported():
+    from krets_gb300.errors import DecompositionFailed, ElementNotFound, MatrixDecomposition
+    from krets_gb300.analyses import DcAnalysis, Op
+    c = parse_circuit_description("V1 a 0 1\nV2 a 0 2\nR1 a 0 1\n")   # V-source loop: singular
+    with pytest.raises((DecompositionFailed, MatrixDecomposition)):
+        Solver(c).solve(Op())
+    c = parse_circuit_description("V1 a 0 1\nR1 a 0 1\n")
+    with pytest.raises(ElementNotFound):
+        Solver(c).solve(DcAnalysis("V9", 0, 1, 0.5))

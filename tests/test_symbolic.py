@@ -1,0 +1,112 @@
+"""Host symbolic pass, checked on the CPU: the exported static program (ordering,
+pivots, fill, stamp maps, level schedules) is executed by a numpy emulator and must
+reproduce the oracle.  Also checks that libkrets_gpu.so exports every declared symbol."""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import program_emulator as PE
+from conftest import circuit_from_case
+from krets_gb300 import parse_circuit_description
+from krets_gb300.generators import config1_circuit, monte_carlo_values, rc_ladder_ac, rlc_ladder
+from krets_gb300.table import element_table
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    import ctypes
+    hdr = (ROOT / "include" / "krets_gpu.h").read_text()
+    names = set(re.findall(r"^(?:krets_status|const char \*|int64_t)\s*(krets_[a-z0-9_]+)\s*\(", hdr, re.M))
+    assert len(names) > 15
+    lib = ctypes.CDLL(str(built_lib.LIB_PATH))
+    for nm in sorted(names):
+        assert hasattr(lib, nm), nm
+
+
+@pytest.mark.parametrize("ordering", [-1, 0, 1, 2])
+def test_op_programs_match_oracle(built_lib, oracle_lib, golden, ordering):
+    for case in golden["op"]:
+        c = circuit_from_case(case)
+        t = element_table(c)
+        prog = PE.export(t, c.size, 0, ordering=ordering)
+        ca, cb = PE.element_coefs(t, 0)
+        if any(el.is_nonlinear for el in c.elements):
+            continue
+        x = PE.emulate(prog, t, c.size, ca, cb)
+        xo = oracle_lib.op(t, c.size)
+        np.testing.assert_allclose(x, xo, rtol=1e-9, atol=1e-12 * max(1.0, np.abs(xo).max()))
+
+
+@pytest.mark.parametrize("method,h", [("be", 1e-12), ("tr", 1e-12), ("tr", 1e-9), ("be", 1e-6)])
+def test_tran_programs_match_dense(built_lib, oracle_lib, method, h):
+    c = rlc_ladder(60)
+    t = element_table(c)
+    n = c.size
+    prev = np.cos(np.arange(n) * 0.37)
+    prog = PE.export(t, n, 2, method=method, h=h)
+    ca, cb = PE.element_coefs(t, 2, method, h, prev=prev, t_src=0.0, icap=np.zeros(len(t)))
+    x = PE.emulate(prog, t, n, ca, cb)
+    A, b = oracle_lib.assemble(t, n, "tran", h, method, sol=prev)
+    xd = np.linalg.solve(A, b)
+    # norm-wise: both solutions carry rounding of order cond(A) * eps
+    np.testing.assert_allclose(x, xd, rtol=0, atol=1e-9 * np.abs(xd).max())
+
+
+def test_ac_program_static_pivots_hold_over_nine_decades(built_lib, oracle_lib):
+    c = rc_ladder_ac(120)
+    t = element_table(c)
+    prog = PE.export(t, c.size, 1, freq=3.16e4)
+    for f in (1.0, 1e3, 1e6, 1e9):
+        ca, cb = PE.element_coefs(t, 1, freq=f)
+        x = PE.emulate(prog, t, c.size, ca, cb, complex_=True)
+        z = oracle_lib.ac(t, c.size, [f])[0]
+        np.testing.assert_allclose(x, z, rtol=1e-9, atol=1e-13 * np.abs(z).max())
+
+
+def test_nested_dissection_gives_log_depth_on_ladders(built_lib):
+    c = config1_circuit()
+    prog = PE.export(element_table(c), c.size, 0, ordering=2)
+    assert prog["meta"][4] <= 24 and prog["meta"][5] <= 24      # ~2 log2(1001) levels
+    nat = PE.export(element_table(c), c.size, 0, ordering=0)
+    assert nat["meta"][4] >= 900                                 # natural order: a chain
+    auto = PE.export(element_table(c), c.size, 0)
+    assert auto["meta"][0] == 2                                  # the cost model picks ND
+
+
+def test_stamp_contributions_keep_emission_order(built_lib):
+    # a node with three resistors: the diagonal entry sums 1/R in element order
+    c = parse_circuit_description("V1 a 0 1\nR1 a 0 3\nR2 a 0 7\nR3 a 0 11\n")
+    t = element_table(c)
+    prog = PE.export(t, c.size, 0)
+    a = c.index_map["V(a)"]
+    qinv = np.argsort(prog["q"])
+    pinv = np.argsort(prog["prow"])
+    row = pinv[a]
+    found = False
+    for tt in range(prog["a_rowptr"][row], prog["a_rowptr"][row + 1]):
+        if prog["a_col"][tt] == qinv[a]:
+            codes = prog["a_contrib"][prog["a_cptr"][tt]:prog["a_cptr"][tt + 1]]
+            assert [int(x) >> 2 for x in codes] == [1, 2, 3]
+            found = True
+    assert found
+
+
+def test_singular_topology_is_reported(built_lib):
+    from krets_gb300 import _lib
+    from krets_gb300.errors import DecompositionFailed
+    # node b floats in DC (only a capacitor attaches it)
+    c = parse_circuit_description("V1 a 0 1\nR1 a 0 1\nC1 a b 1e-6\n")
+    with pytest.raises(DecompositionFailed):
+        PE.export(element_table(c), c.size, 0)
+
+
+def test_monte_carlo_values_deterministic():
+    c = rlc_ladder(10)
+    v1 = monte_carlo_values(c, 4, seed=9)
+    v2 = monte_carlo_values(c, 4, seed=9)
+    np.testing.assert_array_equal(v1, v2)
+    assert v1.shape == (4, len(c.elements))
+    assert np.all(v1[:, 0] == 0.0)            # the source value is not perturbed
