@@ -231,7 +231,12 @@ __global__ void k_tran_step(DevProg P, KCfg cfg, TranState st, double h, int met
       st.icap[e] = st.ca[e] * vn - st.cb[e];
     }
   }
-  for (int k = threadIdx.x; k < P.n; k += blockDim.x) x_out[(size_t)s * P.n + P.q[k]] = x[k];
+  int nonfinite = 0;
+  for (int k = threadIdx.x; k < P.n; k += blockDim.x) {
+    nonfinite |= !isfinite(x[k]);
+    x_out[(size_t)s * P.n + P.q[k]] = x[k];
+  }
+  if (__syncthreads_or(nonfinite) && threadIdx.x == 0) atomicOr(st.status, KS_NONFINITE);
   __syncthreads();
   if (threadIdx.x == 0) *st.step = s;
 }
@@ -433,7 +438,13 @@ __global__ void k_tran_batch(DevProg P, KCfg cfg, Lay L, char *gws, const double
         }
       }
       double *row = out + (size_t)s * P.n;
-      for (int k = threadIdx.x; k < P.n; k += blockDim.x) __stcs(row + P.q[k], x[k]);
+      int nonfinite = 0;
+      for (int k = threadIdx.x; k < P.n; k += blockDim.x) {
+        double v = x[k];
+        nonfinite |= !isfinite(v);
+        __stcs(row + P.q[k], v);
+      }
+      if (__syncthreads_or(nonfinite) && threadIdx.x == 0) atomicOr(status, KS_NONFINITE);
       __syncthreads();
     }
     if (threadIdx.x == 0 && inst_status) inst_status[inst] = *status;

@@ -107,7 +107,8 @@ bool emit(const krets_element &x, int e, int mode, std::vector<MEntry> &M, std::
 }
 
 // Representative value of an element's matrix coefficient (for pivot selection only).
-std::complex<double> rep_coef(const krets_element &x, int mode, int method, double h, double f) {
+std::complex<double> rep_coef(const krets_element &x, int mode, int method, double h, double f,
+                              bool rep_diode_zero) {
   switch (x.kind) {
     case KRETS_ELEM_R:
       return (x.flags & KRETS_FLAG_G2) ? x.value : 1.0 / x.value;
@@ -117,10 +118,15 @@ std::complex<double> rep_coef(const krets_element &x, int mode, int method, doub
     case KRETS_ELEM_L:
       if (mode == MODE_AC) return std::complex<double>(0.0, 2.0 * kPi * f * x.value);
       return (method == KRETS_METHOD_TR ? 2.0 : 1.0) * x.value / h;
-    case KRETS_ELEM_D: {
-      double n = x.wp[0] > 0 ? x.wp[0] : 1.0;
-      return (x.value / (n * kVt)) * std::exp(std::min(0.5 / (n * kVt), 700.0));
-    }
+    case KRETS_ELEM_D:
+      // A diode's conductance spans ~150 decades between reverse and forward bias, so
+      // pivots must not rely on it: it is taken as 0 (the caller retries with the 0.5 V
+      // value only if the matrix is singular without it).
+      if (rep_diode_zero) return 0.0;
+      {
+        double n = x.wp[0] > 0 ? x.wp[0] : 1.0;
+        return (x.value / (n * kVt)) * std::exp(std::min(0.5 / (n * kVt), 700.0));
+      }
     default:
       return 1.0;
   }
@@ -359,7 +365,7 @@ std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<in
 // ------------------------------------------------------------------ program
 static int build_with_order(const krets_element *el, int ne, int n, int mode, int method, double h, double f,
                             const std::vector<MEntry> &M, const std::vector<BEntry> &B,
-                            const std::vector<int> &q, Program &P, std::string &msg) {
+                            const std::vector<int> &q, Program &P, std::string &msg, bool rep_diode_zero) {
   P = Program();
   P.mode = mode;
   P.method = method;
@@ -367,7 +373,7 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
   P.ne = ne;
   // ---- representative numeric matrix (CSC, summed), for pivot selection
   std::vector<std::complex<double>> coef(ne);
-  for (int e = 0; e < ne; ++e) coef[e] = rep_coef(el[e], mode, method, h, f);
+  for (int e = 0; e < ne; ++e) coef[e] = rep_coef(el[e], mode, method, h, f, rep_diode_zero);
   std::vector<std::pair<long long, std::complex<double>>> ent;
   ent.reserve(M.size());
   for (auto &m : M) {
@@ -607,7 +613,9 @@ int build_program(const krets_element *el, int ne, int n, int mode, int method, 
     }
     Program P;
     std::string m2;
-    int st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2);
+    int st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, true);
+    if (st == KRETS_ERR_DECOMPOSITION_FAILED)  // only singular without diode conductances
+      st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, false);
     if (st != KRETS_OK) {
       if (best_st != KRETS_OK) { best_st = st; best_msg = m2; }
       continue;

@@ -21,6 +21,8 @@ def rel_err(x, ref, cur_mask):
     """max over {voltages, currents} of max|x - ref| / max|ref| (arrays [..., n])."""
     x = np.asarray(x)
     ref = np.asarray(ref)
+    if not (np.all(np.isfinite(x)) and np.all(np.isfinite(ref))):
+        return np.inf
     worst = 0.0
     for m in (cur_mask, ~cur_mask):
         if not m.any():
