@@ -6,6 +6,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -13,6 +14,7 @@
 #include <vector>
 
 #include "kernels.cuh"
+#include "warp_kernels.cuh"
 #include "krets_gpu.h"
 #include "symbolic.h"
 
@@ -110,6 +112,7 @@ struct krets_circuit {
   unsigned long long *d_hist = nullptr;
   long long hist[8] = {};
   int fallbacks = 0;
+  int warps_per_cta = 0, grid = 0;
   void *l2buf = nullptr;
 
   ~krets_circuit() {
@@ -159,6 +162,8 @@ krets_status upload_program(krets_circuit *c, Program &&P, DevProgram &D) {
   size_t i_bcp = vi(H.b_cptr), i_bcn = vi(H.b_contrib), i_pp = vi(H.piv_ptr), i_pv = vi(H.piv), i_up = vi(H.upd);
   size_t i_lp = vi(H.lev_ptr), i_lr = vi(H.lev_rows), i_ulp = vi(H.ulev_ptr), i_ulr = vi(H.ulev_rows);
   size_t i_ep = vi(H.el_pos), i_ic = vi(is_cur);
+  size_t i_qi = vi(H.qinv), i_ld = vi(H.ldesc), i_ud = vi(H.udesc), i_rp2 = vi(H.res_ptr), i_ro = vi(H.res_op);
+  size_t i_dy = vi(H.dyn_e), i_bdp = vi(H.bd_ptr), i_bdo = vi(H.bd_op), i_sp = vi(H.sprog);
   CU(cudaMalloc(&D.buf, total));
   std::vector<char> staging(total, 0);
   for (auto &p : parts)
@@ -196,6 +201,20 @@ krets_status upload_program(krets_circuit *c, Program &&P, DevProgram &D) {
   V.el_pos = (const int4 *)ptr(i_ep);
   V.is_cur = (const int *)ptr(i_ic);
   V.el = c->d_el;
+  V.qinv = (const int *)ptr(i_qi);
+  V.ldesc = (const int4 *)ptr(i_ld);
+  V.udesc = (const int4 *)ptr(i_ud);
+  V.res_ptr = (const int *)ptr(i_rp2);
+  V.res_op = (const int2 *)ptr(i_ro);
+  V.dyn_e = (const int *)ptr(i_dy);
+  V.bd_ptr = (const int *)ptr(i_bdp);
+  V.bd_op = (const int *)ptr(i_bdo);
+  V.ndyn = (int)H.dyn_e.size();
+  V.ncap = H.ncap;
+  V.n_resop = (int)H.res_op.size() / 2;
+  V.sprog = (const int *)ptr(i_sp);
+  for (int k = 0; k < 12; ++k) V.sp_off[k] = H.sp_off[k];
+  V.sprog_ok = H.sprog_ok;
   bool nl = false;
   for (int e = 0; e < H.ne; ++e) {
     int k = c->el[e].kind;
@@ -693,25 +712,76 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
   if (s) return s;
   bool mixed = precision == KRETS_PREC_MIXED;
   const DevProg &P = Dtr->view;
-  Lay L = layout_tran(P, mixed);
-  int threads = 128, grid;
-  size_t smem;
-  char *gws;
-  auto kern = mixed ? k_tran_batch<1> : k_tran_batch<0>;
-  s = plan_launch(c, kern, L, threads, n_inst, grid, smem, gws);
-  if (s) return s;
-  double *fb = nullptr;
-  if (mixed) {
-    CU(cudaMalloc(&tfb.p, sizeof(double) * (size_t)P.nnz_lu * grid));
-    fb = (double *)tfb.p;
-  }
   int *queue = c->d_small + 8;
   int *d_fallbacks = c->d_small + 12;
   CU(cudaMemsetAsync(c->d_small + 8, 0, 8 * sizeof(int), c->stream));
   CU(cudaMemsetAsync(c->d_hist, 0, 8 * sizeof(unsigned long long), c->stream));
-  CU(cudaEventRecord(c->ev[2], c->stream));
-  kern<<<grid, threads, smem, c->stream>>>(P, c->cfg, L, gws, (const double *)dv, n_inst, h, n_steps, method,
-                                           source_lag, (double *)dx, d_st, queue, c->d_hist, d_fallbacks, fb);
+  const char *eng = getenv("KRETS_ENGINE");
+  bool warp_engine = !(eng && strcmp(eng, "block") == 0);
+  WarpLay WL{};
+  size_t per_warp = 0;
+  if (warp_engine) {
+    size_t cur = 0;
+    auto put = [&](int &off, size_t bytes) { off = (int)cur; cur = align16(cur + bytes); };
+    put(WL.lu, (mixed ? 4 : 8) * (size_t)P.nnz_lu);
+    put(WL.coef, 8 * (size_t)P.ne);
+    put(WL.x, 8 * (size_t)P.n);
+    put(WL.b, 8 * (size_t)P.n);
+    put(WL.w, mixed ? 4 * (size_t)P.n : 0);
+    put(WL.cb, 8 * (size_t)P.ndyn);
+    put(WL.icap, 8 * (size_t)P.ncap);
+    put(WL.prev, P.nonlinear ? 8 * (size_t)P.n : 0);
+    put(WL.guess, P.nonlinear ? 8 * (size_t)P.n : 0);
+    WL.bytes = (int)align16(cur);
+    WL.sprog_bytes = (int)align16((size_t)P.sp_off[11] * sizeof(int));
+    per_warp = WL.bytes;
+    if (!P.sprog_ok || per_warp + WL.sprog_bytes > max_smem_optin()) warp_engine = false;
+  }
+  double *fb = nullptr;
+  if (warp_engine) {
+    const char *bud = getenv("KRETS_SMEM_BUDGET");
+    size_t budget = bud ? (size_t)atol(bud) : max_smem_optin();
+    budget = std::min(budget, max_smem_optin());
+    int W = (int)std::max<size_t>(1, std::min<size_t>(8, (budget - WL.sprog_bytes) / per_warp));
+    const char *wenv = getenv("KRETS_WARPS_PER_CTA");
+    if (wenv) W = std::max(1, std::min(8, atoi(wenv)));
+    while (W > 1 && WL.sprog_bytes + (size_t)W * per_warp > max_smem_optin()) --W;
+    size_t smem = WL.sprog_bytes + (size_t)W * per_warp;
+    auto kern = mixed ? k_tran_warp<1> : k_tran_warp<0>;
+    CU(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * W, smem));
+    if (per_sm < 1) return fail(KRETS_ERR_CUDA, "warp engine does not fit on an SM");
+    int grid = std::max(1, std::min((n_inst + W - 1) / W, per_sm * device_sm_count()));
+    if (mixed) {
+      CU(cudaMalloc(&tfb.p, sizeof(double) * (size_t)P.nnz_lu * grid * W));
+      fb = (double *)tfb.p;
+    }
+    const char *tenv = getenv("KRETS_REFINE_TOL");
+    double tol = tenv ? atof(tenv) : 1e-10;
+    c->warps_per_cta = W;
+    c->grid = grid;
+    CU(cudaEventRecord(c->ev[2], c->stream));
+    kern<<<grid, 32 * W, smem, c->stream>>>(P, c->cfg, WL, (const double *)dv, n_inst, h, n_steps, method,
+                                           source_lag, (double *)dx, d_st, queue, c->d_hist, d_fallbacks, fb, tol);
+  } else {
+    Lay L = layout_tran(P, mixed);
+    int threads = 128, grid;
+    size_t smem;
+    char *gws;
+    auto kern = mixed ? k_tran_batch<1> : k_tran_batch<0>;
+    s = plan_launch(c, kern, L, threads, n_inst, grid, smem, gws);
+    if (s) return s;
+    if (mixed) {
+      CU(cudaMalloc(&tfb.p, sizeof(double) * (size_t)P.nnz_lu * grid));
+      fb = (double *)tfb.p;
+    }
+    c->warps_per_cta = 0;
+    c->grid = grid;
+    CU(cudaEventRecord(c->ev[2], c->stream));
+    kern<<<grid, threads, smem, c->stream>>>(P, c->cfg, L, gws, (const double *)dv, n_inst, h, n_steps, method,
+                                             source_lag, (double *)dx, d_st, queue, c->d_hist, d_fallbacks, fb);
+  }
   g_launches++;
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[3], c->stream));

@@ -90,6 +90,20 @@ struct DevProg {
   const int *is_cur;     // [n] 1 when the unknown at this position is a branch current
   const krets_element *el;
   int nonlinear;         // any diode / MOSFET / BJT among the stamped elements
+  // step program (warp engine)
+  const int *qinv;       // [n] unknown -> position
+  const int4 *ldesc;     // [n] L-level-ordered {row, first, diag, end}
+  const int4 *udesc;     // [n] U-level-ordered {row, first, diag, end}
+  const int *res_ptr;    // [n+1]
+  const int2 *res_op;    // {col position, packed contribution}
+  const int *dyn_e;      // [ndyn] capacitors first
+  const int *bd_ptr;     // [n+1]
+  const int *bd_op;      // dyn << 1 | neg
+  int ndyn, ncap, n_resop;
+  // compact step program (global copy; the warp engine stages it in shared memory)
+  const int *sprog;
+  int sp_off[12];
+  int sprog_ok;
 };
 
 // status bits written by the engine

@@ -362,6 +362,71 @@ std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<in
   return order;
 }
 
+// ------------------------------------------------------------------ step program
+// Compact, shared-memory resident form of everything the per-step loop reads:
+//   [0] lev_ptr[nlev+1]      [1] ulev_ptr[nulev+1]
+//   [2] ldesc[n] int2 {row | nL << 16, first L slot}
+//   [3] udesc[n] int2 {row | nU << 16, diag slot}        (U entries follow the diag)
+//   [4] lu_col[nnz_lu] as uint16 pairs
+//   [5] res_ptr[n+1]  [6] res_op: col | neg << 15 | slot << 16  (slot 0 = incidence +-1,
+//       slot e+1 = coefficient of element e)
+//   [7] dyn[ndyn] int4 {e | kind << 24, p, m, b} (positions, -1 absent)
+//   [8] bd_ptr[n+1]   [9] bd_op (dyn << 1 | neg)   [10] qinv[n]   [11] end
+static void pack_step_program(const krets_element *el, Program &P) {
+  const int n = P.n;
+  P.sprog.clear();
+  P.sprog_ok = n < 32768 && P.ne < 65535 && P.max_row_lu < 65536;
+  if (!P.sprog_ok) return;
+  std::vector<int> &S = P.sprog;
+  auto mark = [&](int i) {
+    while (S.size() % 4) S.push_back(0);  // 16-byte alignment of each section
+    P.sp_off[i] = (int)S.size();
+  };
+  mark(0);
+  S.insert(S.end(), P.lev_ptr.begin(), P.lev_ptr.end());
+  mark(1);
+  S.insert(S.end(), P.ulev_ptr.begin(), P.ulev_ptr.end());
+  mark(2);
+  for (int t = 0; t < n; ++t) {
+    int k = P.lev_rows[t];
+    S.push_back(k | ((P.lu_diag[k] - P.lu_rowptr[k]) << 16));
+    S.push_back(P.lu_rowptr[k]);
+  }
+  mark(3);
+  for (int t = 0; t < n; ++t) {
+    int k = P.ulev_rows[t];
+    S.push_back(k | ((P.lu_rowptr[k + 1] - P.lu_diag[k] - 1) << 16));
+    S.push_back(P.lu_diag[k]);
+  }
+  mark(4);
+  for (size_t u = 0; u < P.lu_col.size(); u += 2) {
+    int lo = P.lu_col[u], hi = u + 1 < P.lu_col.size() ? P.lu_col[u + 1] : 0;
+    S.push_back(lo | (hi << 16));
+  }
+  mark(5);
+  S.insert(S.end(), P.res_ptr.begin(), P.res_ptr.end());
+  mark(6);
+  for (size_t u = 0; u < P.res_op.size(); u += 2) {
+    int col = P.res_op[u], code = P.res_op[u + 1];
+    int slot = (code & 2) ? 0 : (code >> 2) + 1;
+    S.push_back(col | ((code & 1) << 15) | (slot << 16));
+  }
+  mark(7);
+  for (int e : P.dyn_e) {
+    S.push_back(e | (el[e].kind << 24));
+    S.push_back(P.el_pos[4 * e + 0]);
+    S.push_back(P.el_pos[4 * e + 1]);
+    S.push_back(P.el_pos[4 * e + 2]);
+  }
+  mark(8);
+  S.insert(S.end(), P.bd_ptr.begin(), P.bd_ptr.end());
+  mark(9);
+  S.insert(S.end(), P.bd_op.begin(), P.bd_op.end());
+  mark(10);
+  S.insert(S.end(), P.qinv.begin(), P.qinv.end());
+  mark(11);
+}
+
 // ------------------------------------------------------------------ program
 static int build_with_order(const krets_element *el, int ne, int n, int mode, int method, double h, double f,
                             const std::vector<MEntry> &M, const std::vector<BEntry> &B,
@@ -528,6 +593,47 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
     const int idx[4] = {el[e].p, el[e].m, el[e].b, el[e].g};
     for (int t = 0; t < 4; ++t) P.el_pos[4 * e + t] = idx[t] >= 0 ? P.qinv[idx[t]] : -1;
   }
+  // ---- step program
+  for (int t = 0; t < n; ++t) {
+    int k = P.lev_rows[t];
+    P.ldesc.insert(P.ldesc.end(), {k, P.lu_rowptr[k], P.lu_diag[k], P.lu_rowptr[k + 1]});
+  }
+  for (int t = 0; t < n; ++t) {
+    int k = P.ulev_rows[t];
+    P.udesc.insert(P.udesc.end(), {k, P.lu_rowptr[k], P.lu_diag[k], P.lu_rowptr[k + 1]});
+  }
+  P.res_ptr.assign(n + 1, 0);
+  for (int r = 0; r < n; ++r) {
+    for (int t = P.a_rowptr[r]; t < P.a_rowptr[r + 1]; ++t)
+      for (int u = P.a_cptr[t]; u < P.a_cptr[t + 1]; ++u) P.res_op.insert(P.res_op.end(), {P.a_col[t], P.a_contrib[u]});
+    P.res_ptr[r + 1] = (int)P.res_op.size() / 2;
+  }
+  std::vector<int> dyn_of(ne, -1);
+  for (int pass = 0; pass < 2; ++pass)
+    for (int e = 0; e < ne; ++e) {
+      int k = el[e].kind;
+      bool cap = k == KRETS_ELEM_C;
+      bool dyn = cap || k == KRETS_ELEM_L || k == KRETS_ELEM_V || k == KRETS_ELEM_I || k == KRETS_ELEM_D;
+      if (!dyn || (pass == 0) != cap) continue;
+      if (mode == MODE_DC && cap) continue;
+      dyn_of[e] = (int)P.dyn_e.size();
+      P.dyn_e.push_back(e);
+      if (cap) P.ncap++;
+    }
+  P.bd_ptr.assign(n + 1, 0);
+  for (int r = 0; r < n; ++r) {
+    for (int u = P.b_cptr[r]; u < P.b_cptr[r + 1]; ++u) {
+      int code = P.b_contrib[u];
+      int d = dyn_of[code >> 1];
+      if (d < 0) {
+        msg = "internal: rhs contribution from a non-dynamic element";
+        return KRETS_ERR_UNEXPECTED;
+      }
+      P.bd_op.push_back((d << 1) | (code & 1));
+    }
+    P.bd_ptr[r + 1] = (int)P.bd_op.size();
+  }
+  pack_step_program(el, P);
   uint64_t sig = 1469598103934665603ull;
   sig = fnv1a(sig, (uint64_t)mode);
   sig = fnv1a(sig, (uint64_t)n);

@@ -49,6 +49,21 @@ struct Program {
   std::vector<int> lev_ptr, lev_rows, ulev_ptr, ulev_rows;
   // per element: p, m, b, g in POSITION space (-1 = absent)
   std::vector<int> el_pos;
+  // --- step program (used by the warp-per-instance engine)
+  // level-ordered row descriptors {row, first entry, diag slot, end}: L solve / U solve
+  std::vector<int> ldesc, udesc;
+  // residual ops per position row: {column position, packed contribution (pack_a)}
+  std::vector<int> res_ptr, res_op;
+  // elements with a right-hand-side coefficient (C, L, V, I, D), capacitors first
+  std::vector<int> dyn_e;
+  int ncap = 0;
+  // rhs contributions per position row, packed dyn_index << 1 | neg
+  std::vector<int> bd_ptr, bd_op;
+  // compact step program, copied into shared memory by the warp engine (sprog_ok = the
+  // sizes fit its 16-bit packing).  Layout and packing: see pack_step_program().
+  std::vector<int> sprog;
+  int sp_off[12] = {0};
+  bool sprog_ok = false;
   // per element: 1 when it is a capacitor whose TR history current is state
   long long factor_flops = 0;
   int max_row_lu = 0;

@@ -128,15 +128,38 @@ def test_batched_be_with_source_lag(oracle_lib):
     assert rel_err(x[0], ref, is_current_mask(c)) < TOL
 
 
-def test_batched_nonlinear_rectifier(oracle_lib, golden):
-    case = next(cc for cc in golden["tran"] if cc["name"] == "rectifier_tran")
-    c = circuit_from_case(case)
+HALF_WAVE = ("V1 in 0 SIN(0 5 60 0 0 0)\nR1 in a 10\nD1 a out DMOD\nC1 out 0 10u\nR2 out 0 1k\n"
+             ".model DMOD D (is=1e-12)\n")
+
+
+def test_nonlinear_transient_newton(oracle_lib):
+    """Diode half-wave rectifier: a Newton loop per step (transient.rs:51-109), BE with the
+    reference's source timing, plain and batched forms against the oracle."""
+    c = parse_circuit_description(HALF_WAVE)
     t = element_table(c)
     g = _lib.GpuCircuit(t, c.size)
-    ref = oracle_lib.tran(t, c.size, 50e-6, 300, method="be", lag=True)
+    ref, iters = oracle_lib.tran(t, c.size, 50e-6, 400, method="be", lag=True, return_iters=True)
+    assert iters.max() > 2                      # a genuinely nonlinear solve
+    mask = is_current_mask(c)
+    assert rel_err(g.tran(50e-6, 400, "be", lag=True), ref, mask) < TOL
+    vals = np.tile(t["value"], (3, 1))
     for prec in (_lib.PREC_FP64, _lib.PREC_MIXED):
-        x = g.batch_tran(None, 50e-6, 300, "be", lag=True, precision=prec, n_inst=1)
-        assert rel_err(x[0], ref, is_current_mask(c)) < 1e-8, prec
+        x = g.batch_tran(vals, 50e-6, 400, "be", lag=True, precision=prec)
+        for i in range(3):
+            assert rel_err(x[i], ref, mask) < TOL, prec
+
+
+def test_reference_rectifier_runs():
+    """The reference's rectifier test is smoke only (test_transient.rs:163-178): its
+    ground-anode diodes always see the 0.5 V default guess (diode.rs:26-30), and the
+    solution grows without bound, in the reference as here.  Check it runs to the end."""
+    import json
+    from conftest import GOLDEN
+    case = next(cc for cc in json.loads(GOLDEN.read_text())["tran"] if cc["name"] == "rectifier_tran")
+    c = circuit_from_case(case)
+    g = _lib.GpuCircuit(element_table(c), c.size)
+    x = g.tran(50e-6, 50, "be", lag=True)
+    assert x.shape == (51, c.size)
 
 
 @pytest.mark.parametrize("precision", [_lib.PREC_FP64, _lib.PREC_MIXED])
