@@ -183,6 +183,34 @@ krets_status krets_memcpy_d2h(void *dst, const void *src, size_t bytes);
 krets_status krets_flush_l2(krets_circuit *c);
 krets_status krets_device_synchronize(void);
 
+/* Allocation-free batched transient.  No counterpart in the reference.
+ *
+ * For callers that are not allowed to allocate device memory while they run: a host
+ * program that hands all GPU memory to its own arena at start-up and forbids hidden
+ * allocations, a real-time loop whose allocations must all happen before the loop starts,
+ * or code that enqueues work while another thread is capturing a CUDA graph in a mode in
+ * which cudaMalloc is an error.  krets_batch_tran may allocate temporary device buffers
+ * (scratch, staging of host buffers); this entry point does not call cudaMalloc or
+ * cudaFree at all.
+ *
+ *  - values (may be NULL: nominal values), x_out and inst_status must be device pointers
+ *    (same shapes as krets_batch_tran).
+ *  - The circuit must already hold the compiled programs for (method, h): call
+ *    krets_batch_tran once with the same time step and method during set-up.  Otherwise
+ *    the call fails with KRETS_ERR_INVALID_ARGUMENT.
+ *  - Its scratch is a fixed 16 MiB device array inside the library, present on every GPU
+ *    that loads the library until the process exits.  Requests that do not fit (too many
+ *    instances, or one instance's FP64 fallback factors too large) are rejected with
+ *    KRETS_ERR_INVALID_ARGUMENT; a smaller array only limits the number of concurrent CTAs.
+ *  - The first call on a device looks up that array's device address (once per device);
+ *    make that first call before any stream capture.
+ *  - Every call shares the array and clears what must start at zero on entry; calls that
+ *    overlap on the GPU (other threads, other handles) race on it.
+ *  - The call is synchronous and returns the combined status of all instances. */
+krets_status krets_batch_tran_noalloc(krets_circuit *c, int32_t n_inst, const double *values, double h,
+                                      int32_t n_steps, int32_t method, int32_t source_lag, int32_t precision,
+                                      double *x_out, int32_t *inst_status);
+
 /* ------------------------------------------------- symbolic-pass introspection
  * Builds the static program of a topology for one mode on the host (no GPU needed) and
  * copies array `which` (KRETS_PROG_*) into out[cap]; *len receives its length.  Used by

@@ -68,6 +68,7 @@ def lib():
             "krets_tran": [_P, _D, _I, _I, _I, _I, _P],
             "krets_batch_tran": [_P, _I, _P, _D, _I, _I, _I, _I, _P, _P],
             "krets_batch_ac": [_P, _I, _P, _P, _I, _I, _P, _P],
+            "krets_batch_tran_noalloc": [_P, _I, _P, _D, _I, _I, _I, _I, _P, _P],
             "krets_batch_op": [_P, _I, _P, _P, _P],
             "krets_last_timing": [_P, _P, _P],
             "krets_last_refine_stats": [_P, _P, _P],
@@ -228,6 +229,15 @@ class GpuCircuit:
         check(lib().krets_batch_tran(self.h, ni, ptr(values), h, n_steps, m, int(bool(lag)), precision, ptr(out),
                                      ptr(st)), "batch_tran")
         return out
+
+    def batch_tran_noalloc(self, d_values, h, n_steps, d_out, d_status, n_inst, method="tr", lag=None,
+                           precision=PREC_MIXED):
+        """krets_batch_tran_noalloc: device buffers only, no device allocation inside."""
+        m = METHOD[method]
+        if lag is None:
+            lag = m == 0
+        check(lib().krets_batch_tran_noalloc(self.h, n_inst, ptr(d_values), h, n_steps, m, int(bool(lag)),
+                                             precision, ptr(d_out), ptr(d_status)), "batch_tran_noalloc")
 
     def batch_ac(self, values, freqs, precision=PREC_MIXED, out=None):
         f = np.ascontiguousarray(freqs, dtype=np.float64)

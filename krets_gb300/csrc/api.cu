@@ -372,6 +372,57 @@ int plain_threads(const DevProg &P) {
 
 }  // namespace
 
+// ============================================ fixed scratch for the allocation-free entry
+// krets_batch_tran_noalloc() keeps all of its scratch (work-queue counter, refinement
+// statistics, per-instance operating-point status, FP64 fallback factors) in this array
+// instead of allocating it.  It is 16 MiB, lives on every GPU that loads the library until
+// the process exits, and is shared by every call on that GPU.
+#define KRETS_NOALLOC_SCRATCH_BYTES (16u << 20)
+static __device__ __align__(256) unsigned char g_noalloc_scratch[KRETS_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+// Device address of g_noalloc_scratch per device, looked up once per device (the host-side
+// name of the array is only a stand-in, never a device address).
+constexpr int kMaxDevices = 64;
+void *g_noalloc_addr[kMaxDevices] = {};
+
+krets_status noalloc_scratch_address(void **out) {
+  int dev = 0;
+  CU(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(KRETS_ERR_CUDA, "device index out of range");
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    CU(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return KRETS_OK;
+}
+
+// Lookup without building: the allocation-free entry uses only programs that an earlier
+// call already compiled and uploaded.
+DevProgram *find_program(krets_circuit *c, int mode, int method, double h, double f) {
+  char key[128];
+  snprintf(key, sizeof key, "%d/%d/%.17g/%.17g", mode, method, mode == MODE_TRAN ? h : 0.0, mode == MODE_AC ? f : 0.0);
+  auto it = c->progs.find(key);
+  return it == c->progs.end() ? nullptr : it->second.get();
+}
+
+// OR of the operating-point and transient statuses, folded into the caller's per-instance
+// status array, plus one summary word.
+__global__ void k_status_fold(const int *op_status, int *inst_status, int n, int *any) {
+  int acc = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int v = op_status[i] | inst_status[i];
+    inst_status[i] = v;
+    acc |= v;
+  }
+  if (acc) atomicOr(any, acc);
+}
+
+}  // namespace
+
 // ====================================================================== C ABI
 extern "C" {
 
@@ -886,6 +937,114 @@ krets_status krets_flush_l2(krets_circuit *c) {
 krets_status krets_device_synchronize(void) {
   CU(cudaDeviceSynchronize());
   return KRETS_OK;
+}
+
+// Batched transient for callers that must not allocate device memory (see krets_gpu.h).
+// Same kernels and results as krets_batch_tran with device-resident buffers; the scratch
+// that call would allocate comes from g_noalloc_scratch.
+krets_status krets_batch_tran_noalloc(krets_circuit *c, int32_t n_inst, const double *d_values, double h,
+                                      int32_t n_steps, int32_t method, int32_t source_lag, int32_t precision,
+                                      double *d_x_out, int32_t *d_inst_status) {
+  if (!c || n_inst <= 0 || n_steps < 0 || !(h > 0) || !d_x_out || !d_inst_status)
+    return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments to krets_batch_tran_noalloc");
+  if ((d_values && !is_device_ptr(d_values)) || !is_device_ptr(d_x_out) || !is_device_ptr(d_inst_status))
+    return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc needs device pointers for values, "
+                                            "x_out and inst_status");
+  DevProgram *Ddc = find_program(c, MODE_DC, 0, 0, 0);
+  DevProgram *Dtr = find_program(c, MODE_TRAN, method, h, 0);
+  if (!Ddc || !Dtr)
+    return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc: the circuit has no compiled program for this "
+                                            "time step and method; run krets_batch_tran once with them first");
+  const DevProg &P = Dtr->view;
+  const bool mixed = precision == KRETS_PREC_MIXED;
+  // operating point: its per-CTA workspace must fit in shared memory (no global workspace)
+  Lay Lop = layout_op(Ddc->view);
+  if (Lop.bytes > max_smem_optin())
+    return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc: circuit too large for the shared-memory "
+                                            "operating-point kernel");
+  // warp engine layout (identical to krets_batch_tran's)
+  WarpLay WL{};
+  size_t cur = 0;
+  auto put = [&](int &off, size_t bytes) { off = (int)cur; cur = align16(cur + bytes); };
+  put(WL.lu, (mixed ? 4 : 8) * (size_t)P.nnz_lu);
+  put(WL.coef, 8 * (size_t)P.ne);
+  put(WL.x, 8 * (size_t)P.n);
+  put(WL.b, 8 * (size_t)P.n);
+  put(WL.w, mixed ? 4 * (size_t)P.n : 0);
+  put(WL.cb, 8 * (size_t)P.ndyn);
+  put(WL.icap, 8 * (size_t)P.ncap);
+  put(WL.prev, P.nonlinear ? 8 * (size_t)P.n : 0);
+  put(WL.guess, P.nonlinear ? 8 * (size_t)P.n : 0);
+  WL.bytes = (int)align16(cur);
+  WL.sprog_bytes = (int)align16((size_t)P.sp_off[11] * sizeof(int));
+  const size_t per_warp = WL.bytes;
+  if (!P.sprog_ok || per_warp + WL.sprog_bytes > max_smem_optin())
+    return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc: circuit too large for the warp engine");
+  int W = (int)std::max<size_t>(1, std::min<size_t>(8, (max_smem_optin() - WL.sprog_bytes) / per_warp));
+  const size_t smem = WL.sprog_bytes + (size_t)W * per_warp;
+  auto kern = mixed ? k_tran_warp<1> : k_tran_warp<0>;
+  CU(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * W, smem));
+  if (per_sm < 1) return fail(KRETS_ERR_CUDA, "warp engine does not fit on an SM");
+  int grid = std::max(1, std::min((n_inst + W - 1) / W, per_sm * device_sm_count()));
+  // scratch layout: [0,64) counters, [64,128) histogram, [256, 256+4n) OP status, then the
+  // FP64 fallback factors of every warp slot (mixed precision)
+  const size_t op_off = 256;
+  const size_t lu_off = align16(op_off + sizeof(int) * (size_t)n_inst);
+  const size_t lu_slot = sizeof(double) * (size_t)P.nnz_lu;
+  if (lu_off > KRETS_NOALLOC_SCRATCH_BYTES)
+    return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc: too many instances for the 16 MiB scratch");
+  if (mixed) {
+    const size_t slots = (KRETS_NOALLOC_SCRATCH_BYTES - lu_off) / lu_slot;
+    if (slots < (size_t)W)
+      return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc: instance size exceeds the 16 MiB scratch");
+    grid = std::min(grid, (int)(slots / W));
+  }
+  void *scr = nullptr;
+  krets_status s = noalloc_scratch_address(&scr);
+  if (s) return s;
+  char *base = (char *)scr;
+  int *queue = (int *)(base + 0);
+  int *fallbacks = (int *)(base + 4);
+  int *any = (int *)(base + 8);
+  unsigned long long *hist = (unsigned long long *)(base + 64);
+  int *op_status = (int *)(base + op_off);
+  double *fb = mixed ? (double *)(base + lu_off) : nullptr;
+  CU(cudaEventRecord(c->ev[0], c->stream));
+  // everything that must start at zero: counters, histogram, statuses
+  CU(cudaMemsetAsync(base, 0, 256, c->stream));
+  CU(cudaMemsetAsync(op_status, 0, sizeof(int) * (size_t)n_inst, c->stream));
+  CU(cudaMemsetAsync(d_inst_status, 0, sizeof(int) * (size_t)n_inst, c->stream));
+  const size_t stride = (size_t)c->n * ((size_t)n_steps + 1);
+  int op_grid;
+  size_t op_smem;
+  char *op_gws;
+  s = plan_launch(c, k_op, Lop, 128, n_inst, op_grid, op_smem, op_gws);
+  if (s) return s;
+  k_op<<<op_grid, 128, op_smem, c->stream>>>(Ddc->view, c->cfg, Lop, nullptr, d_values, d_x_out, stride, op_status,
+                                             nullptr, n_inst);
+  g_launches++;
+  CU(cudaGetLastError());
+  const char *tenv = getenv("KRETS_REFINE_TOL");
+  const double tol = tenv ? atof(tenv) : 1e-10;
+  CU(cudaEventRecord(c->ev[2], c->stream));
+  kern<<<grid, 32 * W, smem, c->stream>>>(P, c->cfg, WL, d_values, n_inst, h, n_steps, method, source_lag, d_x_out,
+                                         d_inst_status, queue, hist, fallbacks, fb, tol);
+  g_launches++;
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(c->ev[3], c->stream));
+  k_status_fold<<<std::max(1, std::min(1024, (n_inst + 255) / 256)), 256, 0, c->stream>>>(op_status, d_inst_status,
+                                                                                         n_inst, any);
+  g_launches++;
+  CU(cudaGetLastError());
+  int any_h = 0;
+  CU(cudaMemcpyAsync(&any_h, any, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaEventRecord(c->ev[1], c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  cudaEventElapsedTime(&c->kernel_ms, c->ev[2], c->ev[3]);
+  cudaEventElapsedTime(&c->call_ms, c->ev[0], c->ev[1]);
+  return map_status(any_h, 1);
 }
 
 }  // extern "C"
