@@ -100,7 +100,12 @@ typedef struct krets_config {
 
 /* Precision of the batched transient/AC engines. */
 #define KRETS_PREC_FP64 0  /* FP64 factor and solves (the plain form's arithmetic)          */
-#define KRETS_PREC_MIXED 1 /* FP32 factor + solves, FP64 residual/state, iterative refinement */
+#define KRETS_PREC_MIXED 1 /* FP32 factor + solves, iterative refinement with an FP64-class
+                              residual (double-float pairs on FP32 pipes for linear circuits,
+                              FP64 for nonlinear ones) */
+#define KRETS_PREC_DF 2    /* factors computed in FP64, kept and applied as double-float pairs
+                              (48-bit significand) on FP32 pipes; linear circuits (nonlinear
+                              ones fall back to KRETS_PREC_MIXED) */
 
 typedef struct krets_circuit krets_circuit;
 

@@ -22,7 +22,7 @@ DECOMPOSITION_FAILED, MATRIX_BUILD, MATRIX_DECOMPOSITION, NOT_IMPLEMENTED = 5, 6
 TIMEOUT, CUDA, INVALID_ARGUMENT, OUT_OF_MEMORY, PIVOT_UNSTABLE = 9, 10, 11, 12, 13
 
 METHOD = {"be": 0, "tr": 1}
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_DF = 0, 1, 2
 MODE_DC, MODE_AC, MODE_TRAN = 0, 1, 2
 
 PROG_ARRAYS = ["q", "prow", "lu_rowptr", "lu_col", "lu_diag", "a_rowptr", "a_col", "a_slot", "a_cptr",

@@ -761,8 +761,10 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
   CU(cudaMemsetAsync(ts.p, 0, sizeof(int) * 2 * (size_t)n_inst, c->stream));
   s = run_op(c, Ddc, n_inst, (const double *)dv, (double *)dx, stride, d_opst, nullptr, 128);
   if (s) return s;
+  const bool dfd = precision == KRETS_PREC_DF;
   bool mixed = precision == KRETS_PREC_MIXED;
   const DevProg &P = Dtr->view;
+  if (dfd && P.nonlinear) mixed = true;  // nonlinear circuits: refactor per Newton iteration (FP32 + refinement)
   int *queue = c->d_small + 8;
   int *d_fallbacks = c->d_small + 12;
   CU(cudaMemsetAsync(c->d_small + 8, 0, 8 * sizeof(int), c->stream));
@@ -778,7 +780,7 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
     put(WL.coef, 8 * (size_t)P.ne);
     put(WL.x, 8 * (size_t)P.n);
     put(WL.b, 8 * (size_t)P.n);
-    put(WL.w, mixed ? 4 * (size_t)P.n : 0);
+    put(WL.w, mixed ? 4 * (size_t)P.n : 16);  // double-float direct: the group's 4 status words
     put(WL.cb, 8 * (size_t)P.ndyn);
     put(WL.icap, 8 * (size_t)P.ncap);
     put(WL.prev, P.nonlinear ? 8 * (size_t)P.n : 0);
@@ -789,7 +791,43 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
     if (!P.sprog_ok || per_warp + WL.sprog_bytes > max_smem_optin()) warp_engine = false;
   }
   double *fb = nullptr;
-  if (warp_engine) {
+  if (warp_engine && dfd && !P.nonlinear) {
+    // double-float direct: one instance per group of G threads (default 128)
+    DfdLay DL{};
+    size_t cur = 0;
+    auto put = [&](int &off, size_t bytes) { off = (int)cur; cur = align16(cur + bytes); };
+    put(DL.lu, 8 * (size_t)P.nnz_lu);
+    put(DL.x, 8 * (size_t)P.n);
+    put(DL.cdyn, 8 * (size_t)P.ndyn);
+    put(DL.cb, 8 * (size_t)P.ndyn);
+    put(DL.icap, 8 * (size_t)P.ncap);
+    DL.coef64 = DL.x;  // set-up scratch over x / cdyn / cb / icap (+ padding if needed)
+    if (cur - DL.x < 8 * (size_t)P.ne) cur = DL.x + align16(8 * (size_t)P.ne);
+    put(DL.slot, 16);
+    DL.bytes = (int)align16(cur);
+    DL.sprog_bytes = WL.sprog_bytes;
+    const char *genv = getenv("KRETS_GROUP");
+    int G = genv ? atoi(genv) : 128;
+    if (G != 32 && G != 64 && G != 128) G = 128;
+    if ((size_t)DL.bytes + DL.sprog_bytes > max_smem_optin())
+      return fail(KRETS_ERR_INVALID_ARGUMENT, "circuit too large for the double-float engine");
+    int W = (int)std::max<size_t>(1, std::min<size_t>(640 / G, (max_smem_optin() - DL.sprog_bytes) / DL.bytes));
+    const size_t smem = DL.sprog_bytes + (size_t)W * DL.bytes;
+    const char *oenv = getenv("KRETS_DFD_OPTS");
+    const int opts = oenv ? atoi(oenv) : 0;
+    void (*kd)(DevProg, KCfg, DfdLay, const double *, int, double, int, int, int, double *, int *, int *, int) =
+        G == 32 ? k_tran_dfd<32> : (G == 64 ? k_tran_dfd<64> : k_tran_dfd<128>);
+    CU(cudaFuncSetAttribute(kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kd, G * W, smem));
+    if (per_sm < 1) return fail(KRETS_ERR_CUDA, "double-float engine does not fit on an SM");
+    int grid = std::max(1, std::min((n_inst + W - 1) / W, per_sm * device_sm_count()));
+    c->warps_per_cta = W * G / 32;
+    c->grid = grid;
+    CU(cudaEventRecord(c->ev[2], c->stream));
+    kd<<<grid, G * W, smem, c->stream>>>(P, c->cfg, DL, (const double *)dv, n_inst, h, n_steps, method, source_lag,
+                                        (double *)dx, d_st, queue, opts);
+  } else if (warp_engine) {
     const char *bud = getenv("KRETS_SMEM_BUDGET");
     size_t budget = bud ? (size_t)atol(bud) : max_smem_optin();
     budget = std::min(budget, max_smem_optin());
@@ -799,9 +837,14 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
     while (W > 1 && WL.sprog_bytes + (size_t)W * per_warp > max_smem_optin()) --W;
     size_t smem = WL.sprog_bytes + (size_t)W * per_warp;
     auto kern = mixed ? k_tran_warp<1> : k_tran_warp<0>;
+    // linear circuits in mixed precision take the double-float variant (FP32 pipes)
+    const char *dfenv = getenv("KRETS_DF");
+    const bool use_df = mixed && !P.nonlinear && !(dfenv && dfenv[0] == '0');
     CU(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CU(cudaFuncSetAttribute(k_tran_warp_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * W, smem));
+    if (use_df) CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tran_warp_df, 32 * W, smem));
+    else CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * W, smem));
     if (per_sm < 1) return fail(KRETS_ERR_CUDA, "warp engine does not fit on an SM");
     int grid = std::max(1, std::min((n_inst + W - 1) / W, per_sm * device_sm_count()));
     if (mixed) {
@@ -809,12 +852,16 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
       fb = (double *)tfb.p;
     }
     const char *tenv = getenv("KRETS_REFINE_TOL");
-    double tol = tenv ? atof(tenv) : 1e-10;
+    double tol = tenv ? atof(tenv) : 1e-8;
     c->warps_per_cta = W;
     c->grid = grid;
     CU(cudaEventRecord(c->ev[2], c->stream));
-    kern<<<grid, 32 * W, smem, c->stream>>>(P, c->cfg, WL, (const double *)dv, n_inst, h, n_steps, method,
-                                           source_lag, (double *)dx, d_st, queue, c->d_hist, d_fallbacks, fb, tol);
+    if (use_df)
+      k_tran_warp_df<<<grid, 32 * W, smem, c->stream>>>(P, c->cfg, WL, (const double *)dv, n_inst, h, n_steps, method,
+                                                       source_lag, (double *)dx, d_st, queue, c->d_hist, (float)tol);
+    else
+      kern<<<grid, 32 * W, smem, c->stream>>>(P, c->cfg, WL, (const double *)dv, n_inst, h, n_steps, method,
+                                             source_lag, (double *)dx, d_st, queue, c->d_hist, d_fallbacks, fb, tol);
   } else {
     Lay L = layout_tran(P, mixed);
     int threads = 128, grid;

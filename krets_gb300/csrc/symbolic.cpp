@@ -271,7 +271,7 @@ std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<in
   order.reserve(n);
   std::vector<int> in_set(n, -1), level(n, -1);
   int stamp = 0;
-  const int kLeaf = 4;
+  const int kLeaf = 1;
   // explicit stack of vertex sets to avoid deep recursion
   std::function<void(std::vector<int> &)> nd = [&](std::vector<int> &V) {
     if ((int)V.size() <= kLeaf) {
@@ -337,10 +337,15 @@ std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<in
       // separator: smallest level in the middle third (by vertex count)
       std::vector<int> cum(L + 1, 0);
       for (int l = 0; l < L; ++l) cum[l + 1] = cum[l] + (int)levels[l].size();
+      // smallest separator level in the middle half; among equally small ones, the most
+      // balanced split (keeps the elimination tree shallow)
       int total = cum[L], best = -1;
+      auto imbalance = [&](int l) { return std::abs(cum[l] - (total - cum[l + 1])); };
       for (int l = 1; l < L - 1; ++l) {
         if (cum[l] < total / 4 || cum[l + 1] > total - total / 4) continue;
-        if (best < 0 || levels[l].size() < levels[best].size()) best = l;
+        if (best < 0 || levels[l].size() < levels[best].size() ||
+            (levels[l].size() == levels[best].size() && imbalance(l) < imbalance(best)))
+          best = l;
       }
       if (best < 0) {
         best = 1;
@@ -365,22 +370,31 @@ std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<in
 // ------------------------------------------------------------------ step program
 // Compact, shared-memory resident form of everything the per-step loop reads:
 //   [0] lev_ptr[nlev+1]      [1] ulev_ptr[nulev+1]
-//   [2] ldesc[n] int2 {row | nL << 16, first L slot}
-//   [3] udesc[n] int2 {row | nU << 16, diag slot}        (U entries follow the diag)
+//   [2] ldesc[n] int4, level order   [3] udesc[n] int4, U-level order
+//       {row | rest << 16, base slot, col0 | col1 << 16, nfast}: the first nfast (<= 2)
+//       entries of the row's L part (U part) are at base, base+1 (base+1, base+2 after the
+//       diagonal at base) with columns col0, col1; the remaining `rest` entries follow
+//       contiguously and take their columns from lu_col
 //   [4] lu_col[nnz_lu] as uint16 pairs
-//   [5] res_ptr[n+1]  [6] res_op: col | neg << 15 | slot << 16  (slot 0 = incidence +-1,
+//   [5] res_row[n] int2 {first op, n_unit | n_total << 16}
+//   [6] res_op: col | neg << 15 | slot << 16 (slot 0 = incidence +-1 entries, listed first;
 //       slot e+1 = coefficient of element e)
 //   [7] dyn[ndyn] int4 {e | kind << 24, p, m, b} (positions, -1 absent)
 //   [8] bd_ptr[n+1]   [9] bd_op (dyn << 1 | neg)   [10] qinv[n]   [11] end
 static void pack_step_program(const krets_element *el, Program &P) {
   const int n = P.n;
   P.sprog.clear();
-  P.sprog_ok = n < 32768 && P.ne < 65535 && P.max_row_lu < 65536;
+  P.sprog_ok = n < 32768 && P.ne < 65535 && P.max_row_lu < 32768;
   if (!P.sprog_ok) return;
   std::vector<int> &S = P.sprog;
   auto mark = [&](int i) {
     while (S.size() % 4) S.push_back(0);  // 16-byte alignment of each section
     P.sp_off[i] = (int)S.size();
+  };
+  auto desc = [&](int k, int first, int cnt, int base) {
+    const int nf = std::min(cnt, 2);
+    const int c0 = nf > 0 ? P.lu_col[first] : k, c1 = nf > 1 ? P.lu_col[first + 1] : k;
+    S.insert(S.end(), {k | ((cnt - nf) << 16), base, c0 | (c1 << 16), nf});
   };
   mark(0);
   S.insert(S.end(), P.lev_ptr.begin(), P.lev_ptr.end());
@@ -389,14 +403,12 @@ static void pack_step_program(const krets_element *el, Program &P) {
   mark(2);
   for (int t = 0; t < n; ++t) {
     int k = P.lev_rows[t];
-    S.push_back(k | ((P.lu_diag[k] - P.lu_rowptr[k]) << 16));
-    S.push_back(P.lu_rowptr[k]);
+    desc(k, P.lu_rowptr[k], P.lu_diag[k] - P.lu_rowptr[k], P.lu_rowptr[k]);
   }
   mark(3);
   for (int t = 0; t < n; ++t) {
     int k = P.ulev_rows[t];
-    S.push_back(k | ((P.lu_rowptr[k + 1] - P.lu_diag[k] - 1) << 16));
-    S.push_back(P.lu_diag[k]);
+    desc(k, P.lu_diag[k] + 1, P.lu_rowptr[k + 1] - P.lu_diag[k] - 1, P.lu_diag[k]);
   }
   mark(4);
   for (size_t u = 0; u < P.lu_col.size(); u += 2) {
@@ -404,13 +416,23 @@ static void pack_step_program(const krets_element *el, Program &P) {
     S.push_back(lo | (hi << 16));
   }
   mark(5);
-  S.insert(S.end(), P.res_ptr.begin(), P.res_ptr.end());
-  mark(6);
-  for (size_t u = 0; u < P.res_op.size(); u += 2) {
-    int col = P.res_op[u], code = P.res_op[u + 1];
-    int slot = (code & 2) ? 0 : (code >> 2) + 1;
-    S.push_back(col | ((code & 1) << 15) | (slot << 16));
+  std::vector<int> ops;
+  std::vector<int> rows;
+  for (int r = 0; r < n; ++r) {
+    std::vector<int> unit, coef;
+    for (int u = P.res_ptr[r]; u < P.res_ptr[r + 1]; ++u) {
+      int col = P.res_op[2 * u], code = P.res_op[2 * u + 1];
+      int slot = (code & 2) ? 0 : (code >> 2) + 1;
+      (slot ? coef : unit).push_back(col | ((code & 1) << 15) | (slot << 16));
+    }
+    rows.push_back((int)ops.size());
+    rows.push_back((int)unit.size() | ((int)(unit.size() + coef.size()) << 16));
+    ops.insert(ops.end(), unit.begin(), unit.end());
+    ops.insert(ops.end(), coef.begin(), coef.end());
   }
+  S.insert(S.end(), rows.begin(), rows.end());
+  mark(6);
+  S.insert(S.end(), ops.begin(), ops.end());
   mark(7);
   for (int e : P.dyn_e) {
     S.push_back(e | (el[e].kind << 24));

@@ -33,9 +33,10 @@ __device__ __forceinline__ double warp_max(double v) {
 // Shared-memory view of the compact step program (layout: pack_step_program()).
 struct SProg {
   const int *lev_ptr, *ulev_ptr;
-  const int2 *ldesc, *udesc;
+  const int4 *ldesc, *udesc;
   const unsigned short *lu_col;
-  const int *res_ptr, *res_op;
+  const int2 *res_row;
+  const int *res_op;
   const int4 *dyn;
   const int *bd_ptr, *bd_op, *qinv;
   int nlev, nulev;
@@ -45,10 +46,10 @@ __device__ __forceinline__ SProg sprog_view(const DevProg &P, const int *sp) {
   SProg S;
   S.lev_ptr = sp + P.sp_off[0];
   S.ulev_ptr = sp + P.sp_off[1];
-  S.ldesc = reinterpret_cast<const int2 *>(sp + P.sp_off[2]);
-  S.udesc = reinterpret_cast<const int2 *>(sp + P.sp_off[3]);
+  S.ldesc = reinterpret_cast<const int4 *>(sp + P.sp_off[2]);
+  S.udesc = reinterpret_cast<const int4 *>(sp + P.sp_off[3]);
   S.lu_col = reinterpret_cast<const unsigned short *>(sp + P.sp_off[4]);
-  S.res_ptr = sp + P.sp_off[5];
+  S.res_row = reinterpret_cast<const int2 *>(sp + P.sp_off[5]);
   S.res_op = sp + P.sp_off[6];
   S.dyn = reinterpret_cast<const int4 *>(sp + P.sp_off[7]);
   S.bd_ptr = sp + P.sp_off[8];
@@ -59,36 +60,53 @@ __device__ __forceinline__ SProg sprog_view(const DevProg &P, const int *sp) {
   return S;
 }
 
-// Unit-lower solve, level by level (level 0 rows have no L entries).
-template <typename T, typename V>
-__device__ __forceinline__ void s_lsolve(const SProg &S, const T *lu, V *y, int lane) {
-  for (int l = 1; l < S.nlev; ++l) {
-    const int r0 = S.lev_ptr[l], r1 = S.lev_ptr[l + 1];
-    for (int t = r0 + lane; t < r1; t += 32) {
-      const int2 d = S.ldesc[t];
-      const int k = d.x & 0xffff, cnt = (int)((unsigned)d.x >> 16);
-      V s = y[k];
-      for (int j = 0; j < cnt; ++j) s -= V(lu[d.y + j]) * y[S.lu_col[d.y + j]];
-      y[k] = s;
+// One row of a triangular solve: y[k] - sum(l * y[col]) (times the reciprocal diagonal
+// for U).  The first two entries come from the descriptor, so their loads issue together.
+template <typename T, typename V, bool UPPER>
+__device__ __forceinline__ V s_row(const SProg &S, const T *__restrict__ lu, const V *y, const int4 d, int &k) {
+  k = d.x & 0xffff;
+  const int rest = (int)((unsigned)d.x >> 16);
+  const int first = UPPER ? d.y + 1 : d.y;
+  const int c0 = d.z & 0xffff, c1 = (int)((unsigned)d.z >> 16);
+  const V a0 = d.w > 0 ? V(lu[first]) : V(0);
+  const V a1 = d.w > 1 ? V(lu[first + 1]) : V(0);
+  V s = y[k];
+  s -= a0 * y[c0];
+  s -= a1 * y[c1];
+  for (int j = 2; j < 2 + rest; ++j) s -= V(lu[first + j]) * y[S.lu_col[first + j]];
+  if (UPPER) s *= V(lu[d.y]);
+  return s;
+}
+
+// Level-scheduled solve, two rows per lane in flight.
+template <typename T, typename V, bool UPPER>
+__device__ __forceinline__ void s_solve(const SProg &S, const T *__restrict__ lu, V *y, int lane) {
+  const int nl = UPPER ? S.nulev : S.nlev;
+  const int *ptr = UPPER ? S.ulev_ptr : S.lev_ptr;
+  const int4 *desc = UPPER ? S.udesc : S.ldesc;
+  for (int l = UPPER ? 0 : 1; l < nl; ++l) {  // L level 0 rows have no L entries
+    const int r0 = ptr[l], r1 = ptr[l + 1];
+    for (int t = r0 + lane; t < r1; t += 64) {
+      int k0, k1 = -1;
+      const V v0 = s_row<T, V, UPPER>(S, lu, y, desc[t], k0);
+      V v1 = V(0);
+      if (t + 32 < r1) v1 = s_row<T, V, UPPER>(S, lu, y, desc[t + 32], k1);
+      y[k0] = v0;
+      if (k1 >= 0) y[k1] = v1;
     }
     __syncwarp();
   }
 }
 
+template <typename T, typename V>
+__device__ __forceinline__ void s_lsolve(const SProg &S, const T *lu, V *y, int lane) {
+  s_solve<T, V, false>(S, lu, y, lane);
+}
+
 // Upper solve; the diagonal slots hold reciprocals (see w_factor).
 template <typename T, typename V>
 __device__ __forceinline__ void s_usolve(const SProg &S, const T *lu, V *y, int lane) {
-  for (int l = 0; l < S.nulev; ++l) {
-    const int r0 = S.ulev_ptr[l], r1 = S.ulev_ptr[l + 1];
-    for (int t = r0 + lane; t < r1; t += 32) {
-      const int2 d = S.udesc[t];
-      const int k = d.x & 0xffff, cnt = (int)((unsigned)d.x >> 16);
-      V s = y[k];
-      for (int j = 1; j <= cnt; ++j) s -= V(lu[d.y + j]) * y[S.lu_col[d.y + j]];
-      y[k] = s * V(lu[d.y]);
-    }
-    __syncwarp();
-  }
+  s_solve<T, V, true>(S, lu, y, lane);
 }
 
 // Static-pivot up-looking LU, rows of a level spread over the lanes; afterwards every
@@ -228,10 +246,16 @@ __device__ int s_refine(const DevProg &P, const SProg &S, const double *coef, co
   for (int it = 0; it < max_it; ++it) {
     for (int k = lane; k < P.n; k += 32) {
       double r = b[k];
-      for (int u = S.res_ptr[k]; u < S.res_ptr[k + 1]; ++u) {
-        const int op = S.res_op[u];
-        const int slot = (int)((unsigned)op >> 16);
-        const double a = slot ? coef[slot - 1] : 1.0;
+      const int2 rr = S.res_row[k];
+      const int nu = rr.y & 0xffff, nt = (int)((unsigned)rr.y >> 16);
+      for (int u = 0; u < nu; ++u) {
+        const int op = S.res_op[rr.x + u];
+        const double xj = x[op & 0x7fff];
+        r = (op & 0x8000) ? r + xj : r - xj;
+      }
+      for (int u = nu; u < nt; ++u) {
+        const int op = S.res_op[rr.x + u];
+        const double a = coef[((unsigned)op >> 16) - 1];
         r = fma((op & 0x8000) ? a : -a, x[op & 0x7fff], r);
       }
       w[k] = (float)r;
@@ -280,7 +304,7 @@ struct WarpLay {
 };
 
 template <int MIXED>
-__global__ void __launch_bounds__(256) k_tran_warp(DevProg P, KCfg cfg, WarpLay L, const double *values, int n_inst,
+__global__ void __launch_bounds__(256, 1) k_tran_warp(DevProg P, KCfg cfg, WarpLay L, const double *values, int n_inst,
                                                    double h, int n_steps, int method, int lag, double *x_out,
                                                    int *inst_status, int *queue, unsigned long long *hist,
                                                    int *fallbacks, double *lu64_scratch, double tol) {
@@ -419,6 +443,462 @@ __global__ void __launch_bounds__(256) k_tran_warp(DevProg P, KCfg cfg, WarpLay 
       for (int k = 0; k < 8; ++k)
         if (lh[k]) atomicAdd(hist + k, lh[k]);
     __syncwarp();
+  }
+}
+
+}  // namespace krets
+
+// ===================================================================== double-float path
+// Linear circuits, FP32 factors: the same step as k_tran_warp<1>, with the residual,
+// right-hand side, companion state and solution held in double-float (df.cuh) so the inner
+// loop runs on FP32 pipes.  FP64 is used at set-up (coefficients, LU values before rounding
+// to FP32), for source waveforms, and to write each solution row as FP64.
+#include "df.cuh"
+namespace krets {
+
+__device__ __forceinline__ float warp_maxf(float v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+
+__device__ __forceinline__ df df_at(const df *x, int i) { return i >= 0 ? x[i] : df{0.f, 0.f}; }
+
+__device__ int df_refine(const DevProg &P, const SProg &S, const df *__restrict__ coef, const float *__restrict__ lu32,
+                         const df *__restrict__ b, df *__restrict__ x, float *__restrict__ w, float tol, int max_it,
+                         int lane) {
+  float dprev = 0.f;
+  for (int it = 0; it < max_it; ++it) {
+    for (int k = lane; k < P.n; k += 32) {
+      df r = b[k];
+      const int2 rr = S.res_row[k];
+      const int nu = rr.y & 0xffff, nt = (int)((unsigned)rr.y >> 16);
+      for (int u = 0; u < nu; ++u) {
+        const int op = S.res_op[rr.x + u];
+        const df xj = x[op & 0x7fff];
+        r = df_add(r, (op & 0x8000) ? xj : df_neg(xj));
+      }
+      for (int u = nu; u < nt; ++u) {
+        const int op = S.res_op[rr.x + u];
+        const df a = coef[((unsigned)op >> 16) - 1];
+        r = df_fma((op & 0x8000) ? a : df_neg(a), x[op & 0x7fff], r);
+      }
+      w[k] = df_approx(r);
+    }
+    __syncwarp();
+    s_lsolve<float, float>(S, lu32, w, lane);
+    s_usolve<float, float>(S, lu32, w, lane);
+    float dmax = 0.f, xmax = 0.f;
+    for (int k = lane; k < P.n; k += 32) {
+      const float d = w[k];
+      const df xn = df_add_f(x[k], d);
+      x[k] = xn;
+      dmax = fmaxf(dmax, fabsf(d));
+      xmax = fmaxf(xmax, fabsf(xn.hi));
+    }
+    __syncwarp();
+    dmax = warp_maxf(dmax);
+    xmax = warp_maxf(xmax);
+    if (!(dmax == dmax) || !(xmax == xmax)) return -1;
+    if (dmax <= tol * xmax) return it + 1;
+    if (it > 0 && dmax > 0.5f * dprev) return -1;
+    dprev = dmax;
+  }
+  return -1;
+}
+
+__global__ void __launch_bounds__(256, 1) k_tran_warp_df(DevProg P, KCfg cfg, WarpLay L, const double *values, int n_inst,
+                                                      double h, int n_steps, int method, int lag, double *x_out,
+                                                      int *inst_status, int *queue, unsigned long long *hist,
+                                                      float tol) {
+  extern __shared__ __align__(16) char smem[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  {
+    const int words = P.sp_off[11];
+    const int4 *src = reinterpret_cast<const int4 *>(P.sprog);
+    int4 *dst = reinterpret_cast<int4 *>(smem);
+    for (int i = threadIdx.x; i < words / 4; i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+  }
+  const SProg S = sprog_view(P, reinterpret_cast<const int *>(smem));
+  char *base = smem + L.sprog_bytes + (size_t)wid * L.bytes;
+  float *lu32 = reinterpret_cast<float *>(base + L.lu);
+  df *coef = reinterpret_cast<df *>(base + L.coef);
+  double *coef64 = reinterpret_cast<double *>(base + L.coef);  // same bytes, set-up only
+  df *x = reinterpret_cast<df *>(base + L.x);
+  df *b = reinterpret_cast<df *>(base + L.b);
+  float *w32 = reinterpret_cast<float *>(base + L.w);
+  df *cb = reinterpret_cast<df *>(base + L.cb);
+  df *icap = reinterpret_cast<df *>(base + L.icap);
+  const size_t stride = (size_t)(n_steps + 1) * P.n;
+  const int max_ref = 6;
+  while (true) {
+    int inst = 0;
+    if (lane == 0) inst = atomicAdd(queue, 1);
+    inst = __shfl_sync(kFull, inst, 0);
+    if (inst >= n_inst) break;
+    int st = 0;
+    unsigned long long lh[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const double *vals = values ? values + (size_t)inst * P.ne : nullptr;
+    double *out = x_out + (size_t)inst * stride;
+    // set-up: FP64 coefficients -> FP32 LU -> factor; then the coefficients become df
+    st |= w_coef_pass(P, vals, h, method, nullptr, coef64, lane);
+    w_stamp_lu<float>(P, coef64, lu32, lane);
+    st |= w_factor<float>(P, lu32, lane);
+    for (int e = lane; e < P.ne; e += 32) coef[e] = df_from_double(coef64[e]);
+    for (int k = lane; k < P.n; k += 32) x[k] = df_from_double(out[P.q[k]]);
+    for (int d = lane; d < P.ncap; d += 32) icap[d] = df{0.f, 0.f};
+    __syncwarp();
+    for (int s = 1; s <= n_steps && !(st & (KS_SINGULAR | KS_NONFINITE | KS_NOTIMPL | KS_STALL)); ++s) {
+      const double t = (double)s * h;
+      const double t_src = lag ? (double)(s - 1) * h : t;
+      // companion / source coefficients from the previous solution
+      for (int d = lane; d < P.ndyn; d += 32) {
+        const int4 dd = S.dyn[d];
+        const int e = dd.x & 0xffffff, kind = (int)((unsigned)dd.x >> 24);
+        df v{0.f, 0.f};
+        if (kind == KRETS_ELEM_C) {
+          const df vprev = df_sub(df_at(x, dd.y), df_at(x, dd.z));
+          v = method == KRETS_METHOD_TR ? df_fma(coef[e], vprev, icap[d]) : df_mul(coef[e], vprev);
+        } else if (kind == KRETS_ELEM_L) {
+          const df li = df_neg(df_mul(coef[e], x[dd.w]));
+          v = method == KRETS_METHOD_TR ? df_sub(li, df_sub(df_at(x, dd.y), df_at(x, dd.z))) : li;
+        } else if (kind == KRETS_ELEM_V) {
+          const krets_element &E = P.el[e];
+          v = df_from_double(wave_value(E, vals ? vals[e] : E.value, t_src));
+        } else if (kind == KRETS_ELEM_I) {
+          v = coef[e];
+        }
+        cb[d] = v;
+      }
+      __syncwarp();
+      for (int k = lane; k < P.n; k += 32) {
+        df acc{0.f, 0.f};
+        for (int u = S.bd_ptr[k]; u < S.bd_ptr[k + 1]; ++u) {
+          const int code = S.bd_op[u];
+          acc = (code & 1) ? df_sub(acc, cb[code >> 1]) : df_add(acc, cb[code >> 1]);
+        }
+        b[k] = acc;
+      }
+      __syncwarp();
+      const int r = df_refine(P, S, coef, lu32, b, x, w32, tol, max_ref, lane);
+      if (r > 0) lh[r < 8 ? r : 7]++;
+      else st |= KS_STALL;
+      if (method == KRETS_METHOD_TR) {
+        for (int d = lane; d < P.ncap; d += 32) {
+          const int4 dd = S.dyn[d];
+          const df vn = df_sub(df_at(x, dd.y), df_at(x, dd.z));
+          icap[d] = df_sub(df_mul(coef[dd.x & 0xffffff], vn), cb[d]);
+        }
+      }
+      double *row = out + (size_t)s * P.n;
+      int nonfinite = 0;
+      for (int k = lane; k < P.n; k += 32) {
+        const double v = df_to_double(x[S.qinv[k]]);
+        nonfinite |= !isfinite(v);
+        __stcs(row + k, v);
+      }
+      if (__any_sync(kFull, nonfinite)) st |= KS_NONFINITE;
+      __syncwarp();
+    }
+    if (lane == 0 && inst_status) inst_status[inst] = st;
+    if (hist && lane == 0)
+      for (int k = 0; k < 8; ++k)
+        if (lh[k]) atomicAdd(hist + k, lh[k]);
+    __syncwarp();
+  }
+}
+
+}  // namespace krets
+
+// ===================================================================== double-float direct
+// Linear circuits: the LU is computed once in FP64 and each entry split into hi + lo FP32
+// (reciprocal diagonals included); every step then does one forward and one backward solve
+// in double-float arithmetic on the FP32 pipes.  No refinement loop: the factors carry
+// 48 significand bits.
+//
+// One instance is handled by a group of G threads (G = 32, 64 or 128): a warp, or several
+// warps joined by a named barrier.  More threads per instance shorten the wide levels of
+// the solves and give each SM scheduler several warps to switch between, without more
+// shared memory per instance.
+namespace krets {
+
+template <int G>
+__device__ __forceinline__ void gsync(int gid) {
+  if (G == 32) __syncwarp();
+  else asm volatile("bar.sync %0, %1;" ::"r"(gid + 1), "n"(G) : "memory");
+}
+
+// group-wide "any": every thread of the group gets the same answer
+template <int G>
+__device__ __forceinline__ bool gany(bool v, int gid) {
+  if (G == 32) return __any_sync(kFull, v);
+  int r;
+  asm volatile(
+      "{ .reg .pred p, q;\n\t"
+      "setp.ne.s32 p, %1, 0;\n\t"
+      "barrier.red.or.pred q, %2, %3, p;\n\t"
+      "selp.s32 %0, 1, 0, q; }"
+      : "=r"(r)
+      : "r"((int)v), "r"(gid + 1), "n"(G)
+      : "memory");
+  return r != 0;
+}
+
+template <int G>
+__device__ int g_coef_pass(const DevProg &P, const double *values, double h, int method, double *coef, int gl) {
+  int err = 0;
+  for (int e = gl; e < P.ne; e += G) {
+    const krets_element &E = P.el[e];
+    const double val = values ? values[e] : E.value;
+    double c = 0.0;
+    switch (E.kind) {
+      case KRETS_ELEM_R: c = (E.flags & KRETS_FLAG_G2) ? val : 1.0 / val; break;
+      case KRETS_ELEM_C: c = method == KRETS_METHOD_TR ? 2.0 * val / h : val / h; break;
+      case KRETS_ELEM_L: c = method == KRETS_METHOD_TR ? 2.0 * val / h : val / h; break;
+      case KRETS_ELEM_V:
+      case KRETS_ELEM_I: c = val; break;
+      case KRETS_ELEM_M: break;
+      default: err |= KS_NOTIMPL;  // diodes never reach the linear engine
+    }
+    coef[e] = c;
+  }
+  return err;
+}
+
+template <int G>
+__device__ int g_factor64(const DevProg &P, double *lu, int gl, int gid) {
+  int bad = 0;
+  for (int l = 0; l < P.nlev; ++l) {
+    const int r0 = P.lev_ptr[l], r1 = P.lev_ptr[l + 1];
+    for (int t = r0 + gl; t < r1; t += G) {
+      const int k = P.ldesc[t].x;
+      for (int pi = P.piv_ptr[k]; pi < P.piv_ptr[k + 1]; ++pi) {
+        const int4 pv = P.piv[pi];
+        const double l_kj = lu[pv.x] / lu[P.lu_diag[pv.y]];
+        lu[pv.x] = l_kj;
+        for (int u = pv.z; u < pv.w; ++u) {
+          const int2 d = P.upd[u];
+          lu[d.x] -= l_kj * lu[d.y];
+        }
+      }
+      const double dk = lu[P.lu_diag[k]];
+      if (!(fabs(dk) > 0)) bad |= KS_SINGULAR;
+      else if (!isfinite(dk)) bad |= KS_NONFINITE;
+    }
+    gsync<G>(gid);
+  }
+  for (int k = gl; k < P.n; k += G) {
+    const int sl = P.lu_diag[k];
+    lu[sl] = 1.0 / lu[sl];
+  }
+  gsync<G>(gid);
+  return bad;
+}
+
+template <bool UPPER>
+__device__ __forceinline__ df df_row(const SProg &S, const df *__restrict__ lu, const df *y, const int4 d, int &k) {
+  k = d.x & 0xffff;
+  const int rest = (int)((unsigned)d.x >> 16);
+  const int first = UPPER ? d.y + 1 : d.y;
+  const int c0 = d.z & 0xffff, c1 = (int)((unsigned)d.z >> 16);
+  const df zero{0.f, 0.f};
+  const df a0 = d.w > 0 ? lu[first] : zero;
+  const df a1 = d.w > 1 ? lu[first + 1] : zero;
+  df s = y[k];
+  s = df_fma(df_neg(a0), y[c0], s);
+  s = df_fma(df_neg(a1), y[c1], s);
+  for (int j = 2; j < 2 + rest; ++j) s = df_fma(df_neg(lu[first + j]), y[S.lu_col[first + j]], s);
+  if (UPPER) s = df_mul(s, lu[d.y]);
+  return s;
+}
+
+// Level-scheduled double-float solve by a group of G threads.  Levels with at most 64 rows
+// (the top of the elimination tree: its last levels for L, its first for U) run on the
+// group's first warp alone with warp barriers; `nar` is the first narrow level of L (rows
+// of every later level <= 64) or the number of leading narrow levels of U.
+template <int G, bool UPPER>
+__device__ __forceinline__ void df_level(const SProg &S, const df *__restrict__ lu, df *y, const int *ptr,
+                                         const int4 *desc, int l, int tid, int stride) {
+  const int r0 = ptr[l], r1 = ptr[l + 1];
+  for (int t = r0 + tid; t < r1; t += 2 * stride) {
+    int k0, k1 = -1;
+    const df v0 = df_row<UPPER>(S, lu, y, desc[t], k0);
+    df v1{0.f, 0.f};
+    if (t + stride < r1) v1 = df_row<UPPER>(S, lu, y, desc[t + stride], k1);
+    y[k0] = v0;
+    if (k1 >= 0) y[k1] = v1;
+  }
+}
+
+template <int G, bool UPPER>
+__device__ __forceinline__ void df_solve(const SProg &S, const df *__restrict__ lu, df *y, int gl, int gid, int nar) {
+  const int nl = UPPER ? S.nulev : S.nlev;
+  const int *ptr = UPPER ? S.ulev_ptr : S.lev_ptr;
+  const int4 *desc = UPPER ? S.udesc : S.ldesc;
+  const bool w0 = gl < 32;
+  if (nar < 0) {  // no narrow-level split: every level on the whole group
+    for (int l = UPPER ? 0 : 1; l < nl; ++l) {
+      df_level<G, UPPER>(S, lu, y, ptr, desc, l, gl, G);
+      gsync<G>(gid);
+    }
+    return;
+  }
+  if (!UPPER) {
+    for (int l = 1; l < nar; ++l) {
+      df_level<G, UPPER>(S, lu, y, ptr, desc, l, gl, G);
+      gsync<G>(gid);
+    }
+    if (w0) {
+      for (int l = nar > 1 ? nar : 1; l < nl; ++l) {
+        df_level<G, UPPER>(S, lu, y, ptr, desc, l, gl, 32);
+        __syncwarp();
+      }
+    }
+    gsync<G>(gid);
+  } else {
+    if (w0) {
+      for (int l = 0; l < nar; ++l) {
+        df_level<G, UPPER>(S, lu, y, ptr, desc, l, gl, 32);
+        __syncwarp();
+      }
+    }
+    gsync<G>(gid);
+    for (int l = nar; l < nl; ++l) {
+      df_level<G, UPPER>(S, lu, y, ptr, desc, l, gl, G);
+      gsync<G>(gid);
+    }
+  }
+}
+
+// Shared-memory layout of one instance of the double-float direct engine.
+struct DfdLay {
+  int lu;     // df[nnz_lu]
+  int x;      // df[n]  (solution; the rhs is assembled and solved in place)
+  int cdyn;   // df[ndyn] coefficients of the rhs elements (C/h or 2C/h, L/h or 2L/h, source values)
+  int cb;     // df[ndyn] rhs coefficients of the step
+  int icap;   // df[ncap] trapezoidal capacitor currents
+  int slot;   // int[4]   group's work item and status words
+  int coef64; // double[ne] set-up scratch (aliases x / cdyn / cb / icap and padding)
+  int bytes;  // per instance
+  int sprog_bytes;
+};
+
+// opts bit 0: run narrow levels on one warp; bit 1: integer-only FP64 output conversion
+template <int G>
+__global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay L, const double *values, int n_inst,
+                                                     double h, int n_steps, int method, int lag, double *x_out,
+                                                     int *inst_status, int *queue, int opts) {
+  extern __shared__ __align__(16) char smem[];
+  const int gl = threadIdx.x % G, gid = threadIdx.x / G;
+  {
+    const int words = P.sp_off[11];
+    const int4 *src = reinterpret_cast<const int4 *>(P.sprog);
+    int4 *dst = reinterpret_cast<int4 *>(smem);
+    for (int i = threadIdx.x; i < words / 4; i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+  }
+  const SProg S = sprog_view(P, reinterpret_cast<const int *>(smem));
+  int lnar = S.nlev, unar = 0;  // narrow-level split points (see df_solve)
+  while (lnar > 1 && S.lev_ptr[lnar] - S.lev_ptr[lnar - 1] <= 64) --lnar;
+  while (unar < S.nulev && S.ulev_ptr[unar + 1] - S.ulev_ptr[unar] <= 64) ++unar;
+  if (!(opts & 1)) lnar = unar = -1;
+  const bool int_cvt = (opts & 2) != 0;
+  char *base = smem + L.sprog_bytes + (size_t)gid * L.bytes;
+  df *lu = reinterpret_cast<df *>(base + L.lu);
+  double *lu64 = reinterpret_cast<double *>(base + L.lu);  // same bytes, set-up only
+  df *x = reinterpret_cast<df *>(base + L.x);
+  df *cdyn = reinterpret_cast<df *>(base + L.cdyn);
+  df *cb = reinterpret_cast<df *>(base + L.cb);
+  df *icap = reinterpret_cast<df *>(base + L.icap);
+  int *slot = reinterpret_cast<int *>(base + L.slot);
+  double *coef64 = reinterpret_cast<double *>(base + L.coef64);  // set-up only
+  const size_t stride = (size_t)(n_steps + 1) * P.n;
+  while (true) {
+    if (gl == 0) slot[0] = atomicAdd(queue, 1);
+    gsync<G>(gid);
+    const int inst = slot[0];
+    gsync<G>(gid);
+    if (inst >= n_inst) break;
+    const double *vals = values ? values + (size_t)inst * P.ne : nullptr;
+    double *out = x_out + (size_t)inst * stride;
+    // set-up: FP64 coefficients, LU stamped and factored in FP64, then split to df
+    int st = g_coef_pass<G>(P, vals, h, method, coef64, gl);
+    gsync<G>(gid);
+    for (int sl = gl; sl < P.nnz_lu; sl += G) {
+      const int t = P.lu_src[sl];
+      lu64[sl] = t < 0 ? 0.0 : sum_entry<double>(P, t, coef64, nullptr);
+    }
+    gsync<G>(gid);
+    st |= g_factor64<G>(P, lu64, gl, gid);
+    for (int sl = gl; sl < P.nnz_lu; sl += G) lu[sl] = df_from_double(lu64[sl]);
+    // coef64 is dead from here on (its bytes alias x / cdyn / cb / icap): the rhs-element
+    // coefficients are recomputed with the same expressions as g_coef_pass
+    for (int d = gl; d < P.ndyn; d += G) {
+      const int e = S.dyn[d].x & 0xffffff;
+      const krets_element &E = P.el[e];
+      const double val = vals ? vals[e] : E.value;
+      double c = val;
+      if (E.kind == KRETS_ELEM_C || E.kind == KRETS_ELEM_L) c = method == KRETS_METHOD_TR ? 2.0 * val / h : val / h;
+      cdyn[d] = df_from_double(c);
+    }
+    for (int k = gl; k < P.n; k += G) x[k] = df_from_double(out[P.q[k]]);
+    for (int d = gl; d < P.ncap; d += G) icap[d] = df{0.f, 0.f};
+    const bool fatal = gany<G>((st & (KS_SINGULAR | KS_NONFINITE | KS_NOTIMPL)) != 0, gid);
+    for (int s = 1; s <= n_steps && !fatal; ++s) {
+      const double t = (double)s * h;
+      const double t_src = lag ? (double)(s - 1) * h : t;
+      for (int d = gl; d < P.ndyn; d += G) {
+        const int4 dd = S.dyn[d];
+        const int kind = (int)((unsigned)dd.x >> 24);
+        df v{0.f, 0.f};
+        if (kind == KRETS_ELEM_C) {
+          const df vprev = df_sub(df_at(x, dd.y), df_at(x, dd.z));
+          v = method == KRETS_METHOD_TR ? df_fma(cdyn[d], vprev, icap[d]) : df_mul(cdyn[d], vprev);
+        } else if (kind == KRETS_ELEM_L) {
+          const df li = df_neg(df_mul(cdyn[d], x[dd.w]));
+          v = method == KRETS_METHOD_TR ? df_sub(li, df_sub(df_at(x, dd.y), df_at(x, dd.z))) : li;
+        } else if (kind == KRETS_ELEM_V) {
+          const int e = dd.x & 0xffffff;
+          const krets_element &E = P.el[e];
+          v = df_from_double(wave_value(E, vals ? vals[e] : E.value, t_src));
+        } else if (kind == KRETS_ELEM_I) {
+          v = cdyn[d];
+        }
+        cb[d] = v;
+      }
+      gsync<G>(gid);  // x (previous solution) fully read: the rhs overwrites it
+      for (int k = gl; k < P.n; k += G) {
+        df acc{0.f, 0.f};
+        for (int u = S.bd_ptr[k]; u < S.bd_ptr[k + 1]; ++u) {
+          const int code = S.bd_op[u];
+          acc = df_add(acc, (code & 1) ? df_neg(cb[code >> 1]) : cb[code >> 1]);
+        }
+        x[k] = acc;
+      }
+      gsync<G>(gid);
+      df_solve<G, false>(S, lu, x, gl, gid, lnar);
+      df_solve<G, true>(S, lu, x, gl, gid, unar);
+      if (method == KRETS_METHOD_TR) {
+        for (int d = gl; d < P.ncap; d += G) {
+          const int4 dd = S.dyn[d];
+          const df vn = df_sub(df_at(x, dd.y), df_at(x, dd.z));
+          icap[d] = df_sub(df_mul(cdyn[d], vn), cb[d]);
+        }
+      }
+      double *row = out + (size_t)s * P.n;
+      for (int k = gl; k < P.n; k += G) {
+        const df xv = x[S.qinv[k]];
+        const double v = int_cvt ? df_to_double_int(xv) : df_to_double(xv);
+        if (!isfinite(v)) st |= KS_NONFINITE;
+        __stcs(row + k, v);
+      }
+      gsync<G>(gid);
+    }
+    if (gl == 0) slot[1] = 0;
+    gsync<G>(gid);
+    if (st) atomicOr(&slot[1], st);
+    gsync<G>(gid);
+    if (gl == 0 && inst_status) inst_status[inst] = slot[1];
   }
 }
 

@@ -98,7 +98,7 @@ def test_plain_transient_refactor_matches_reuse(oracle_lib):
     assert rel_err(a, ref, is_current_mask(c)) < TOL
 
 
-@pytest.mark.parametrize("precision", [_lib.PREC_FP64, _lib.PREC_MIXED])
+@pytest.mark.parametrize("precision", [_lib.PREC_FP64, _lib.PREC_MIXED, _lib.PREC_DF])
 def test_batched_mc_transient_matches_oracle(oracle_lib, precision):
     c = rlc_ladder(200)
     t = element_table(c)
