@@ -160,6 +160,17 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
 krets_status krets_batch_ac(krets_circuit *c, int32_t n_inst, const double *values, const double *freqs,
                             int32_t n_freq, int32_t precision, double *x_out, int32_t *item_status);
 
+/* Adjoint sensitivities of a batched linear transient (no counterpart in the reference).
+ * Loss per instance: sum over steps n = 1..n_steps of x_out(t_n)^2, out_unknown being the
+ * MNA index of the output (e.g. V(out)).  grad_out[n_inst][n_elem] receives dLoss/dvalue for
+ * every R, C and L element (0 for the others).  The forward pass keeps a checkpoint every
+ * checkpoint_every steps and the backward sweep recomputes each segment from it; transposed
+ * solves reuse the forward LU factors.  gradient = 0 runs the forward pass only (loss).
+ * The operating point at t = 0 must be zero (KRETS_ERR_NOT_IMPLEMENTED otherwise). */
+krets_status krets_adjoint_tran(krets_circuit *c, int32_t n_inst, const double *values, double h, int32_t n_steps,
+                                int32_t method, int32_t out_unknown, int32_t checkpoint_every, int32_t gradient,
+                                double *loss_out, double *grad_out);
+
 /* Batched operating points: x_out[n_inst][n]. */
 krets_status krets_batch_op(krets_circuit *c, int32_t n_inst, const double *values, double *x_out,
                             int32_t *inst_status);
@@ -241,6 +252,8 @@ krets_status krets_batch_tran_noalloc(krets_circuit *c, int32_t n_inst, const do
 #define KRETS_PROG_ULEV_ROWS 18
 #define KRETS_PROG_EL_POS 19
 #define KRETS_PROG_META 20 /* {ordering, n, nnz_a, nnz_lu, n_levels, n_ulevels, factor_flops} */
+#define KRETS_PROG_TPROG 21 /* transposed-solve program (transient mode) */
+#define KRETS_PROG_TPOFF 22 /* its section offsets (6) and level counts of U^T and L^T */
 #define KRETS_MODE_DC 0
 #define KRETS_MODE_AC 1
 #define KRETS_MODE_TRAN 2

@@ -27,7 +27,7 @@ MODE_DC, MODE_AC, MODE_TRAN = 0, 1, 2
 
 PROG_ARRAYS = ["q", "prow", "lu_rowptr", "lu_col", "lu_diag", "a_rowptr", "a_col", "a_slot", "a_cptr",
                "a_contrib", "b_cptr", "b_contrib", "piv_ptr", "piv", "upd", "lev_ptr", "lev_rows",
-               "ulev_ptr", "ulev_rows", "el_pos", "meta"]
+               "ulev_ptr", "ulev_rows", "el_pos", "meta", "tprog", "tpoff"]
 
 _EXC = {
     ELEMENT_NOT_FOUND: E.ElementNotFound, MAX_ITERATIONS: E.MaximumIterationsExceeded,
@@ -69,6 +69,7 @@ def lib():
             "krets_batch_tran": [_P, _I, _P, _D, _I, _I, _I, _I, _P, _P],
             "krets_batch_ac": [_P, _I, _P, _P, _I, _I, _P, _P],
             "krets_batch_tran_noalloc": [_P, _I, _P, _D, _I, _I, _I, _I, _P, _P],
+            "krets_adjoint_tran": [_P, _I, _P, _D, _I, _I, _I, _I, _I, _P, _P],
             "krets_batch_op": [_P, _I, _P, _P, _P],
             "krets_last_timing": [_P, _P, _P],
             "krets_last_refine_stats": [_P, _P, _P],
@@ -238,6 +239,23 @@ class GpuCircuit:
             lag = m == 0
         check(lib().krets_batch_tran_noalloc(self.h, n_inst, ptr(d_values), h, n_steps, m, int(bool(lag)),
                                              precision, ptr(d_out), ptr(d_status)), "batch_tran_noalloc")
+
+    def adjoint_tran(self, values, h, n_steps, out_unknown, method="tr", checkpoint_every=100, gradient=True,
+                     n_inst=None):
+        """Loss sum_n x_out(t_n)^2 per instance and its gradient w.r.t. every element value."""
+        if values is None:
+            ni = 1 if n_inst is None else n_inst
+        elif isinstance(values, DeviceArray):
+            ni = values.shape[0]
+        else:
+            values = np.ascontiguousarray(values, dtype=np.float64)
+            ni = values.shape[0]
+        loss = np.zeros(ni)
+        grad = np.zeros((ni, self.ne)) if gradient else None
+        check(lib().krets_adjoint_tran(self.h, ni, ptr(values), h, n_steps, METHOD[method], out_unknown,
+                                       checkpoint_every, int(bool(gradient)), ptr(loss), ptr(grad)),
+              "adjoint_tran")
+        return (loss, grad) if gradient else loss
 
     def batch_ac(self, values, freqs, precision=PREC_MIXED, out=None):
         f = np.ascontiguousarray(freqs, dtype=np.float64)

@@ -15,6 +15,7 @@
 
 #include "kernels.cuh"
 #include "warp_kernels.cuh"
+#include "adjoint.cuh"
 #include "krets_gpu.h"
 #include "symbolic.h"
 
@@ -164,6 +165,7 @@ krets_status upload_program(krets_circuit *c, Program &&P, DevProgram &D) {
   size_t i_ep = vi(H.el_pos), i_ic = vi(is_cur);
   size_t i_qi = vi(H.qinv), i_ld = vi(H.ldesc), i_ud = vi(H.udesc), i_rp2 = vi(H.res_ptr), i_ro = vi(H.res_op);
   size_t i_dy = vi(H.dyn_e), i_bdp = vi(H.bd_ptr), i_bdo = vi(H.bd_op), i_sp = vi(H.sprog);
+  size_t i_tp = vi(H.tprog), i_pr = vi(H.prow);
   CU(cudaMalloc(&D.buf, total));
   std::vector<char> staging(total, 0);
   for (auto &p : parts)
@@ -213,8 +215,13 @@ krets_status upload_program(krets_circuit *c, Program &&P, DevProgram &D) {
   V.ncap = H.ncap;
   V.n_resop = (int)H.res_op.size() / 2;
   V.sprog = (const int *)ptr(i_sp);
-  for (int k = 0; k < 12; ++k) V.sp_off[k] = H.sp_off[k];
+  for (int k = 0; k < 14; ++k) V.sp_off[k] = H.sp_off[k];
   V.sprog_ok = H.sprog_ok;
+  V.tprog = (const int *)ptr(i_tp);
+  for (int k = 0; k < 8; ++k) V.tp_off[k] = H.tp_off[k];
+  V.n_utlev = H.n_utlev;
+  V.n_ltlev = H.n_ltlev;
+  V.prow = (const int *)ptr(i_pr);
   bool nl = false;
   for (int e = 0; e < H.ne; ++e) {
     int k = c->el[e].kind;
@@ -791,9 +798,12 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
     if (!P.sprog_ok || per_warp + WL.sprog_bytes > max_smem_optin()) warp_engine = false;
   }
   double *fb = nullptr;
-  if (warp_engine && dfd && !P.nonlinear) {
-    // double-float direct: one instance per group of G threads (default 128)
-    DfdLay DL{};
+  // double-float direct: one instance per group of G threads (default 128); it stages only
+  // the step-program words before the residual operators, so it fits where the warp
+  // engine may not
+  DfdLay DL{};
+  bool use_dfd = dfd && !P.nonlinear && P.sprog_ok && !(eng && strcmp(eng, "block") == 0);
+  if (use_dfd) {
     size_t cur = 0;
     auto put = [&](int &off, size_t bytes) { off = (int)cur; cur = align16(cur + bytes); };
     put(DL.lu, 8 * (size_t)P.nnz_lu);
@@ -805,12 +815,13 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
     if (cur - DL.x < 8 * (size_t)P.ne) cur = DL.x + align16(8 * (size_t)P.ne);
     put(DL.slot, 16);
     DL.bytes = (int)align16(cur);
-    DL.sprog_bytes = WL.sprog_bytes;
+    DL.sprog_bytes = (int)align16((size_t)P.sp_off[5] * sizeof(int));
+    if ((size_t)DL.bytes + DL.sprog_bytes > max_smem_optin()) use_dfd = false;
+  }
+  if (use_dfd) {
     const char *genv = getenv("KRETS_GROUP");
     int G = genv ? atoi(genv) : 128;
     if (G != 32 && G != 64 && G != 128) G = 128;
-    if ((size_t)DL.bytes + DL.sprog_bytes > max_smem_optin())
-      return fail(KRETS_ERR_INVALID_ARGUMENT, "circuit too large for the double-float engine");
     int W = (int)std::max<size_t>(1, std::min<size_t>(640 / G, (max_smem_optin() - DL.sprog_bytes) / DL.bytes));
     const size_t smem = DL.sprog_bytes + (size_t)W * DL.bytes;
     const char *oenv = getenv("KRETS_DFD_OPTS");
@@ -904,6 +915,145 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
     any_op |= st[n_inst + i];
   }
   if (any_op) return map_status(any_op, 0);
+  return map_status(any, 1);
+}
+
+krets_status krets_adjoint_tran(krets_circuit *c, int32_t n_inst, const double *values, double h, int32_t n_steps,
+                                int32_t method, int32_t out_unknown, int32_t checkpoint_every, int32_t gradient,
+                                double *loss_out, double *grad_out) {
+  if (!c || n_inst <= 0 || n_steps <= 0 || !(h > 0) || !loss_out || (gradient && !grad_out) || checkpoint_every <= 0 ||
+      out_unknown < 0 || out_unknown >= c->n)
+    return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments to krets_adjoint_tran");
+  DevProgram *Ddc, *Dtr;
+  krets_status s = get_program(c, MODE_DC, 0, 0, 0, &Ddc);
+  if (s != KRETS_OK) return s;
+  s = get_program(c, MODE_TRAN, method, h, 0, &Dtr);
+  if (s != KRETS_OK) return s;
+  const DevProg &P = Dtr->view;
+  const Program &H = Dtr->host;
+  if (P.nonlinear) return fail(KRETS_ERR_NOT_IMPLEMENTED, "adjoint sensitivities need a linear circuit");
+  if (!P.sprog_ok) return fail(KRETS_ERR_INVALID_ARGUMENT, "circuit too large for the adjoint engine");
+  CU(cudaEventRecord(c->ev[0], c->stream));
+  DevBuf tv, top, tbufs, tck, tseg, tloss, tgrad, tst;
+  void *dv;
+  s = dev_view(values, sizeof(double) * c->ne * (size_t)n_inst, true, c->stream, tv, &dv);
+  if (s) return s;
+  // the recurrence starts from x_0 = 0: check that the operating point is zero
+  CU(cudaMalloc(&top.p, sizeof(double) * c->n * (size_t)n_inst + sizeof(int) * (size_t)n_inst));
+  int *op_st = (int *)((double *)top.p + (size_t)c->n * n_inst);
+  s = run_op(c, Ddc, n_inst, (const double *)dv, (double *)top.p, c->n, op_st, nullptr, 128);
+  if (s) return s;
+  std::vector<double> opx((size_t)c->n * n_inst);
+  CU(cudaMemcpyAsync(opx.data(), top.p, sizeof(double) * opx.size(), cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  for (double v : opx)
+    if (v != 0.0)
+      return fail(KRETS_ERR_NOT_IMPLEMENTED, "adjoint sensitivities need a zero operating point at t = 0 "
+                                             "(sources at 0 when the transient starts)");
+  // per-element adjoint descriptors and the column map of C^T lambda
+  std::vector<int> adj(4 * (size_t)P.ne, -1), ccp(P.n + 1, 0), cco;
+  std::vector<std::vector<int>> cols(P.n);
+  for (int e = 0; e < P.ne; ++e) {
+    const krets_element &E = c->el[e];
+    if ((E.kind == KRETS_ELEM_R || E.kind == KRETS_ELEM_C) && (E.flags & KRETS_FLAG_G2))
+      return fail(KRETS_ERR_NOT_IMPLEMENTED, "adjoint sensitivities of group-2 resistor/capacitor stamps");
+    adj[4 * e] = E.kind;
+    adj[4 * e + 1] = E.p >= 0 ? H.pinv[E.p] : -1;
+    adj[4 * e + 2] = E.m >= 0 ? H.pinv[E.m] : -1;
+    adj[4 * e + 3] = E.b >= 0 ? H.pinv[E.b] : -1;
+  }
+  for (size_t d = 0; d < H.dyn_e.size(); ++d) {
+    const krets_element &E = c->el[H.dyn_e[d]];
+    if (E.kind == KRETS_ELEM_C) {
+      if (E.p >= 0) cols[H.qinv[E.p]].push_back((int)d << 1);
+      if (E.m >= 0) cols[H.qinv[E.m]].push_back(((int)d << 1) | 1);
+    } else if (E.kind == KRETS_ELEM_L && E.b >= 0) {
+      cols[H.qinv[E.b]].push_back((int)d << 1);
+    }
+  }
+  for (int k = 0; k < P.n; ++k) {
+    cco.insert(cco.end(), cols[k].begin(), cols[k].end());
+    ccp[k + 1] = (int)cco.size();
+  }
+  size_t nb = sizeof(int) * (adj.size() + ccp.size() + cco.size() + 8);
+  CU(cudaMalloc(&tbufs.p, nb));
+  int *d_adj = (int *)tbufs.p, *d_ccp = d_adj + adj.size(), *d_cco = d_ccp + ccp.size();
+  CU(cudaMemcpyAsync(d_adj, adj.data(), sizeof(int) * adj.size(), cudaMemcpyHostToDevice, c->stream));
+  CU(cudaMemcpyAsync(d_ccp, ccp.data(), sizeof(int) * ccp.size(), cudaMemcpyHostToDevice, c->stream));
+  if (!cco.empty()) CU(cudaMemcpyAsync(d_cco, cco.data(), sizeof(int) * cco.size(), cudaMemcpyHostToDevice, c->stream));
+  // shared-memory layout: step program, transposed program, then one slice per instance
+  // shared memory: step program, transposed program, then the instance's arrays
+  AdjLay AL{};
+  size_t cur = 0;
+  auto put = [&](int &off, size_t bytes) { off = (int)cur; cur = align16(cur + bytes); };
+  put(AL.slot, 16);
+  put(AL.lu, 8 * (size_t)P.nnz_lu);
+  put(AL.x, 8 * (size_t)P.n);
+  put(AL.cdyn, 8 * (size_t)P.ndyn);
+  put(AL.cb, 8 * (size_t)P.ndyn);
+  put(AL.icap, 8 * (size_t)P.ncap);
+  put(AL.lam, 8 * (size_t)P.n);
+  put(AL.cba, 8 * (size_t)P.ndyn);
+  AL.coef64 = AL.x;  // set-up scratch over x .. cba (dead once the LU is formed)
+  if (cur - AL.x < 8 * (size_t)P.ne) cur = AL.x + align16(8 * (size_t)P.ne);
+  AL.bytes = (int)align16(cur);
+  AL.sprog_bytes = (int)align16((size_t)P.sp_off[5] * sizeof(int));
+  AL.tprog_bytes = (int)align16((size_t)P.tp_off[5] * sizeof(int));
+  const size_t smem = (size_t)AL.sprog_bytes + AL.tprog_bytes + AL.bytes;
+  if (smem > max_smem_optin())
+    return fail(KRETS_ERR_INVALID_ARGUMENT, "circuit too large for the adjoint engine's shared memory");
+  // per-thread register caches: n <= 4 x 256, ndyn <= 4 x 256, ne <= 8 x 256
+  constexpr int RK = 4, RD = 4, RE = 8;
+  if (P.n > RK * kAdjHalf || P.ndyn > RD * kAdjHalf || P.ne > RE * kAdjHalf)
+    return fail(KRETS_ERR_INVALID_ARGUMENT,
+                "circuit too large for the adjoint engine (n > 1024, more than 1024 C/L/V/I or ne > 2048)");
+  auto ka = k_adjoint_dfd<RK, RD, RE>;
+  CU(cudaFuncSetAttribute(ka, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ka, kAdjThreads, smem));
+  if (per_sm < 1) return fail(KRETS_ERR_CUDA, "adjoint engine does not fit on an SM");
+  const int grid = std::max(1, std::min(n_inst, per_sm * device_sm_count()));
+  const int K = std::min(checkpoint_every, n_steps);
+  const int J = (n_steps + K - 1) / K;
+  CU(cudaMalloc(&tck.p, sizeof(df) * (size_t)grid * J * ((size_t)P.n + P.ncap)));
+  // three segment buffers of K+1 states and two lambda histories of K vectors per CTA
+  const size_t seg_bytes = sizeof(df) * (size_t)grid * 3 * ((size_t)K + 1) * P.n;
+  const size_t hist_bytes = sizeof(df) * (size_t)grid * 2 * (size_t)K * P.n;
+  CU(cudaMalloc(&tseg.p, gradient ? seg_bytes + hist_bytes : 16));
+  df *d_hist = gradient ? (df *)((char *)tseg.p + seg_bytes) : nullptr;
+  DevBuf dl_loss, dl_grad;
+  void *d_loss, *d_grad = nullptr;
+  s = dev_view(loss_out, sizeof(double) * n_inst, false, c->stream, dl_loss, &d_loss);
+  if (s) return s;
+  if (gradient) {
+    s = dev_view(grad_out, sizeof(double) * (size_t)n_inst * c->ne, false, c->stream, dl_grad, &d_grad);
+    if (s) return s;
+  }
+  CU(cudaMalloc(&tst.p, sizeof(int) * n_inst));
+  CU(cudaMemsetAsync(tst.p, 0, sizeof(int) * n_inst, c->stream));
+  int *queue = c->d_small + 8;
+  CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
+  CU(cudaEventRecord(c->ev[2], c->stream));
+  ka<<<grid, kAdjThreads, smem, c->stream>>>(P, AL, (const double *)dv, n_inst, h, n_steps, method, K,
+                                             H.qinv[out_unknown], (const int4 *)d_adj, d_ccp, d_cco, (df *)tck.p,
+                                             (df *)tseg.p, d_hist, (double *)d_loss, (double *)d_grad, (int *)tst.p,
+                                             queue, gradient ? 1 : 0);
+  g_launches++;
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(c->ev[3], c->stream));
+  if (dl_loss.p) CU(cudaMemcpyAsync(loss_out, d_loss, sizeof(double) * n_inst, cudaMemcpyDeviceToHost, c->stream));
+  if (dl_grad.p)
+    CU(cudaMemcpyAsync(grad_out, d_grad, sizeof(double) * (size_t)n_inst * c->ne, cudaMemcpyDeviceToHost, c->stream));
+  std::vector<int> st(n_inst);
+  CU(cudaMemcpyAsync(st.data(), tst.p, sizeof(int) * n_inst, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaEventRecord(c->ev[1], c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  cudaEventElapsedTime(&c->kernel_ms, c->ev[2], c->ev[3]);
+  cudaEventElapsedTime(&c->call_ms, c->ev[0], c->ev[1]);
+  c->warps_per_cta = kAdjThreads / 32;
+  c->grid = grid;
+  int any = 0;
+  for (int v : st) any |= v;
   return map_status(any, 1);
 }
 

@@ -102,8 +102,13 @@ struct DevProg {
   int ndyn, ncap, n_resop;
   // compact step program (global copy; the warp engine stages it in shared memory)
   const int *sprog;
-  int sp_off[12];
+  int sp_off[14];
   int sprog_ok;
+  // transposed-solve program (adjoint)
+  const int *tprog;
+  int tp_off[8];
+  int n_utlev, n_ltlev;
+  const int *prow;  // [n] position -> pivot row (unknown index of the row)
 };
 
 // status bits written by the engine

@@ -376,11 +376,14 @@ std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<in
 //       diagonal at base) with columns col0, col1; the remaining `rest` entries follow
 //       contiguously and take their columns from lu_col
 //   [4] lu_col[nnz_lu] as uint16 pairs
+//   [7] dyn[ndyn] int4 {e | kind << 24, p, m, b} (positions, -1 absent)
+//   [8] bd_ptr[n+1]   [9] bd_op (dyn << 1 | neg)   [10] qinv[n]
+//   [12] lmax[nlev], [13] umax[nulev]: longest row of each L / U level (off-diagonal entries)
 //   [5] res_row[n] int2 {first op, n_unit | n_total << 16}
 //   [6] res_op: col | neg << 15 | slot << 16 (slot 0 = incidence +-1 entries, listed first;
 //       slot e+1 = coefficient of element e)
-//   [7] dyn[ndyn] int4 {e | kind << 24, p, m, b} (positions, -1 absent)
-//   [8] bd_ptr[n+1]   [9] bd_op (dyn << 1 | neg)   [10] qinv[n]   [11] end
+//   [11] end
+// (in this physical order: sp_off[5] ends the part that the direct engines stage)
 static void pack_step_program(const krets_element *el, Program &P) {
   const int n = P.n;
   P.sprog.clear();
@@ -415,6 +418,39 @@ static void pack_step_program(const krets_element *el, Program &P) {
     int lo = P.lu_col[u], hi = u + 1 < P.lu_col.size() ? P.lu_col[u + 1] : 0;
     S.push_back(lo | (hi << 16));
   }
+  mark(7);
+  for (int e : P.dyn_e) {
+    S.push_back(e | (el[e].kind << 24));
+    S.push_back(P.el_pos[4 * e + 0]);
+    S.push_back(P.el_pos[4 * e + 1]);
+    S.push_back(P.el_pos[4 * e + 2]);
+  }
+  mark(8);
+  S.insert(S.end(), P.bd_ptr.begin(), P.bd_ptr.end());
+  mark(9);
+  S.insert(S.end(), P.bd_op.begin(), P.bd_op.end());
+  mark(10);
+  S.insert(S.end(), P.qinv.begin(), P.qinv.end());
+  // longest row (entries besides the diagonal) of each L level and each U level
+  mark(12);
+  for (size_t l = 0; l + 1 < P.lev_ptr.size(); ++l) {
+    int mx = 0;
+    for (int t = P.lev_ptr[l]; t < P.lev_ptr[l + 1]; ++t) {
+      const int k = P.lev_rows[t];
+      mx = std::max(mx, P.lu_diag[k] - P.lu_rowptr[k]);
+    }
+    S.push_back(mx);
+  }
+  mark(13);
+  for (size_t l = 0; l + 1 < P.ulev_ptr.size(); ++l) {
+    int mx = 0;
+    for (int t = P.ulev_ptr[l]; t < P.ulev_ptr[l + 1]; ++t) {
+      const int k = P.ulev_rows[t];
+      mx = std::max(mx, P.lu_rowptr[k + 1] - P.lu_diag[k] - 1);
+    }
+    S.push_back(mx);
+  }
+  // the residual operators come last: the direct engines stage only the words before them
   mark(5);
   std::vector<int> ops;
   std::vector<int> rows;
@@ -433,20 +469,77 @@ static void pack_step_program(const krets_element *el, Program &P) {
   S.insert(S.end(), rows.begin(), rows.end());
   mark(6);
   S.insert(S.end(), ops.begin(), ops.end());
-  mark(7);
-  for (int e : P.dyn_e) {
-    S.push_back(e | (el[e].kind << 24));
-    S.push_back(P.el_pos[4 * e + 0]);
-    S.push_back(P.el_pos[4 * e + 1]);
-    S.push_back(P.el_pos[4 * e + 2]);
-  }
-  mark(8);
-  S.insert(S.end(), P.bd_ptr.begin(), P.bd_ptr.end());
-  mark(9);
-  S.insert(S.end(), P.bd_op.begin(), P.bd_op.end());
-  mark(10);
-  S.insert(S.end(), P.qinv.begin(), P.qinv.end());
   mark(11);
+}
+
+// ------------------------------------------------------------------ transposed program
+// Rows of U^T are the columns of U (diagonal included), rows of L^T the columns of L; the
+// values are read from the same LU slots.  Levels: U^T row j waits for the rows k < j with
+// U(k,j) != 0; L^T row k waits for the rows j > k with L(j,k) != 0.  Sections, in order:
+//   [0] ut_ptr[nut+1]  [1] ut_desc[n] int4 {row | cnt << 16, first entry, diagonal slot, 0}
+//   [2] lt_ptr[nlt+1]  [3] lt_desc[n] int4 {row | cnt << 16, first entry, -1, 0}
+//   [6] utmax[nut], [7] ltmax[nlt]: longest row of each level
+//   [4] entries int2 {LU slot, position}   [5] end
+static void pack_transposed_program(Program &P) {
+  const int n = P.n;
+  std::vector<std::vector<std::pair<int, int>>> ut(n), lt(n);  // (slot, col)
+  for (int k = 0; k < n; ++k) {
+    for (int s = P.lu_rowptr[k]; s < P.lu_diag[k]; ++s) lt[P.lu_col[s]].push_back({s, k});     // L(k,j) -> L^T row j
+    for (int s = P.lu_diag[k] + 1; s < P.lu_rowptr[k + 1]; ++s) ut[P.lu_col[s]].push_back({s, k});  // U(k,j) -> U^T row j
+  }
+  std::vector<int> ulev(n, 0), llev(n, 0);
+  int nu = 0, nl = 0;
+  for (int j = 0; j < n; ++j) {
+    int l = 0;
+    for (auto &e : ut[j]) l = std::max(l, ulev[e.second] + 1);
+    ulev[j] = l;
+    nu = std::max(nu, l + 1);
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    int l = 0;
+    for (auto &e : lt[k]) l = std::max(l, llev[e.second] + 1);
+    llev[k] = l;
+    nl = std::max(nl, l + 1);
+  }
+  P.n_utlev = nu;
+  P.n_ltlev = nl;
+  std::vector<int> &T = P.tprog;
+  T.clear();
+  auto mark = [&](int i) {
+    while (T.size() % 4) T.push_back(0);
+    P.tp_off[i] = (int)T.size();
+  };
+  std::vector<int> ent;
+  auto emit = [&](const std::vector<int> &lv, int nlev, const std::vector<std::vector<std::pair<int, int>>> &rows,
+                  bool with_diag, int ptr_sec, int desc_sec) {
+    std::vector<int> ptr(nlev + 1, 0), order;
+    for (int k = 0; k < n; ++k) ptr[lv[k] + 1]++;
+    for (int l = 0; l < nlev; ++l) ptr[l + 1] += ptr[l];
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    order.assign(n, 0);
+    for (int k = 0; k < n; ++k) order[fill[lv[k]]++] = k;
+    mark(ptr_sec);
+    T.insert(T.end(), ptr.begin(), ptr.end());
+    mark(desc_sec);
+    for (int k : order) {
+      T.insert(T.end(), {k | ((int)rows[k].size() << 16), (int)ent.size() / 2, with_diag ? P.lu_diag[k] : -1, 0});
+      for (auto &e : rows[k]) ent.insert(ent.end(), {e.first, e.second});
+    }
+  };
+  emit(ulev, nu, ut, true, 0, 1);
+  emit(llev, nl, lt, false, 2, 3);
+  // longest row of each U^T / L^T level
+  for (int pass = 0; pass < 2; ++pass) {
+    const std::vector<int> &lv = pass ? llev : ulev;
+    const auto &rows = pass ? lt : ut;
+    std::vector<int> mx(pass ? nl : nu, 0);
+    for (int k = 0; k < n; ++k) mx[lv[k]] = std::max(mx[lv[k]], (int)rows[k].size());
+    mark(6 + pass);
+    T.insert(T.end(), mx.begin(), mx.end());
+  }
+  mark(4);
+  T.insert(T.end(), ent.begin(), ent.end());
+  mark(5);
 }
 
 // ------------------------------------------------------------------ program
@@ -656,6 +749,7 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
     P.bd_ptr[r + 1] = (int)P.bd_op.size();
   }
   pack_step_program(el, P);
+  if (mode == MODE_TRAN) pack_transposed_program(P);
   uint64_t sig = 1469598103934665603ull;
   sig = fnv1a(sig, (uint64_t)mode);
   sig = fnv1a(sig, (uint64_t)n);
@@ -779,7 +873,20 @@ extern "C" krets_status krets_symbolic_export(const krets_element *elems, int32_
                                     &P.a_slot, &P.a_cptr, &P.a_contrib, &P.b_cptr, &P.b_contrib, &P.piv_ptr,
                                     &P.piv, &P.upd, &P.lev_ptr, &P.lev_rows, &P.ulev_ptr, &P.ulev_rows,
                                     &P.el_pos};
-  if (which < 0 || which > KRETS_PROG_META) return KRETS_ERR_INVALID_ARGUMENT;
+  if (which < 0 || which > KRETS_PROG_TPOFF) return KRETS_ERR_INVALID_ARGUMENT;
+  if (which == KRETS_PROG_TPROG || which == KRETS_PROG_TPOFF) {
+    std::vector<long long> v;
+    if (which == KRETS_PROG_TPROG) v.assign(P.tprog.begin(), P.tprog.end());
+    else {
+      v.assign(P.tp_off, P.tp_off + 8);
+      v.push_back(P.n_utlev);
+      v.push_back(P.n_ltlev);
+    }
+    *len = (int64_t)v.size();
+    if (out)
+      for (int64_t k = 0; k < std::min<int64_t>(cap, *len); ++k) out[k] = v[k];
+    return KRETS_OK;
+  }
   if (which == KRETS_PROG_META) {
     *len = (int64_t)meta.size();
     if (out)

@@ -62,8 +62,15 @@ struct Program {
   // compact step program, copied into shared memory by the warp engine (sprog_ok = the
   // sizes fit its 16-bit packing).  Layout and packing: see pack_step_program().
   std::vector<int> sprog;
-  int sp_off[12] = {0};
+  int sp_off[14] = {0};
   bool sprog_ok = false;
+  // transposed-solve program (adjoint): A^T y = c  <=>  U^T z = c[q], then L^T y' = z, y = y'[pinv]
+  //   tprog sections: [0] ut_ptr (levels of U^T, forward)  [1] ut_desc int4 {row | cnt << 16,
+  //   first entry, diag slot, 0}  [2] lt_ptr (levels of L^T, backward)  [3] lt_desc
+  //   {row | cnt << 16, first entry, -1, 0}  [4] entries int2 {lu slot, column}  [5] end
+  std::vector<int> tprog;
+  int tp_off[8] = {0};
+  int n_utlev = 0, n_ltlev = 0;
   // per element: 1 when it is a capacitor whose TR history current is state
   long long factor_flops = 0;
   int max_row_lu = 0;

@@ -39,6 +39,7 @@ struct SProg {
   const int *res_op;
   const int4 *dyn;
   const int *bd_ptr, *bd_op, *qinv;
+  const int *lmax, *umax;  // longest row of each L / U level
   int nlev, nulev;
 };
 
@@ -55,6 +56,8 @@ __device__ __forceinline__ SProg sprog_view(const DevProg &P, const int *sp) {
   S.bd_ptr = sp + P.sp_off[8];
   S.bd_op = sp + P.sp_off[9];
   S.qinv = sp + P.sp_off[10];
+  S.lmax = sp + P.sp_off[12];
+  S.umax = sp + P.sp_off[13];
   S.nlev = P.nlev;
   S.nulev = P.nulev;
   return S;
@@ -730,15 +733,62 @@ __device__ __forceinline__ void df_level(const SProg &S, const df *__restrict__ 
   }
 }
 
-template <int G, bool UPPER>
+// Lanes per row for a level of `rows` rows whose longest row has `mx` entries: rows with
+// more than two entries per lane are split over up to 8 lanes of a warp while the level
+// still fits the group.
+template <int G>
+__device__ __forceinline__ int split_lanes(int rows, int mx) {
+  int s = 1;
+  while (s < 8 && mx > 2 * s && rows * s * 2 <= G) s *= 2;
+  return s;
+}
+
+// Sum a double-float over the `spl` aligned lanes of a row (xor butterfly: every lane ends
+// with the same sum, formed in the same order on every run).
+__device__ __forceinline__ df df_lane_sum(df s, int spl, unsigned mask) {
+  for (int o = spl >> 1; o > 0; o >>= 1) {
+    df r;
+    r.hi = __shfl_xor_sync(mask, s.hi, o);
+    r.lo = __shfl_xor_sync(mask, s.lo, o);
+    s = df_add(s, r);
+  }
+  return s;
+}
+
+// One level with each row split over `spl` lanes (a power of two <= 8): lane j of a row
+// takes entries j, j + spl, ...; the first lane adds the right-hand side and writes.
+template <bool UPPER>
+__device__ __forceinline__ void df_level_split(const SProg &S, const df *__restrict__ lu, df *y, const int *ptr,
+                                               const int4 *desc, int l, int tid, int nthreads, int spl) {
+  const int r0 = ptr[l], r1 = ptr[l + 1];
+  const int sub = tid & (spl - 1);
+  const unsigned mask = ((1u << spl) - 1u) << ((threadIdx.x & 31) & ~(spl - 1));
+  for (int t = r0 + tid / spl; t < r1; t += nthreads / spl) {
+    const int4 d = desc[t];
+    const int k = d.x & 0xffff;
+    const int cnt = d.w + (int)((unsigned)d.x >> 16);
+    const int first = UPPER ? d.y + 1 : d.y;
+    df s = sub == 0 ? y[k] : df{0.f, 0.f};
+    for (int j = sub; j < cnt; j += spl) s = df_fma(df_neg(lu[first + j]), y[S.lu_col[first + j]], s);
+    s = df_lane_sum(s, spl, mask);
+    if (sub == 0) y[k] = UPPER ? df_mul(s, lu[d.y]) : s;
+  }
+}
+
+// SG: group size the row splits are chosen for (a caller that must reproduce another
+// group size's arithmetic bit for bit passes that size)
+template <int G, bool UPPER, int SG = G>
 __device__ __forceinline__ void df_solve(const SProg &S, const df *__restrict__ lu, df *y, int gl, int gid, int nar) {
   const int nl = UPPER ? S.nulev : S.nlev;
   const int *ptr = UPPER ? S.ulev_ptr : S.lev_ptr;
   const int4 *desc = UPPER ? S.udesc : S.ldesc;
+  const int *mx = UPPER ? S.umax : S.lmax;
   const bool w0 = gl < 32;
   if (nar < 0) {  // no narrow-level split: every level on the whole group
     for (int l = UPPER ? 0 : 1; l < nl; ++l) {
-      df_level<G, UPPER>(S, lu, y, ptr, desc, l, gl, G);
+      const int spl = split_lanes<SG>(ptr[l + 1] - ptr[l], mx[l]);
+      if (spl > 1) df_level_split<UPPER>(S, lu, y, ptr, desc, l, gl, G, spl);
+      else df_level<G, UPPER>(S, lu, y, ptr, desc, l, gl, G);
       gsync<G>(gid);
     }
     return;
@@ -791,7 +841,7 @@ __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
   extern __shared__ __align__(16) char smem[];
   const int gl = threadIdx.x % G, gid = threadIdx.x / G;
   {
-    const int words = P.sp_off[11];
+    const int words = P.sp_off[5];  // everything before the residual operators
     const int4 *src = reinterpret_cast<const int4 *>(P.sprog);
     int4 *dst = reinterpret_cast<int4 *>(smem);
     for (int i = threadIdx.x; i < words / 4; i += blockDim.x) dst[i] = src[i];

@@ -685,6 +685,105 @@ int ko_assemble(const ko_elem *el, int ne, int n, int mode, double h, int method
   return st;
 }
 
+/* ------------------------------------------------ adjoint sensitivities (extension) */
+/* Solve A^T y = c with factors of P A Q = L U: U^T w = Q^T c (forward over positions),
+ * L^T v = w (backward), y = P^T v.  c and y may alias; work has n entries. */
+static void ko_lu_tsolve_d(const ko_lu_d *F, const double *c, double *y, double *work) {
+  int n = F->n;
+  for (int k = 0; k < n; ++k) work[k] = c[F->q[k]];
+  for (int k = 0; k < n; ++k) {
+    int pd = F->up[k + 1] - 1;
+    double s = work[k];
+    for (int p = F->up[k]; p < pd; ++p) s -= F->ux[p] * work[F->ui[p]];
+    work[k] = s / F->ux[pd];
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    double s = work[k];
+    for (int p = F->lp[k]; p < F->lp[k + 1]; ++p) s -= F->lx[p] * work[F->pinv[F->li[p]]];
+    work[k] = s;
+  }
+  for (int r = 0; r < n; ++r) y[r] = work[F->pinv[r]];
+}
+
+/* Loss sum_{s=1..N} x_s[out]^2 of a linear transient from a zero operating point and its
+ * gradient with respect to every R, C and L value (0 for other elements), by the discrete
+ * adjoint of the companion recurrence  M x_s = N x_{s-1} + src:
+ *   TR: M = G + (2/h) C, N = (2/h) C - G;  BE: M = G + C/h, N = C/h
+ *   M^T l_s = 2 x_s[out] e_out + N^T l_{s+1},  l_{N+1} = 0
+ *   dloss/dp = sum_s l_s^T (dN/dp x_{s-1} - dM/dp x_s).
+ * N^T l is formed as a C^T l - (M^T l from M's triplets): an independent route from the
+ * device kernel's recurrence on previous right-hand sides. */
+int ko_adjoint_tran(const ko_elem *el, int ne, int n, const ko_cfg *cfg, double h, int n_steps, int method,
+                    int out, double *loss, double *grad) {
+  if (out < 0 || out >= n || n_steps < 1) return KO_BADELEM;
+  if (ko_nonlinear(el, ne, 0)) return KO_NOTIMPL;
+  for (int k = 0; k < ne; ++k)
+    if ((el[k].kind == K_R || el[k].kind == K_C) && (el[k].flags & F_G2)) return KO_NOTIMPL;
+  double *X = (double *)malloc(sizeof(double) * (size_t)(n_steps + 1) * n);
+  double *lam = (double *)calloc(n, sizeof(double)), *nxt = (double *)calloc(n, sizeof(double));
+  double *rhs = (double *)malloc(sizeof(double) * n), *work = (double *)malloc(sizeof(double) * n);
+  double *zero = (double *)calloc(n, sizeof(double)), *icap = (double *)calloc(ne > 0 ? ne : 1, sizeof(double));
+  ko_tlist G = {0}, E = {0};
+  ko_solver S = {0};
+  S.n = n;
+  int st = ko_tran(el, ne, n, cfg, h, n_steps, method, 0, X, NULL);
+  for (int k = 0; !st && k < n; ++k)
+    if (X[k] != 0.0) st = KO_NOTIMPL; /* the recurrence starts from x_0 = 0 */
+  if (!st) {
+    ko_ctx cx = {0};
+    cx.mode = MODE_TRAN;
+    cx.guess = zero;
+    cx.prev = zero;
+    cx.h = h;
+    cx.trap = method == 1;
+    cx.ic_prev = icap;
+    cx.t_now = h;
+    for (int k = 0; !st && k < ne; ++k) st = ko_stamp(&el[k], k, &cx, &G, &E);
+  }
+  if (!st) st = ko_factor(&S, &G);
+  if (!st) {
+    const double a = method == 1 ? 2.0 / h : 1.0 / h, ca = method == 1 ? 2.0 * a : a;
+    double L = 0.0;
+    for (int k = 0; k < ne; ++k) grad[k] = 0.0;
+    for (int s = n_steps; s >= 1; --s) {
+      const double *xs = X + (size_t)s * n, *xp = X + (size_t)(s - 1) * n;
+      L += xs[out] * xs[out];
+      for (int k = 0; k < n; ++k) rhs[k] = 0.0;
+      for (int k = 0; k < ne; ++k) { /* C^T l_{s+1}, scaled */
+        const ko_elem *e = &el[k];
+        if (e->kind == K_C) {
+          double u = e->value * ((e->p >= 0 ? nxt[e->p] : 0.0) - (e->m >= 0 ? nxt[e->m] : 0.0));
+          if (e->p >= 0) rhs[e->p] += ca * u;
+          if (e->m >= 0) rhs[e->m] -= ca * u;
+        } else if (e->kind == K_L && e->b >= 0) {
+          rhs[e->b] -= ca * e->value * nxt[e->b];
+        }
+      }
+      if (method == 1)
+        for (long t = 0; t < G.n; ++t) rhs[G.t[t].c] -= creal(G.t[t].v) * nxt[G.t[t].r];
+      rhs[out] += 2.0 * xs[out];
+      ko_lu_tsolve_d(&S.Fd, rhs, lam, work);
+      for (int k = 0; k < ne; ++k) {
+        const ko_elem *e = &el[k];
+        double dl = (e->p >= 0 ? lam[e->p] : 0.0) - (e->m >= 0 ? lam[e->m] : 0.0);
+        double vn = (e->p >= 0 ? xs[e->p] : 0.0) - (e->m >= 0 ? xs[e->m] : 0.0);
+        double vp = (e->p >= 0 ? xp[e->p] : 0.0) - (e->m >= 0 ? xp[e->m] : 0.0);
+        if (e->kind == K_R) grad[k] += dl * (method == 1 ? vp + vn : vn) / (e->value * e->value);
+        else if (e->kind == K_C) grad[k] += a * dl * (vp - vn);
+        else if (e->kind == K_L && e->b >= 0) grad[k] += a * lam[e->b] * (xs[e->b] - xp[e->b]);
+      }
+      double *tmp = nxt;
+      nxt = lam;
+      lam = tmp;
+    }
+    *loss = L;
+  }
+  free(X); free(lam); free(nxt); free(rhs); free(work); free(zero); free(icap);
+  free(G.t); free(E.t);
+  ko_solver_free(&S);
+  return st;
+}
+
 /* Solve a dense/CSC system with the oracle LU (used to cross-check the LU itself). */
 int ko_lu_solve_csc(int n, const int *ap, const int *ai, const double *ax, const double *b, double *x) {
   int *q = ko_mindeg(n, ap, ai);

@@ -54,6 +54,7 @@ def lib():
         L.ko_tran.argtypes = [P, I, I, P, D, I, I, I, P, P]
         L.ko_assemble.argtypes = [P, I, I, I, D, I, D, P, P, P]
         L.ko_lu_solve_csc.argtypes = [I, P, P, P, P, P]
+        L.ko_adjoint_tran.argtypes = [P, I, I, P, D, I, I, I, P, P]
         L.ko_pulse.argtypes = [P, D]
         L.ko_pulse.restype = D
         L.ko_sin.argtypes = [P, D]
@@ -122,6 +123,18 @@ def tran(table, n, h, n_steps, method="be", lag=None, config=None, faithful=Fals
     if st:
         raise OracleError(st, "tran")
     return (x, iters) if return_iters else x
+
+
+def adjoint_tran(table, n, h, n_steps, out, method="tr", config=None):
+    """Loss sum_s x_s[out]^2 and its gradient w.r.t. every element value (FP64 adjoint)."""
+    loss = ctypes.c_double(0.0)
+    grad = np.zeros(len(table))
+    c = _cfg(config)
+    st = lib().ko_adjoint_tran(_p(table), len(table), n, ctypes.byref(c), h, n_steps,
+                               1 if method == "tr" else 0, out, ctypes.byref(loss), _p(grad))
+    if st:
+        raise OracleError(st, "adjoint_tran")
+    return loss.value, grad
 
 
 def assemble(table, n, mode="dc", h=0.0, method="be", freq=0.0, sol=None):

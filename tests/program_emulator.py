@@ -120,3 +120,60 @@ def emulate(prog, table, n, ca, cb, complex_=False):
 
 def export(table, n, mode, method="be", h=1.0, freq=1e3, ordering=-1):
     return _lib.symbolic_export(table, n, mode, method, h, freq, ordering)
+
+
+def factor_only(prog, n, ca, complex_=False):
+    """Stamp and factor with the program (as emulate()); returns the LU value array."""
+    dt = complex if complex_ else float
+    cav = ca if complex_ else ca.real
+    lu = np.zeros(len(prog["lu_col"]), dtype=dt)
+    for t in range(len(prog["a_col"])):
+        s = dt(0)
+        for u in range(prog["a_cptr"][t], prog["a_cptr"][t + 1]):
+            code = int(prog["a_contrib"][u])
+            val = dt(1.0) if code & 2 else cav[code >> 2]
+            s += -val if code & 1 else val
+        lu[prog["a_slot"][t]] = s
+    piv = prog["piv"].reshape(-1, 4)
+    upd = prog["upd"].reshape(-1, 2)
+    diag = prog["lu_diag"]
+    lev_ptr, lev_rows = prog["lev_ptr"], prog["lev_rows"]
+    for lv in range(len(lev_ptr) - 1):
+        for k in lev_rows[lev_ptr[lv]:lev_ptr[lv + 1]]:
+            for pi in range(prog["piv_ptr"][k], prog["piv_ptr"][k + 1]):
+                s, j, u0, u1 = piv[pi]
+                l = lu[s] / lu[diag[j]]
+                lu[s] = l
+                for dst, src in upd[u0:u1]:
+                    lu[dst] -= l * lu[src]
+    return lu
+
+
+def transposed_solve(prog, n, lu, c):
+    """Solve A^T y = c with the transposed program and the (unscaled-diagonal) LU values."""
+    T = prog["tprog"]
+    off = prog["tpoff"]
+    ut_ptr = T[off[0]:off[0] + int(off[8]) + 1]
+    ut_desc = T[off[1]:off[1] + 4 * n].reshape(n, 4)
+    lt_ptr = T[off[2]:off[2] + int(off[9]) + 1]
+    lt_desc = T[off[3]:off[3] + 4 * n].reshape(n, 4)
+    ent = T[off[4]:off[5]].reshape(-1, 2)
+    z = np.asarray(c, dtype=float)[prog["q"]].copy()      # c in position space (columns)
+    for lv in range(len(ut_ptr) - 1):
+        for t in range(ut_ptr[lv], ut_ptr[lv + 1]):
+            r, first, dslot = ut_desc[t][0] & 0xffff, ut_desc[t][1], ut_desc[t][2]
+            cnt = ut_desc[t][0] >> 16
+            s = z[r]
+            for e in range(first, first + cnt):
+                s -= lu[ent[e][0]] * z[ent[e][1]]
+            z[r] = s / lu[dslot]
+    for lv in range(len(lt_ptr) - 1):
+        for t in range(lt_ptr[lv], lt_ptr[lv + 1]):
+            r, first, cnt = lt_desc[t][0] & 0xffff, lt_desc[t][1], lt_desc[t][0] >> 16
+            s = z[r]
+            for e in range(first, first + cnt):
+                s -= lu[ent[e][0]] * z[ent[e][1]]
+            z[r] = s
+    y = np.zeros(n)
+    y[prog["prow"]] = z                                      # position k <-> row prow[k]
+    return y

@@ -55,6 +55,42 @@ def test_tran_programs_match_dense(built_lib, oracle_lib, method, h):
     np.testing.assert_allclose(x, xd, rtol=0, atol=1e-9 * np.abs(xd).max())
 
 
+@pytest.mark.parametrize("sections", [12, 1000])
+def test_transposed_program_solves_adjoint_systems(built_lib, oracle_lib, sections):
+    """The transposed program (used by the adjoint sweep) solves A^T y = c with the forward
+    LU values; its indices stay inside the LU value array and the position vectors."""
+    from krets_gb300.generators import rc_ladder_step
+    c = rc_ladder_step(sections)
+    t = element_table(c)
+    n = c.size
+    h = 1e-9
+    prog = PE.export(t, n, 2, method="tr", h=h)
+    T, off = prog["tprog"], prog["tpoff"]
+    nnz = len(prog["lu_col"])
+    nut, nlt = int(off[8]), int(off[9])
+    for dsec, psec, msec, nlev, upper in ((1, 0, 6, nut, True), (3, 2, 7, nlt, False)):
+        ptr = T[off[psec]:off[psec] + nlev + 1]
+        assert ptr[0] == 0 and ptr[-1] == n and np.all(np.diff(ptr) >= 0)
+        desc = T[off[dsec]:off[dsec] + 4 * n].reshape(n, 4)
+        rows = desc[:, 0] & 0xffff
+        assert sorted(rows) == list(range(n))
+        cnt, first = desc[:, 0] >> 16, desc[:, 1]
+        mx = T[off[msec]:off[msec] + nlev]
+        assert all(mx[l] == cnt[ptr[l]:ptr[l + 1]].max() for l in range(nlev))
+        assert np.all(first + cnt <= (off[5] - off[4]) // 2)
+        if upper:
+            assert np.all((desc[:, 2] >= 0) & (desc[:, 2] < nnz))
+    ent = T[off[4]:off[5]].reshape(-1, 2)
+    assert np.all((ent[:, 0] >= 0) & (ent[:, 0] < nnz) & (ent[:, 1] >= 0) & (ent[:, 1] < n))
+    ca, _ = PE.element_coefs(t, 2, "tr", h, prev=np.zeros(n), icap=np.zeros(len(t)))
+    lu = PE.factor_only(prog, n, ca)
+    A, _ = oracle_lib.assemble(t, n, "tran", h, "tr", sol=np.zeros(n))
+    rhs = np.sin(np.arange(n) * 0.7)
+    y = PE.transposed_solve(prog, n, lu, rhs)
+    yd = np.linalg.solve(A.T, rhs)
+    np.testing.assert_allclose(y, yd, rtol=0, atol=1e-10 * np.abs(yd).max())
+
+
 def test_ac_program_static_pivots_hold_over_nine_decades(built_lib, oracle_lib):
     c = rc_ladder_ac(120)
     t = element_table(c)
