@@ -171,6 +171,28 @@ krets_status krets_adjoint_tran(krets_circuit *c, int32_t n_inst, const double *
                                 int32_t method, int32_t out_unknown, int32_t checkpoint_every, int32_t gradient,
                                 double *loss_out, double *grad_out);
 
+/* ---- Many distinct linear circuits (R, C, L, V, I) in one launch set (no counterpart in the
+ * reference, whose Solver runs one circuit at a time: krets-solver/src/solver.rs:22-52).
+ * Circuit c has elements elems[elem_offsets[c] .. elem_offsets[c+1]) numbered over its own
+ * n_unknowns[c] unknowns.  krets_multi_create runs the host symbolic pass of every circuit
+ * (DC program for the operating point, transient program for method/h) on all host threads
+ * and uploads them in one device image. */
+typedef struct krets_multi krets_multi;
+krets_status krets_multi_create(int32_t n_circuits, const krets_element *elems, const int64_t *elem_offsets,
+                                const int32_t *n_unknowns, int32_t method, double h, krets_multi **out);
+krets_status krets_multi_destroy(krets_multi *m);
+/* info[0..3] = circuits, sum of n, sum of transient LU entries, sum of transient solve levels;
+ * info[4..] = circuits per size class (shared-memory regions from small to large, then global). */
+krets_status krets_multi_info(const krets_multi *m, int64_t *info, int32_t cap);
+/* Operating point then n_steps transient steps of every circuit (transient.rs:14-114 per
+ * circuit).  Circuit c writes (n_steps+1) x n_c doubles (row 0 = operating point, original
+ * unknown order) at x_out + x_offsets[c] (x_offsets NULL: circuits packed in order).
+ * x_out may be host or device memory.  circuit_status (optional) receives each circuit's
+ * status. */
+krets_status krets_multi_tran(krets_multi *m, int32_t n_steps, int32_t source_lag, double *x_out,
+                              const int64_t *x_offsets, int32_t *circuit_status);
+krets_status krets_multi_last_timing(const krets_multi *m, float *kernel_ms, float *call_ms);
+
 /* Batched operating points: x_out[n_inst][n]. */
 krets_status krets_batch_op(krets_circuit *c, int32_t n_inst, const double *values, double *x_out,
                             int32_t *inst_status);

@@ -70,6 +70,11 @@ def lib():
             "krets_batch_ac": [_P, _I, _P, _P, _I, _I, _P, _P],
             "krets_batch_tran_noalloc": [_P, _I, _P, _D, _I, _I, _I, _I, _P, _P],
             "krets_adjoint_tran": [_P, _I, _P, _D, _I, _I, _I, _I, _I, _P, _P],
+            "krets_multi_create": [_I, _P, _P, _P, _I, _D, _P],
+            "krets_multi_destroy": [_P],
+            "krets_multi_info": [_P, _P, _I],
+            "krets_multi_tran": [_P, _I, _I, _P, _P, _P],
+            "krets_multi_last_timing": [_P, _P, _P],
             "krets_batch_op": [_P, _I, _P, _P, _P],
             "krets_last_timing": [_P, _P, _P],
             "krets_last_refine_stats": [_P, _P, _P],
@@ -144,6 +149,63 @@ class DeviceArray:
             self.free()
         except Exception:
             pass
+
+
+class MultiCircuit:
+    """Many distinct linear circuits (tables with their own unknown counts) run together."""
+
+    def __init__(self, tables, sizes, method="be", h=1e-9):
+        self.sizes = np.asarray(sizes, dtype=np.int32)
+        self.tables = [np.ascontiguousarray(t, dtype=ELEM_DTYPE) for t in tables]
+        el = np.concatenate(self.tables) if self.tables else np.zeros(0, ELEM_DTYPE)
+        off = np.zeros(len(self.tables) + 1, dtype=np.int64)
+        off[1:] = np.cumsum([len(t) for t in self.tables])
+        self.method = method
+        h_ = ctypes.c_void_p()
+        check(lib().krets_multi_create(len(self.tables), ptr(el), ptr(off), ptr(self.sizes), METHOD[method], h,
+                                       ctypes.byref(h_)), "multi_create")
+        self.h = h_
+
+    def close(self):
+        if self.h:
+            lib().krets_multi_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def offsets(self, n_steps):
+        off = np.zeros(len(self.sizes), dtype=np.int64)
+        off[1:] = np.cumsum((n_steps + 1) * self.sizes.astype(np.int64))[:-1]
+        return off
+
+    def total(self, n_steps):
+        return int((n_steps + 1) * self.sizes.astype(np.int64).sum())
+
+    def tran(self, n_steps, lag=None, out=None):
+        """Operating point then n_steps steps; returns the flat output (or fills `out`,
+        a host array or DeviceArray of total(n_steps) doubles) and per-circuit status."""
+        if lag is None:
+            lag = self.method == "be"
+        if out is None:
+            out = np.zeros(self.total(n_steps))
+        st = np.zeros(len(self.sizes), dtype=np.int32)
+        check(lib().krets_multi_tran(self.h, n_steps, int(bool(lag)), ptr(out), None, ptr(st)), "multi_tran")
+        return out, st
+
+    def split(self, flat, n_steps):
+        off = self.offsets(n_steps)
+        return [flat[o:o + (n_steps + 1) * n].reshape(n_steps + 1, n) for o, n in zip(off, self.sizes)]
+
+    def info(self):
+        v = np.zeros(12, dtype=np.int64)
+        check(lib().krets_multi_info(self.h, ptr(v), len(v)), "multi_info")
+        return v
+
+    def timing(self):
+        k = ctypes.c_float()
+        c = ctypes.c_float()
+        check(lib().krets_multi_last_timing(self.h, ctypes.byref(k), ctypes.byref(c)))
+        return k.value, c.value
 
 
 class GpuCircuit:

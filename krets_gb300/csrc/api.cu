@@ -11,11 +11,13 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "kernels.cuh"
 #include "warp_kernels.cuh"
 #include "adjoint.cuh"
+#include "multi.cuh"
 #include "krets_gpu.h"
 #include "symbolic.h"
 
@@ -140,40 +142,50 @@ struct krets_circuit {
 
 namespace {
 
-krets_status upload_program(krets_circuit *c, Program &&P, DevProgram &D) {
-  D.host = std::move(P);
-  Program &H = D.host;
-  // compute lu_src: A entry index per LU slot
-  std::vector<int> lu_src(H.lu_col.size(), -1);
-  for (size_t t = 0; t < H.a_slot.size(); ++t) lu_src[H.a_slot[t]] = (int)t;
-  std::vector<int> is_cur(H.n, 0);
+// Device image of a program: every array at a 16-byte aligned offset of one buffer.
+// program_bytes() sizes it; place_program() writes the arrays into a host staging copy of
+// that buffer (host_base) and sets the view's pointers into its device copy (dev_base).
+struct ProgramImage {
+  std::vector<int> lu_src, is_cur;
+};
+
+static void image_extras(const Program &H, ProgramImage &X) {
+  X.lu_src.assign(H.lu_col.size(), -1);
+  for (size_t t = 0; t < H.a_slot.size(); ++t) X.lu_src[H.a_slot[t]] = (int)t;
+  X.is_cur.assign(H.n, 0);
   for (int e = 0; e < H.ne; ++e)
-    if (H.el_pos[4 * e + 2] >= 0) is_cur[H.el_pos[4 * e + 2]] = 1;
-  struct Part { const void *src; size_t bytes; size_t off; };
-  std::vector<Part> parts;
+    if (H.el_pos[4 * e + 2] >= 0) X.is_cur[H.el_pos[4 * e + 2]] = 1;
+}
+
+template <typename F>
+static void for_each_array(const Program &H, const ProgramImage &X, F &&f) {
+  f(H.q); f(H.lu_rowptr); f(H.lu_col); f(H.lu_diag); f(X.lu_src);
+  f(H.a_rowptr); f(H.a_col); f(H.a_cptr); f(H.a_contrib);
+  f(H.b_cptr); f(H.b_contrib); f(H.piv_ptr); f(H.piv); f(H.upd);
+  f(H.lev_ptr); f(H.lev_rows); f(H.ulev_ptr); f(H.ulev_rows);
+  f(H.el_pos); f(X.is_cur);
+  f(H.qinv); f(H.ldesc); f(H.udesc); f(H.res_ptr); f(H.res_op);
+  f(H.dyn_e); f(H.bd_ptr); f(H.bd_op); f(H.sprog);
+  f(H.tprog); f(H.prow);
+}
+
+static size_t program_bytes(const Program &H, const ProgramImage &X) {
   size_t total = 0;
-  auto add = [&](const void *src, size_t bytes) {
-    parts.push_back({src, bytes, total});
-    total = align16(total + (bytes ? bytes : 4));
-    return parts.size() - 1;
-  };
-  auto vi = [&](const std::vector<int> &v) { return add(v.data(), v.size() * sizeof(int)); };
-  size_t i_q = vi(H.q), i_rp = vi(H.lu_rowptr), i_col = vi(H.lu_col), i_dg = vi(H.lu_diag), i_src = vi(lu_src);
-  size_t i_arp = vi(H.a_rowptr), i_acol = vi(H.a_col), i_acp = vi(H.a_cptr), i_acn = vi(H.a_contrib);
-  size_t i_bcp = vi(H.b_cptr), i_bcn = vi(H.b_contrib), i_pp = vi(H.piv_ptr), i_pv = vi(H.piv), i_up = vi(H.upd);
-  size_t i_lp = vi(H.lev_ptr), i_lr = vi(H.lev_rows), i_ulp = vi(H.ulev_ptr), i_ulr = vi(H.ulev_rows);
-  size_t i_ep = vi(H.el_pos), i_ic = vi(is_cur);
-  size_t i_qi = vi(H.qinv), i_ld = vi(H.ldesc), i_ud = vi(H.udesc), i_rp2 = vi(H.res_ptr), i_ro = vi(H.res_op);
-  size_t i_dy = vi(H.dyn_e), i_bdp = vi(H.bd_ptr), i_bdo = vi(H.bd_op), i_sp = vi(H.sprog);
-  size_t i_tp = vi(H.tprog), i_pr = vi(H.prow);
-  CU(cudaMalloc(&D.buf, total));
-  std::vector<char> staging(total, 0);
-  for (auto &p : parts)
-    if (p.bytes) memcpy(staging.data() + p.off, p.src, p.bytes);
-  CU(cudaMemcpy(D.buf, staging.data(), total, cudaMemcpyHostToDevice));
-  char *b = (char *)D.buf;
-  auto ptr = [&](size_t i) { return (const void *)(b + parts[i].off); };
-  DevProg &V = D.view;
+  for_each_array(H, X, [&](const std::vector<int> &v) { total = align16(total + (v.empty() ? 4 : v.size() * 4)); });
+  return total;
+}
+
+static void place_program(const Program &H, const ProgramImage &X, const krets_element *el_host,
+                          const krets_element *d_el, char *dev_base, char *host_base, DevProg &V) {
+  std::vector<const void *> p;
+  size_t off = 0;
+  for_each_array(H, X, [&](const std::vector<int> &v) {
+    if (!v.empty()) memcpy(host_base + off, v.data(), v.size() * 4);
+    p.push_back(dev_base + off);
+    off = align16(off + (v.empty() ? 4 : v.size() * 4));
+  });
+  size_t i = 0;
+  auto nx = [&]() { return p[i++]; };
   V.n = H.n;
   V.ne = H.ne;
   V.nnz_a = (int)H.a_col.size();
@@ -182,53 +194,64 @@ krets_status upload_program(krets_circuit *c, Program &&P, DevProgram &D) {
   V.nulev = (int)H.ulev_ptr.size() - 1;
   V.mode = H.mode;
   V.method = H.method;
-  V.q = (const int *)ptr(i_q);
-  V.lu_rowptr = (const int *)ptr(i_rp);
-  V.lu_col = (const int *)ptr(i_col);
-  V.lu_diag = (const int *)ptr(i_dg);
-  V.lu_src = (const int *)ptr(i_src);
-  V.a_rowptr = (const int *)ptr(i_arp);
-  V.a_col = (const int *)ptr(i_acol);
-  V.a_cptr = (const int *)ptr(i_acp);
-  V.a_contrib = (const int *)ptr(i_acn);
-  V.b_cptr = (const int *)ptr(i_bcp);
-  V.b_contrib = (const int *)ptr(i_bcn);
-  V.piv_ptr = (const int *)ptr(i_pp);
-  V.piv = (const int4 *)ptr(i_pv);
-  V.upd = (const int2 *)ptr(i_up);
-  V.lev_ptr = (const int *)ptr(i_lp);
-  V.lev_rows = (const int *)ptr(i_lr);
-  V.ulev_ptr = (const int *)ptr(i_ulp);
-  V.ulev_rows = (const int *)ptr(i_ulr);
-  V.el_pos = (const int4 *)ptr(i_ep);
-  V.is_cur = (const int *)ptr(i_ic);
-  V.el = c->d_el;
-  V.qinv = (const int *)ptr(i_qi);
-  V.ldesc = (const int4 *)ptr(i_ld);
-  V.udesc = (const int4 *)ptr(i_ud);
-  V.res_ptr = (const int *)ptr(i_rp2);
-  V.res_op = (const int2 *)ptr(i_ro);
-  V.dyn_e = (const int *)ptr(i_dy);
-  V.bd_ptr = (const int *)ptr(i_bdp);
-  V.bd_op = (const int *)ptr(i_bdo);
+  V.q = (const int *)nx();
+  V.lu_rowptr = (const int *)nx();
+  V.lu_col = (const int *)nx();
+  V.lu_diag = (const int *)nx();
+  V.lu_src = (const int *)nx();
+  V.a_rowptr = (const int *)nx();
+  V.a_col = (const int *)nx();
+  V.a_cptr = (const int *)nx();
+  V.a_contrib = (const int *)nx();
+  V.b_cptr = (const int *)nx();
+  V.b_contrib = (const int *)nx();
+  V.piv_ptr = (const int *)nx();
+  V.piv = (const int4 *)nx();
+  V.upd = (const int2 *)nx();
+  V.lev_ptr = (const int *)nx();
+  V.lev_rows = (const int *)nx();
+  V.ulev_ptr = (const int *)nx();
+  V.ulev_rows = (const int *)nx();
+  V.el_pos = (const int4 *)nx();
+  V.is_cur = (const int *)nx();
+  V.qinv = (const int *)nx();
+  V.ldesc = (const int4 *)nx();
+  V.udesc = (const int4 *)nx();
+  V.res_ptr = (const int *)nx();
+  V.res_op = (const int2 *)nx();
+  V.dyn_e = (const int *)nx();
+  V.bd_ptr = (const int *)nx();
+  V.bd_op = (const int *)nx();
+  V.sprog = (const int *)nx();
+  V.tprog = (const int *)nx();
+  V.prow = (const int *)nx();
+  V.el = d_el;
   V.ndyn = (int)H.dyn_e.size();
   V.ncap = H.ncap;
   V.n_resop = (int)H.res_op.size() / 2;
-  V.sprog = (const int *)ptr(i_sp);
   for (int k = 0; k < 14; ++k) V.sp_off[k] = H.sp_off[k];
   V.sprog_ok = H.sprog_ok;
-  V.tprog = (const int *)ptr(i_tp);
   for (int k = 0; k < 8; ++k) V.tp_off[k] = H.tp_off[k];
   V.n_utlev = H.n_utlev;
   V.n_ltlev = H.n_ltlev;
-  V.prow = (const int *)ptr(i_pr);
   bool nl = false;
   for (int e = 0; e < H.ne; ++e) {
-    int k = c->el[e].kind;
+    int k = el_host[e].kind;
     if (H.mode == MODE_DC && k == KRETS_ELEM_C) continue;
     if (k == KRETS_ELEM_D || k == KRETS_ELEM_M || k == KRETS_ELEM_Q) nl = true;
   }
   V.nonlinear = nl;
+}
+
+krets_status upload_program(krets_circuit *c, Program &&P, DevProgram &D) {
+  D.host = std::move(P);
+  ProgramImage X;
+  image_extras(D.host, X);
+  const size_t total = program_bytes(D.host, X);
+  CU(cudaMalloc(&D.buf, total));
+  std::vector<char> staging(total, 0);
+  place_program(D.host, X, c->el.data(), c->d_el, (char *)D.buf, staging.data(), D.view);
+  CU(cudaMemcpy(D.buf, staging.data(), total, cudaMemcpyHostToDevice));
   return KRETS_OK;
 }
 
@@ -431,6 +454,48 @@ __global__ void k_status_fold(const int *op_status, int *inst_status, int n, int
 }  // namespace
 
 // ====================================================================== C ABI
+// Many distinct circuits run by one multi-circuit launch set (krets_multi_*).
+struct MultiClass {
+  int G = 0, W = 0;          // group size, groups per CTA
+  bool global = false;       // working arrays in global memory
+  long long region = 0;      // bytes per group
+  std::vector<int> items;    // circuits, largest first
+  int grid = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+};
+
+struct krets_multi {
+  int n_circ = 0, method = 0;
+  double h = 0;
+  std::vector<int> n, ne;
+  std::vector<long long> el_off;
+  krets_element *d_el = nullptr;
+  void *d_image = nullptr;  // every program's arrays
+  DevProg *d_views = nullptr;  // [2 * n_circ]: DC, TRAN
+  std::vector<long long> nnz_lu_tr, levels_tr;
+  std::vector<MultiClass> classes;
+  int *d_queue = nullptr, *d_status = nullptr;
+  long long *d_xoff = nullptr;
+  int *d_items = nullptr;
+  char *gscratch = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {};
+  float kernel_ms = 0.f, call_ms = 0.f;
+  ~krets_multi() {
+    for (auto &k : classes) {
+      if (k.stream) cudaStreamDestroy(k.stream);
+      if (k.done) cudaEventDestroy(k.done);
+    }
+    for (auto p : {(void *)d_el, d_image, (void *)d_views, (void *)d_queue, (void *)d_status, (void *)d_xoff,
+                   (void *)d_items, (void *)gscratch})
+      if (p) cudaFree(p);
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
 extern "C" {
 
 krets_status krets_circuit_create(const krets_element *elems, int32_t n_elem, int32_t n_unknowns,
@@ -1242,6 +1307,243 @@ krets_status krets_batch_tran_noalloc(krets_circuit *c, int32_t n_inst, const do
   cudaEventElapsedTime(&c->kernel_ms, c->ev[2], c->ev[3]);
   cudaEventElapsedTime(&c->call_ms, c->ev[0], c->ev[1]);
   return map_status(any_h, 1);
+}
+
+// ------------------------------------------------------------------ multi-circuit
+krets_status krets_multi_create(int32_t n_circuits, const krets_element *elems, const int64_t *elem_offsets,
+                                const int32_t *n_unknowns, int32_t method, double h, krets_multi **out) {
+  if (!out || n_circuits <= 0 || !elems || !elem_offsets || !n_unknowns || !(h > 0) ||
+      (method != KRETS_METHOD_BE && method != KRETS_METHOD_TR))
+    return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments to krets_multi_create");
+  *out = nullptr;
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
+    cudaGetLastError();
+    return fail(KRETS_ERR_CUDA, "no CUDA device is available (this library has no CPU fallback)");
+  }
+  auto m = std::make_unique<krets_multi>();
+  const int N = n_circuits;
+  m->n_circ = N;
+  m->method = method;
+  m->h = h;
+  m->n.assign(n_unknowns, n_unknowns + N);
+  m->el_off.assign(elem_offsets, elem_offsets + N + 1);
+  m->ne.resize(N);
+  for (int c = 0; c < N; ++c) {
+    const long long e0 = m->el_off[c], e1 = m->el_off[c + 1];
+    if (e1 < e0 || m->n[c] <= 0) return fail(KRETS_ERR_INVALID_ARGUMENT, "circuit " + std::to_string(c) + ": bad sizes");
+    m->ne[c] = (int)(e1 - e0);
+    for (long long e = e0; e < e1; ++e) {
+      const krets_element &x = elems[e];
+      if (x.kind < KRETS_ELEM_R || x.kind > KRETS_ELEM_Q)
+        return fail(KRETS_ERR_INVALID_ELEMENT, "circuit " + std::to_string(c) + ": unknown element kind");
+      for (int v : {x.p, x.m, x.b, x.g})
+        if (v < -1 || v >= m->n[c])
+          return fail(KRETS_ERR_INVALID_ARGUMENT, "circuit " + std::to_string(c) + ": unknown index out of range");
+    }
+  }
+  // host symbolic pass of every circuit (DC and TRAN programs), on all host threads
+  std::vector<Program> progs(2 * (size_t)N);
+  std::vector<int> pst(2 * (size_t)N, 0);
+  std::vector<std::string> pmsg(2 * (size_t)N);
+  {
+    std::atomic<int> next{0};
+    const int nt = std::max(1, std::min((int)std::thread::hardware_concurrency(), 64));
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&]() {
+        for (int j; (j = next.fetch_add(1)) < 2 * N;) {
+          const int c = j / 2, mode = (j & 1) ? MODE_TRAN : MODE_DC;
+          pst[j] = build_program(elems + m->el_off[c], m->ne[c], m->n[c], mode, method, h, 0.0, -1, progs[j], pmsg[j],
+                                 false);
+        }
+      });
+    for (auto &t : th) t.join();
+  }
+  for (int j = 0; j < 2 * N; ++j) {
+    if (pst[j] != KRETS_OK) return fail(pst[j], "circuit " + std::to_string(j / 2) + ": " + pmsg[j]);
+    bool nonlinear = false;
+    for (long long e = m->el_off[j / 2]; e < m->el_off[j / 2 + 1]; ++e)
+      nonlinear |= elems[e].kind == KRETS_ELEM_D || elems[e].kind == KRETS_ELEM_M || elems[e].kind == KRETS_ELEM_Q;
+    if (nonlinear)
+      return fail(KRETS_ERR_NOT_IMPLEMENTED, "circuit " + std::to_string(j / 2) +
+                                                 ": the multi-circuit engine runs linear circuits (R, C, L, V, I)");
+    if (!progs[j].sprog_ok) return fail(KRETS_ERR_INVALID_ARGUMENT, "circuit " + std::to_string(j / 2) + " too large");
+  }
+  // one device image for all programs
+  CU(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+  for (auto &e : m->ev) CU(cudaEventCreate(&e));
+  const long long ne_total = m->el_off[N];
+  CU(cudaMalloc(&m->d_el, sizeof(krets_element) * std::max(1ll, ne_total)));
+  CU(cudaMemcpy(m->d_el, elems, sizeof(krets_element) * ne_total, cudaMemcpyHostToDevice));
+  std::vector<ProgramImage> X(2 * (size_t)N);
+  std::vector<size_t> off(2 * (size_t)N + 1, 0);
+  for (int j = 0; j < 2 * N; ++j) {
+    image_extras(progs[j], X[j]);
+    off[j + 1] = off[j] + program_bytes(progs[j], X[j]);
+  }
+  CU(cudaMalloc(&m->d_image, off[2 * N]));
+  std::vector<DevProg> views(2 * (size_t)N);
+  {
+    std::vector<char> staging(off[2 * N], 0);
+    for (int j = 0; j < 2 * N; ++j) {
+      const int c = j / 2;
+      place_program(progs[j], X[j], elems + m->el_off[c], m->d_el + m->el_off[c], (char *)m->d_image + off[j],
+                    staging.data() + off[j], views[j]);
+    }
+    CU(cudaMemcpy(m->d_image, staging.data(), off[2 * N], cudaMemcpyHostToDevice));
+  }
+  CU(cudaMalloc(&m->d_views, sizeof(DevProg) * views.size()));
+  CU(cudaMemcpy(m->d_views, views.data(), sizeof(DevProg) * views.size(), cudaMemcpyHostToDevice));
+  // size classes: the smallest shared-memory region that holds both phases of a circuit
+  const long long smax = (long long)max_smem_optin();
+  struct Spec { int G, W; };
+  const Spec specs[] = {{32, 16}, {32, 8}, {64, 4}, {128, 2}, {128, 1}};
+  for (const Spec &sp : specs) {
+    MultiClass k;
+    k.G = sp.G;
+    k.W = sp.W;
+    k.region = (smax / sp.W) & ~15ll;
+    m->classes.push_back(k);
+  }
+  MultiClass kg;
+  kg.G = 256;
+  kg.W = 1;
+  kg.global = true;
+  m->classes.push_back(kg);
+  std::vector<long long> need(N), need_g(N);
+  m->nnz_lu_tr.resize(N);
+  m->levels_tr.resize(N);
+  for (int c = 0; c < N; ++c) {
+    long long a = 0, g = 0;
+    for (int ph = 0; ph < 2; ++ph) {
+      const DevProg &V = views[2 * c + ph];
+      a = std::max<long long>(a, multi_lay(V.nnz_lu, V.n, V.ndyn, V.ncap, V.ne, V.sp_off[5]).bytes);
+      g = std::max<long long>(g, multi_lay(V.nnz_lu, V.n, V.ndyn, V.ncap, V.ne, 0).bytes);
+    }
+    need[c] = a;
+    need_g[c] = g;
+    m->nnz_lu_tr[c] = views[2 * c + 1].nnz_lu;
+    m->levels_tr[c] = views[2 * c + 1].nlev + views[2 * c + 1].nulev;
+  }
+  std::vector<int> order(N);
+  for (int c = 0; c < N; ++c) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return need[a] > need[b]; });
+  for (int c : order) {
+    // smallest fitting region: the classes are in increasing region size
+    int pick = -1;
+    for (size_t q = 0; q + 1 < m->classes.size(); ++q)
+      if (m->classes[q].region >= need[c]) { pick = (int)q; break; }
+    if (pick < 0) {
+      pick = (int)m->classes.size() - 1;
+      m->classes[pick].region = std::max(m->classes[pick].region, (long long)mlay_al16(need_g[c]));
+    }
+    m->classes[pick].items.push_back(c);
+  }
+  std::vector<int> all_items;
+  long long gscratch_bytes = 0;
+  for (auto &k : m->classes) {
+    if (k.items.empty()) continue;
+    CU(cudaStreamCreateWithFlags(&k.stream, cudaStreamNonBlocking));
+    CU(cudaEventCreateWithFlags(&k.done, cudaEventDisableTiming));
+    const int per_sm = k.global ? 2 : 1;
+    k.grid = std::max(1, std::min(((int)k.items.size() + k.W - 1) / k.W, per_sm * device_sm_count()));
+    if (k.global) gscratch_bytes = k.region * k.grid * k.W;
+    all_items.insert(all_items.end(), k.items.begin(), k.items.end());
+  }
+  CU(cudaMalloc(&m->d_items, sizeof(int) * all_items.size()));
+  CU(cudaMemcpy(m->d_items, all_items.data(), sizeof(int) * all_items.size(), cudaMemcpyHostToDevice));
+  CU(cudaMalloc(&m->d_queue, sizeof(int) * 16));
+  CU(cudaMalloc(&m->d_status, sizeof(int) * N));
+  CU(cudaMalloc(&m->d_xoff, sizeof(long long) * N));
+  if (gscratch_bytes) CU(cudaMalloc(&m->gscratch, gscratch_bytes));
+  *out = m.release();
+  return KRETS_OK;
+}
+
+krets_status krets_multi_destroy(krets_multi *m) {
+  delete m;
+  return KRETS_OK;
+}
+
+krets_status krets_multi_info(const krets_multi *m, int64_t *info, int32_t cap) {
+  if (!m || !info || cap < 4) return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments to krets_multi_info");
+  long long sn = 0, snnz = 0, slev = 0;
+  for (int c = 0; c < m->n_circ; ++c) {
+    sn += m->n[c];
+    snnz += m->nnz_lu_tr[c];
+    slev += m->levels_tr[c];
+  }
+  std::vector<long long> v{m->n_circ, sn, snnz, slev};
+  for (auto &k : m->classes) v.push_back((long long)k.items.size());
+  for (int i = 0; i < cap && i < (int)v.size(); ++i) info[i] = v[i];
+  return KRETS_OK;
+}
+
+krets_status krets_multi_tran(krets_multi *m, int32_t n_steps, int32_t source_lag, double *x_out,
+                              const int64_t *x_offsets, int32_t *circuit_status) {
+  if (!m || n_steps < 0 || !x_out) return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments to krets_multi_tran");
+  const int N = m->n_circ;
+  std::vector<long long> xo(N);
+  long long total = 0;
+  for (int c = 0; c < N; ++c) {
+    xo[c] = x_offsets ? x_offsets[c] : total;
+    total = std::max(total, xo[c] + (long long)(n_steps + 1) * m->n[c]);
+  }
+  CU(cudaEventRecord(m->ev[0], m->stream));
+  DevBuf tx;
+  void *dx;
+  krets_status s = dev_view(x_out, sizeof(double) * total, false, m->stream, tx, &dx);
+  if (s) return s;
+  CU(cudaMemcpyAsync(m->d_xoff, xo.data(), sizeof(long long) * N, cudaMemcpyHostToDevice, m->stream));
+  CU(cudaMemsetAsync(m->d_queue, 0, sizeof(int) * 16, m->stream));
+  CU(cudaMemsetAsync(m->d_status, 0, sizeof(int) * N, m->stream));
+  CU(cudaEventRecord(m->ev[2], m->stream));
+  // every size class on its own stream: CTAs of the next class fill SMs as a class drains
+  int base = 0, qi = 0;
+  for (auto &k : m->classes) {
+    if (k.items.empty()) continue;
+    CU(cudaStreamWaitEvent(k.stream, m->ev[2], 0));
+    const int threads = k.G * k.W;
+    const size_t smem = k.global ? 0 : (size_t)(k.region * k.W);
+    void (*kern)(const DevProg *, const int *, int, const long long *, long long, char *, double, int, int, int,
+                 double *, int *, int *) = nullptr;
+    if (k.global) kern = k_multi_tran<256, true>;
+    else if (k.G == 32) kern = k_multi_tran<32, false>;
+    else if (k.G == 64) kern = k_multi_tran<64, false>;
+    else kern = k_multi_tran<128, false>;
+    if (!k.global) CU(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<k.grid, threads, smem, k.stream>>>(m->d_views, m->d_items + base, (int)k.items.size(), m->d_xoff, k.region,
+                                             m->gscratch, m->h, n_steps, m->method, source_lag, (double *)dx,
+                                             m->d_status, m->d_queue + qi);
+    g_launches++;
+    CU(cudaGetLastError());
+    CU(cudaEventRecord(k.done, k.stream));
+    CU(cudaStreamWaitEvent(m->stream, k.done, 0));
+    base += (int)k.items.size();
+    ++qi;
+  }
+  CU(cudaEventRecord(m->ev[3], m->stream));
+  if (tx.p) CU(cudaMemcpyAsync(x_out, dx, sizeof(double) * total, cudaMemcpyDeviceToHost, m->stream));
+  std::vector<int> st(N);
+  CU(cudaMemcpyAsync(st.data(), m->d_status, sizeof(int) * N, cudaMemcpyDeviceToHost, m->stream));
+  CU(cudaEventRecord(m->ev[1], m->stream));
+  CU(cudaStreamSynchronize(m->stream));
+  cudaEventElapsedTime(&m->kernel_ms, m->ev[2], m->ev[3]);
+  cudaEventElapsedTime(&m->call_ms, m->ev[0], m->ev[1]);
+  int any = 0;
+  for (int c = 0; c < N; ++c) {
+    if (circuit_status) circuit_status[c] = map_status(st[c], 0);
+    any |= st[c];
+  }
+  return map_status(any, 0);
+}
+
+krets_status krets_multi_last_timing(const krets_multi *m, float *kernel_ms, float *call_ms) {
+  if (!m) return fail(KRETS_ERR_INVALID_ARGUMENT, "null multi-circuit handle");
+  if (kernel_ms) *kernel_ms = m->kernel_ms;
+  if (call_ms) *call_ms = m->call_ms;
+  return KRETS_OK;
 }
 
 }  // extern "C"

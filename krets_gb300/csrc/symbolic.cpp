@@ -141,9 +141,11 @@ struct GP {
   double min_ratio = 1.0;
 };
 
+constexpr int kFillCapExceeded = -100;  // gp_factor gave up: more L+U entries than the cap
+
 template <typename T>
 int gp_factor(int n, const std::vector<int> &ap, const std::vector<int> &ai, const std::vector<T> &ax,
-              const std::vector<int> &q, double tau, GP &F) {
+              const std::vector<int> &q, double tau, GP &F, size_t fill_cap = 0) {
   F.n = n;
   F.lp.assign(n + 1, 0);
   F.up.assign(n + 1, 0);
@@ -207,6 +209,7 @@ int gp_factor(int n, const std::vector<int> &ap, const std::vector<int> &ai, con
         F.ui.push_back(F.pinv[i]);
       }
     }
+    if (fill_cap && F.li.size() + F.ui.size() > fill_cap) return kFillCapExceeded;
     if (ipiv < 0) return KRETS_ERR_DECOMPOSITION_FAILED;  // structurally singular column
     if (!(amax > 0.0) || !std::isfinite(amax)) return KRETS_ERR_DECOMPOSITION_FAILED;
     // diagonal preference: keep the row paired with this column if it is large enough
@@ -545,7 +548,8 @@ static void pack_transposed_program(Program &P) {
 // ------------------------------------------------------------------ program
 static int build_with_order(const krets_element *el, int ne, int n, int mode, int method, double h, double f,
                             const std::vector<MEntry> &M, const std::vector<BEntry> &B,
-                            const std::vector<int> &q, Program &P, std::string &msg, bool rep_diode_zero) {
+                            const std::vector<int> &q, Program &P, std::string &msg, bool rep_diode_zero,
+                            size_t fill_cap = 0, bool update_list = true) {
   P = Program();
   P.mode = mode;
   P.method = method;
@@ -580,12 +584,13 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
   int st;
   const double tau = 1e-3;  // threshold partial pivoting (diagonal kept when >= tau * column max)
   if (mode == MODE_AC) {
-    st = gp_factor<std::complex<double>>(n, ap, ai, axz, q, tau, F);
+    st = gp_factor<std::complex<double>>(n, ap, ai, axz, q, tau, F, fill_cap);
   } else {
     std::vector<double> axr(axz.size());
     for (size_t k = 0; k < axz.size(); ++k) axr[k] = axz[k].real();
-    st = gp_factor<double>(n, ap, ai, axr, q, tau, F);
+    st = gp_factor<double>(n, ap, ai, axr, q, tau, F, fill_cap);
   }
+  if (st == kFillCapExceeded) return st;
   if (st != KRETS_OK) {
     msg = "matrix is singular for the representative element values (no usable pivot)";
     return st;
@@ -626,7 +631,27 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
   }
   // ---- factorisation program (IKJ)
   P.piv_ptr.assign(n + 1, 0);
-  for (int k = 0; k < n; ++k) {
+  if (!update_list) {
+    // no explicit update list (the device merges each U row into the pattern of row k):
+    // count the work and check that every update lands inside the static pattern
+    for (int k = 0; k < n; ++k) {
+      for (int s = P.lu_rowptr[k]; s < P.lu_diag[k]; ++s) {
+        const int j = P.lu_col[s];
+        int p = s + 1;
+        for (int t = P.lu_diag[j] + 1; t < P.lu_rowptr[j + 1]; ++t) {
+          const int c = P.lu_col[t];
+          while (p < P.lu_rowptr[k + 1] && P.lu_col[p] < c) ++p;
+          if (p >= P.lu_rowptr[k + 1] || P.lu_col[p] != c) {
+            msg = "internal: fill entry missing from static pattern";
+            return KRETS_ERR_UNEXPECTED;
+          }
+          P.factor_flops += 2;
+        }
+        P.factor_flops += 1;
+      }
+    }
+  }
+  for (int k = 0; k < n && update_list; ++k) {
     for (int s = P.lu_rowptr[k]; s < P.lu_diag[k]; ++s) {
       int j = P.lu_col[s];
       int ub = (int)P.upd.size() / 2;
@@ -785,7 +810,7 @@ static double program_cost(const Program &P) {
 }
 
 int build_program(const krets_element *el, int ne, int n, int mode, int method, double h, double f,
-                  int forced_ordering, Program &out, std::string &msg) {
+                  int forced_ordering, Program &out, std::string &msg, bool update_list) {
   if (n <= 0) {
     msg = "circuit has no unknowns";
     return KRETS_ERR_MATRIX_BUILD;
@@ -817,14 +842,21 @@ int build_program(const krets_element *el, int ne, int n, int mode, int method, 
     std::sort(a.begin(), a.end());
     a.erase(std::unique(a.begin(), a.end()), a.end());
   }
+  // minimum degree first: its fill caps the others (an ordering with more than twice its
+  // L+U entries is abandoned during the factorisation; nested dissection by BFS levels
+  // suits ladders and meshes but fills in heavily on random graphs)
   std::vector<int> cands = forced_ordering >= 0 ? std::vector<int>{forced_ordering}
-                                                : std::vector<int>{ORDER_NESTED, ORDER_MINDEG, ORDER_NATURAL};
+                                                : std::vector<int>{ORDER_MINDEG, ORDER_NESTED, ORDER_NATURAL};
+  size_t fill_cap = 0;
   double best_cost = 0;
   int best_st = KRETS_ERR_DECOMPOSITION_FAILED;
   std::string best_msg;
   for (int o : cands) {
     std::vector<int> q;
     if (o == ORDER_NATURAL) {
+      // the natural order is a candidate only for small systems (chains, tests): on a
+      // general graph its fill grows towards n^2
+      if (forced_ordering < 0 && n > 256) continue;
       q.resize(n);
       std::iota(q.begin(), q.end(), 0);
     } else if (o == ORDER_MINDEG) {
@@ -835,14 +867,16 @@ int build_program(const krets_element *el, int ne, int n, int mode, int method, 
     }
     Program P;
     std::string m2;
-    int st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, true);
+    int st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, true, fill_cap, update_list);
     if (st == KRETS_ERR_DECOMPOSITION_FAILED)  // only singular without diode conductances
-      st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, false);
+      st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, false, fill_cap, update_list);
+    if (st == kFillCapExceeded) continue;
     if (st != KRETS_OK) {
       if (best_st != KRETS_OK) { best_st = st; best_msg = m2; }
       continue;
     }
     P.ordering = o;
+    if (!fill_cap) fill_cap = 2 * P.lu_col.size() + (size_t)n;
     double c = program_cost(P);
     if (best_st != KRETS_OK || c < best_cost) {
       best_cost = c;

@@ -81,7 +81,8 @@ struct Program {
 // Build the program for one mode.  h / freq: representative step and frequency used to
 // evaluate values for pivot selection.  Returns KRETS_OK or an error code (msg filled).
 int build_program(const krets_element *el, int ne, int n, int mode, int method, double h, double freq,
-                  int forced_ordering, Program &out, std::string &msg);
+                  int forced_ordering, Program &out, std::string &msg,
+                  bool update_list = true);
 
 // Exposed for tests of the symbolic pass itself.
 std::vector<int> order_min_degree(int n, const std::vector<std::vector<int>> &adj);

@@ -668,6 +668,47 @@ __device__ int g_coef_pass(const DevProg &P, const double *values, double h, int
   return err;
 }
 
+// As g_factor64, without an update list: row k merges each U row j (columns ascending)
+// into its own sorted pattern.  The host checked that every update lands in the pattern;
+// an entry not found (an inconsistent program) stops the row and reports it singular.
+template <int G>
+__device__ int g_factor64_merge(const DevProg &P, double *lu, int gl, int gid) {
+  int bad = 0;
+  for (int l = 0; l < P.nlev; ++l) {
+    const int r0 = P.lev_ptr[l], r1 = P.lev_ptr[l + 1];
+    for (int t = r0 + gl; t < r1; t += G) {
+      const int k = P.ldesc[t].x;
+      const int dk = P.lu_diag[k], re = P.lu_rowptr[k + 1];
+      for (int s = P.lu_rowptr[k]; s < dk; ++s) {
+        const int j = P.lu_col[s];
+        const double l_kj = lu[s] / lu[P.lu_diag[j]];
+        lu[s] = l_kj;
+        int p = s + 1;
+        const int ue = P.lu_rowptr[j + 1];
+        for (int u = P.lu_diag[j] + 1; u < ue; ++u) {
+          const int c = P.lu_col[u];
+          while (p < re && P.lu_col[p] < c) ++p;
+          if (p >= re || P.lu_col[p] != c) {
+            bad |= KS_SINGULAR;
+            break;
+          }
+          lu[p] -= l_kj * lu[u];
+        }
+      }
+      const double d = lu[dk];
+      if (!(fabs(d) > 0)) bad |= KS_SINGULAR;
+      else if (!isfinite(d)) bad |= KS_NONFINITE;
+    }
+    gsync<G>(gid);
+  }
+  for (int k = gl; k < P.n; k += G) {
+    const int sl = P.lu_diag[k];
+    lu[sl] = 1.0 / lu[sl];
+  }
+  gsync<G>(gid);
+  return bad;
+}
+
 template <int G>
 __device__ int g_factor64(const DevProg &P, double *lu, int gl, int gid) {
   int bad = 0;
@@ -833,6 +874,94 @@ struct DfdLay {
   int sprog_bytes;
 };
 
+// Set-up of one instance for the double-float direct engine: FP64 coefficients, LU
+// stamped and factored in FP64 (in lu64), then split to double-float pairs in place (lu);
+// coefficients of the rhs elements (C/h or 2C/h, L/h or 2L/h, source values) to cdyn.
+// coef64 may alias x / cdyn / cb / icap: it is dead once the LU is formed, and the
+// rhs-element coefficients are recomputed with the same expressions as g_coef_pass.
+template <int G, bool MERGE = false>
+__device__ __forceinline__ int dfd_setup(const DevProg &P, const SProg &S, const double *vals, double h, int method,
+                                         df *lu, double *lu64, double *coef64, df *cdyn, int gl, int gid) {
+  int st = g_coef_pass<G>(P, vals, h, method, coef64, gl);
+  gsync<G>(gid);
+  for (int sl = gl; sl < P.nnz_lu; sl += G) {
+    const int t = P.lu_src[sl];
+    lu64[sl] = t < 0 ? 0.0 : sum_entry<double>(P, t, coef64, nullptr);
+  }
+  gsync<G>(gid);
+  st |= MERGE ? g_factor64_merge<G>(P, lu64, gl, gid) : g_factor64<G>(P, lu64, gl, gid);
+  for (int sl = gl; sl < P.nnz_lu; sl += G) lu[sl] = df_from_double(lu64[sl]);
+  for (int d = gl; d < P.ndyn; d += G) {
+    const int e = S.dyn[d].x & 0xffffff;
+    const krets_element &E = P.el[e];
+    const double val = vals ? vals[e] : E.value;
+    double c = val;
+    if (E.kind == KRETS_ELEM_C || E.kind == KRETS_ELEM_L) c = method == KRETS_METHOD_TR ? 2.0 * val / h : val / h;
+    cdyn[d] = df_from_double(c);
+  }
+  return st;
+}
+
+// Transient steps 1..n_steps of one instance from the state in x (position space), rows
+// of `out` (original unknown order, n per row) written with streaming stores.
+template <int G>
+__device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const df *lu, df *x, const df *cdyn, df *cb,
+                                         df *icap, const double *vals, double h, int n_steps, int method, int lag,
+                                         double *out, int lnar, int unar, bool int_cvt, int gl, int gid) {
+  int st = 0;
+  for (int s = 1; s <= n_steps; ++s) {
+    const double t = (double)s * h;
+    const double t_src = lag ? (double)(s - 1) * h : t;
+    for (int d = gl; d < P.ndyn; d += G) {
+      const int4 dd = S.dyn[d];
+      const int kind = (int)((unsigned)dd.x >> 24);
+      df v{0.f, 0.f};
+      if (kind == KRETS_ELEM_C) {
+        const df vprev = df_sub(df_at(x, dd.y), df_at(x, dd.z));
+        v = method == KRETS_METHOD_TR ? df_fma(cdyn[d], vprev, icap[d]) : df_mul(cdyn[d], vprev);
+      } else if (kind == KRETS_ELEM_L) {
+        const df li = df_neg(df_mul(cdyn[d], x[dd.w]));
+        v = method == KRETS_METHOD_TR ? df_sub(li, df_sub(df_at(x, dd.y), df_at(x, dd.z))) : li;
+      } else if (kind == KRETS_ELEM_V) {
+        const int e = dd.x & 0xffffff;
+        const krets_element &E = P.el[e];
+        v = df_from_double(wave_value(E, vals ? vals[e] : E.value, t_src));
+      } else if (kind == KRETS_ELEM_I) {
+        v = cdyn[d];
+      }
+      cb[d] = v;
+    }
+    gsync<G>(gid);  // x (previous solution) fully read: the rhs overwrites it
+    for (int k = gl; k < P.n; k += G) {
+      df acc{0.f, 0.f};
+      for (int u = S.bd_ptr[k]; u < S.bd_ptr[k + 1]; ++u) {
+        const int code = S.bd_op[u];
+        acc = df_add(acc, (code & 1) ? df_neg(cb[code >> 1]) : cb[code >> 1]);
+      }
+      x[k] = acc;
+    }
+    gsync<G>(gid);
+    df_solve<G, false>(S, lu, x, gl, gid, lnar);
+    df_solve<G, true>(S, lu, x, gl, gid, unar);
+    if (method == KRETS_METHOD_TR) {
+      for (int d = gl; d < P.ncap; d += G) {
+        const int4 dd = S.dyn[d];
+        const df vn = df_sub(df_at(x, dd.y), df_at(x, dd.z));
+        icap[d] = df_sub(df_mul(cdyn[d], vn), cb[d]);
+      }
+    }
+    double *row = out + (size_t)s * P.n;
+    for (int k = gl; k < P.n; k += G) {
+      const df xv = x[S.qinv[k]];
+      const double v = int_cvt ? df_to_double_int(xv) : df_to_double(xv);
+      if (!isfinite(v)) st |= KS_NONFINITE;
+      __stcs(row + k, v);
+    }
+    gsync<G>(gid);
+  }
+  return st;
+}
+
 // opts bit 0: run narrow levels on one warp; bit 1: integer-only FP64 output conversion
 template <int G>
 __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay L, const double *values, int n_inst,
@@ -871,79 +1000,12 @@ __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
     if (inst >= n_inst) break;
     const double *vals = values ? values + (size_t)inst * P.ne : nullptr;
     double *out = x_out + (size_t)inst * stride;
-    // set-up: FP64 coefficients, LU stamped and factored in FP64, then split to df
-    int st = g_coef_pass<G>(P, vals, h, method, coef64, gl);
-    gsync<G>(gid);
-    for (int sl = gl; sl < P.nnz_lu; sl += G) {
-      const int t = P.lu_src[sl];
-      lu64[sl] = t < 0 ? 0.0 : sum_entry<double>(P, t, coef64, nullptr);
-    }
-    gsync<G>(gid);
-    st |= g_factor64<G>(P, lu64, gl, gid);
-    for (int sl = gl; sl < P.nnz_lu; sl += G) lu[sl] = df_from_double(lu64[sl]);
-    // coef64 is dead from here on (its bytes alias x / cdyn / cb / icap): the rhs-element
-    // coefficients are recomputed with the same expressions as g_coef_pass
-    for (int d = gl; d < P.ndyn; d += G) {
-      const int e = S.dyn[d].x & 0xffffff;
-      const krets_element &E = P.el[e];
-      const double val = vals ? vals[e] : E.value;
-      double c = val;
-      if (E.kind == KRETS_ELEM_C || E.kind == KRETS_ELEM_L) c = method == KRETS_METHOD_TR ? 2.0 * val / h : val / h;
-      cdyn[d] = df_from_double(c);
-    }
+    int st = dfd_setup<G>(P, S, vals, h, method, lu, lu64, coef64, cdyn, gl, gid);
     for (int k = gl; k < P.n; k += G) x[k] = df_from_double(out[P.q[k]]);
     for (int d = gl; d < P.ncap; d += G) icap[d] = df{0.f, 0.f};
     const bool fatal = gany<G>((st & (KS_SINGULAR | KS_NONFINITE | KS_NOTIMPL)) != 0, gid);
-    for (int s = 1; s <= n_steps && !fatal; ++s) {
-      const double t = (double)s * h;
-      const double t_src = lag ? (double)(s - 1) * h : t;
-      for (int d = gl; d < P.ndyn; d += G) {
-        const int4 dd = S.dyn[d];
-        const int kind = (int)((unsigned)dd.x >> 24);
-        df v{0.f, 0.f};
-        if (kind == KRETS_ELEM_C) {
-          const df vprev = df_sub(df_at(x, dd.y), df_at(x, dd.z));
-          v = method == KRETS_METHOD_TR ? df_fma(cdyn[d], vprev, icap[d]) : df_mul(cdyn[d], vprev);
-        } else if (kind == KRETS_ELEM_L) {
-          const df li = df_neg(df_mul(cdyn[d], x[dd.w]));
-          v = method == KRETS_METHOD_TR ? df_sub(li, df_sub(df_at(x, dd.y), df_at(x, dd.z))) : li;
-        } else if (kind == KRETS_ELEM_V) {
-          const int e = dd.x & 0xffffff;
-          const krets_element &E = P.el[e];
-          v = df_from_double(wave_value(E, vals ? vals[e] : E.value, t_src));
-        } else if (kind == KRETS_ELEM_I) {
-          v = cdyn[d];
-        }
-        cb[d] = v;
-      }
-      gsync<G>(gid);  // x (previous solution) fully read: the rhs overwrites it
-      for (int k = gl; k < P.n; k += G) {
-        df acc{0.f, 0.f};
-        for (int u = S.bd_ptr[k]; u < S.bd_ptr[k + 1]; ++u) {
-          const int code = S.bd_op[u];
-          acc = df_add(acc, (code & 1) ? df_neg(cb[code >> 1]) : cb[code >> 1]);
-        }
-        x[k] = acc;
-      }
-      gsync<G>(gid);
-      df_solve<G, false>(S, lu, x, gl, gid, lnar);
-      df_solve<G, true>(S, lu, x, gl, gid, unar);
-      if (method == KRETS_METHOD_TR) {
-        for (int d = gl; d < P.ncap; d += G) {
-          const int4 dd = S.dyn[d];
-          const df vn = df_sub(df_at(x, dd.y), df_at(x, dd.z));
-          icap[d] = df_sub(df_mul(cdyn[d], vn), cb[d]);
-        }
-      }
-      double *row = out + (size_t)s * P.n;
-      for (int k = gl; k < P.n; k += G) {
-        const df xv = x[S.qinv[k]];
-        const double v = int_cvt ? df_to_double_int(xv) : df_to_double(xv);
-        if (!isfinite(v)) st |= KS_NONFINITE;
-        __stcs(row + k, v);
-      }
-      gsync<G>(gid);
-    }
+    if (!fatal) st |= dfd_steps<G>(P, S, lu, x, cdyn, cb, icap, vals, h, n_steps, method, lag, out, lnar, unar, int_cvt,
+                                   gl, gid);
     if (gl == 0) slot[1] = 0;
     gsync<G>(gid);
     if (st) atomicOr(&slot[1], st);

@@ -127,3 +127,134 @@ def rc_ladder_step(sections: int = 1000, seed: int = 5) -> Circuit:
         lines.append(f"C{k} n{k} 0 {float(c[k - 1])!r}")
         prev = f"n{k}"
     return parse_circuit_description("\n".join(lines) + "\n")
+
+
+# ---------------------------------------------------------------- uneven batch
+UNEVEN_NODES = (10, 5000)
+
+
+def _uneven_elements(index: int, seed: int = 4):
+    """Element list [(letter, name, a, b, value, wave_params)] of uneven netlist `index`.
+
+    Nodes N log-uniform in [10, 5000].  A random recursive spanning tree of resistors
+    (node k attaches to a uniform earlier node, 0 = ground) plus N/2 extra random edges, so
+    the mean degree is 3.  Tree edges are resistors; extra edges are R 10%, C 60%, L 30%, so
+    that all edges together are 70% R, 20% C, 10% L.  Values: R log-U 1 Ohm-1 MOhm, C log-U
+    1 fF-1 nF, L log-U 1 nH-1 uH.  1-4 voltage sources from distinct nodes to ground (DC in
+    [-5, 5] V, or a pulse to that level, half of them), 1-4 current sources node to ground,
+    DC in [-1, 1] mA.  An inductor or voltage source that would close a loop made only of
+    inductors and voltage sources (a singular DC system) becomes a resistor.
+    """
+    base = seed * 1000003 + index * 7919
+    u = uniform(base, 8)
+    N = int(np.floor(np.exp(np.log(UNEVEN_NODES[0]) + u[0] * (np.log(UNEVEN_NODES[1] + 1) - np.log(UNEVEN_NODES[0])))))
+    N = max(UNEVEN_NODES[0], min(UNEVEN_NODES[1], N))
+    n_extra = N // 2
+    n_v = 1 + int(u[1] * 4)
+    n_i = 1 + int(u[2] * 4)
+    r = uniform(base + 1, 4 * N + 8 * n_extra + 64)
+    parent = np.floor(r[:N] * np.arange(1, N + 1)).astype(np.int64)   # in [0, k-1] for node k (1-based)
+    ea = np.floor(r[N:N + n_extra] * (N + 1)).astype(np.int64)
+    eb = np.floor(r[N + n_extra:N + 2 * n_extra] * (N + 1)).astype(np.int64)
+    et = r[N + 2 * n_extra:N + 3 * n_extra]
+    lv = r[N + 3 * n_extra:N + 4 * n_extra]
+    tv = r[N + 4 * n_extra:2 * N + 4 * n_extra]
+    src = r[2 * N + 4 * n_extra:]
+    # union-find over the inductor / voltage-source graph (0 = ground)
+    uf = list(range(N + 1))
+
+    def find(a):
+        while uf[a] != a:
+            uf[a] = uf[uf[a]]
+            a = uf[a]
+        return a
+
+    def nm(k):
+        return "0" if k == 0 else f"n{k}"
+
+    els = []
+    vnodes = []
+    for k in range(n_v):
+        node = 1 + int(src[4 * k] * N)
+        if node in vnodes or find(node) == find(0):
+            continue
+        vnodes.append(node)
+        uf[find(node)] = find(0)
+        level = float(-5.0 + 10.0 * src[4 * k + 1])
+        if src[4 * k + 2] < 0.5:
+            els.append(("V", str(k + 1), nm(node), "0", level, None))
+        else:
+            els.append(("V", str(k + 1), nm(node), "0", 0.0, [0.0, level, 1e-9 * (1 + int(src[4 * k + 3] * 100)),
+                                                              1e-10, 1e-10, 5e-7, 1e-6]))
+    for k in range(n_i):
+        node = 1 + int(src[16 + 2 * k] * N)
+        els.append(("I", str(k + 1), nm(node), "0", float(-1e-3 + 2e-3 * src[17 + 2 * k]), None))
+    for k in range(1, N + 1):
+        els.append(("R", f"t{k}", nm(k), nm(int(parent[k - 1])), float(np.exp(np.log(1.0) + tv[k - 1] * np.log(1e6))), None))
+    for j in range(n_extra):
+        a, b = int(ea[j]), int(eb[j])
+        if a == b:
+            b = (a + 1) % (N + 1)
+        t = et[j]
+        if t < 0.1:
+            kind = "R"
+        elif t < 0.7:
+            kind = "C"
+        else:
+            kind = "L"
+        if kind == "L":
+            fa, fb = find(a), find(b)
+            if fa == fb:
+                kind = "R"
+            else:
+                uf[fa] = fb
+        lo, hi = {"R": (1.0, 1e6), "C": (1e-15, 1e-9), "L": (1e-9, 1e-6)}[kind]
+        val = float(np.exp(np.log(lo) + lv[j] * (np.log(hi) - np.log(lo))))
+        els.append((kind, f"x{j}", nm(a), nm(b), val, None))
+    return els, N
+
+
+def uneven_netlist(index: int, seed: int = 4) -> str:
+    """SPICE text of uneven netlist `index` (see _uneven_elements)."""
+    els, _ = _uneven_elements(index, seed)
+    lines = [f"* uneven netlist {index}"]
+    for letter, name, a, b, v, w in els:
+        if letter == "V":
+            if w is None:
+                lines.append(f"V{name} {a} {b} dc {v!r}")
+            else:
+                lines.append(f"V{name} {a} {b} dc 0 PULSE({' '.join(repr(float(x)) for x in w)})")
+        else:
+            lines.append(f"{letter}{name} {a} {b} {v!r}")
+    return "\n".join(lines) + "\n"
+
+
+def uneven_table(index: int, seed: int = 4):
+    """(element table, n) of uneven netlist `index`, built without text parsing; the MNA
+    numbering follows the parser's rule (branch unknowns of V/L/I in element order, each
+    first-seen non-ground node after them)."""
+    from .table import ELEM_DTYPE
+    els, _ = _uneven_elements(index, seed)
+    kinds = {"R": 1, "C": 2, "L": 3, "V": 4, "I": 5}
+    t = np.zeros(len(els), dtype=ELEM_DTYPE)
+    idx = {}
+    counter = 0
+    for k, (letter, name, a, b, v, w) in enumerate(els):
+        rec = t[k]
+        rec["kind"] = kinds[letter]
+        rec["g"] = -1
+        rec["b"] = -1
+        if letter in "VLI":
+            rec["b"] = counter
+            counter += 1
+        for nd in (a, b):
+            if nd != "0" and nd not in idx:
+                idx[nd] = counter
+                counter += 1
+        rec["p"] = idx.get(a, -1)
+        rec["m"] = idx.get(b, -1)
+        rec["value"] = v
+        if w is not None:
+            rec["wave"] = 1
+            rec["wp"][:7] = w
+    return t, counter

@@ -1,0 +1,72 @@
+"""Multi-circuit engine: many distinct netlists (uneven sizes) in one launch set, each
+checked against the oracle's operating point + backward-Euler transient (reference source
+timing, transient.rs:14-114)."""
+import numpy as np
+import pytest
+
+from krets_gb300 import _lib
+from krets_gb300.generators import uneven_netlist, uneven_table
+from krets_gb300.netlist import parse_circuit_description
+from krets_gb300.table import element_table
+
+TOL = 1e-9
+
+
+def _cur_mask(t, n):
+    m = np.zeros(n, dtype=bool)
+    b = t["b"][t["b"] >= 0]
+    m[b] = True
+    return m
+
+
+def _rel_err(x, ref, mask):
+    worst = 0.0
+    for m in (mask, ~mask):
+        if m.any():
+            r = np.abs(ref[..., m]).max()
+            d = np.abs(x[..., m] - ref[..., m]).max()
+            worst = max(worst, d / r if r > 0 else d)
+    return worst
+
+
+@pytest.mark.parametrize("index", [0, 1, 7, 12])
+def test_uneven_table_matches_parsed_netlist(index):
+    t, n = uneven_table(index)
+    c = parse_circuit_description(uneven_netlist(index))
+    assert c.size == n
+    assert np.array_equal(t.view(np.uint8), element_table(c).view(np.uint8))
+
+
+def test_uneven_netlists_have_regular_dc_systems(oracle_lib):
+    for i in range(6):
+        t, n = uneven_table(i)
+        x = oracle_lib.op(t, n)
+        assert np.all(np.isfinite(x))
+
+
+@pytest.mark.gpu
+def test_multi_circuit_transient_matches_oracle(oracle_lib):
+    idx = [i for i in range(40) if uneven_table(i)[1] <= 2600][:20]
+    tabs = [uneven_table(i) for i in idx]
+    m = _lib.MultiCircuit([t for t, _ in tabs], [n for _, n in tabs], method="be", h=1e-9)
+    info = m.info()
+    assert info[0] == len(idx) and (info[4:10] > 0).sum() >= 3    # several size classes used
+    steps = 200
+    flat, st = m.tran(steps)
+    assert np.all(st == 0)
+    for (t, n), x in zip(tabs, m.split(flat, steps)):
+        ref = oracle_lib.tran(t, n, 1e-9, steps, method="be", lag=True)
+        assert _rel_err(x, ref, _cur_mask(t, n)) < TOL, n
+
+
+@pytest.mark.gpu
+def test_multi_circuit_output_offsets_and_device_buffers():
+    tabs = [uneven_table(i) for i in (3, 7, 9)]
+    m = _lib.MultiCircuit([t for t, _ in tabs], [n for _, n in tabs], method="be", h=1e-9)
+    steps = 50
+    host, _ = m.tran(steps)
+    dev = _lib.DeviceArray(m.total(steps))
+    m.tran(steps, out=dev)
+    assert np.array_equal(dev.download(), host)
+    host2, _ = m.tran(steps)
+    assert np.array_equal(host, host2)                                   # deterministic
