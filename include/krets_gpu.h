@@ -182,7 +182,9 @@ krets_status krets_multi_create(int32_t n_circuits, const krets_element *elems, 
                                 const int32_t *n_unknowns, int32_t method, double h, krets_multi **out);
 krets_status krets_multi_destroy(krets_multi *m);
 /* info[0..3] = circuits, sum of n, sum of transient LU entries, sum of transient solve levels;
- * info[4..] = circuits per size class (shared-memory regions from small to large, then global). */
+ * info[4..9] = circuits per size class (shared-memory regions from small to large, then
+ * global); info[10..15] = microseconds from the start of the last krets_multi_tran launch set
+ * to the end of each class. */
 krets_status krets_multi_info(const krets_multi *m, int64_t *info, int32_t cap);
 /* Operating point then n_steps transient steps of every circuit (transient.rs:14-114 per
  * circuit).  Circuit c writes (n_steps+1) x n_c doubles (row 0 = operating point, original
@@ -273,14 +275,18 @@ krets_status krets_batch_tran_noalloc(krets_circuit *c, int32_t n_inst, const do
 #define KRETS_PROG_ULEV_PTR 17
 #define KRETS_PROG_ULEV_ROWS 18
 #define KRETS_PROG_EL_POS 19
-#define KRETS_PROG_META 20 /* {ordering, n, nnz_a, nnz_lu, n_levels, n_ulevels, factor_flops} */
+#define KRETS_PROG_META 20 /* {ordering, n, nnz_a, nnz_lu, n_levels, n_ulevels, factor_flops, tail0, tail_m} */
 #define KRETS_PROG_TPROG 21 /* transposed-solve program (transient mode) */
 #define KRETS_PROG_TPOFF 22 /* its section offsets (6) and level counts of U^T and L^T */
 #define KRETS_MODE_DC 0
 #define KRETS_MODE_AC 1
 #define KRETS_MODE_TRAN 2
+/* ordering: -1 = autotune, else a fixed ORDER; ORDER | KRETS_PROG_MULTI builds the program
+ * the multi-circuit engine uses (dense trailing block, no factorisation update list), with
+ * 0xff | KRETS_PROG_MULTI for autotune. */
+#define KRETS_PROG_MULTI 0x100
 krets_status krets_symbolic_export(const krets_element *elems, int32_t n_elem, int32_t n_unknowns, int32_t mode,
-                                   int32_t method, double h, double freq, int32_t ordering /* -1 = autotune */,
+                                   int32_t method, double h, double freq, int32_t ordering,
                                    int32_t which, int64_t *out, int64_t cap, int64_t *len);
 
 #ifdef __cplusplus

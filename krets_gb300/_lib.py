@@ -197,7 +197,7 @@ class MultiCircuit:
         return [flat[o:o + (n_steps + 1) * n].reshape(n_steps + 1, n) for o, n in zip(off, self.sizes)]
 
     def info(self):
-        v = np.zeros(12, dtype=np.int64)
+        v = np.zeros(16, dtype=np.int64)
         check(lib().krets_multi_info(self.h, ptr(v), len(v)), "multi_info")
         return v
 

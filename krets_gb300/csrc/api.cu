@@ -234,6 +234,8 @@ static void place_program(const Program &H, const ProgramImage &X, const krets_e
   for (int k = 0; k < 8; ++k) V.tp_off[k] = H.tp_off[k];
   V.n_utlev = H.n_utlev;
   V.n_ltlev = H.n_ltlev;
+  V.tail0 = H.tail0;
+  V.tail_m = H.tail_m;
   bool nl = false;
   for (int e = 0; e < H.ne; ++e) {
     int k = el_host[e].kind;
@@ -461,6 +463,9 @@ struct MultiClass {
   long long region = 0;      // bytes per group
   std::vector<int> items;    // circuits, largest first
   int grid = 0;
+  long long gsm = 0;         // global class: shared memory per group
+  bool x_smem = false;       // global class: solution and rhs coefficients in shared memory
+  float ms = 0.f;            // last run: launch set start to this class's end
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
 };
@@ -1355,7 +1360,7 @@ krets_status krets_multi_create(int32_t n_circuits, const krets_element *elems, 
         for (int j; (j = next.fetch_add(1)) < 2 * N;) {
           const int c = j / 2, mode = (j & 1) ? MODE_TRAN : MODE_DC;
           pst[j] = build_program(elems + m->el_off[c], m->ne[c], m->n[c], mode, method, h, 0.0, -1, progs[j], pmsg[j],
-                                 false);
+                                 false, true);
         }
       });
     for (auto &t : th) t.join();
@@ -1445,10 +1450,22 @@ krets_status krets_multi_create(int32_t n_circuits, const krets_element *elems, 
   for (auto &k : m->classes) {
     if (k.items.empty()) continue;
     CU(cudaStreamCreateWithFlags(&k.stream, cudaStreamNonBlocking));
-    CU(cudaEventCreateWithFlags(&k.done, cudaEventDisableTiming));
+    CU(cudaEventCreate(&k.done));
     const int per_sm = k.global ? 2 : 1;
     k.grid = std::max(1, std::min(((int)k.items.size() + k.W - 1) / k.W, per_sm * device_sm_count()));
-    if (k.global) gscratch_bytes = k.region * k.grid * k.W;
+    if (k.global) {
+      gscratch_bytes = k.region * k.grid * k.W;
+      // shared memory of a global-class group: staging tile, then x and the rhs
+      // coefficients when the largest circuit's fit in half an SM's shared memory
+      long long xb = 0;
+      for (int c : k.items)
+        for (int ph = 0; ph < 2; ++ph) {
+          const DevProg &V = views[2 * c + ph];
+          xb = std::max<long long>(xb, mlay_al16(8ll * V.n) + mlay_al16(8ll * V.ndyn));
+        }
+      k.x_smem = kStageBytes + xb <= smax / 2;
+      k.gsm = kStageBytes + (k.x_smem ? xb : 0);
+    }
     all_items.insert(all_items.end(), k.items.begin(), k.items.end());
   }
   CU(cudaMalloc(&m->d_items, sizeof(int) * all_items.size()));
@@ -1476,6 +1493,7 @@ krets_status krets_multi_info(const krets_multi *m, int64_t *info, int32_t cap) 
   }
   std::vector<long long> v{m->n_circ, sn, snnz, slev};
   for (auto &k : m->classes) v.push_back((long long)k.items.size());
+  for (auto &k : m->classes) v.push_back((long long)(1000.0 * k.ms));
   for (int i = 0; i < cap && i < (int)v.size(); ++i) info[i] = v[i];
   return KRETS_OK;
 }
@@ -1505,17 +1523,17 @@ krets_status krets_multi_tran(krets_multi *m, int32_t n_steps, int32_t source_la
     if (k.items.empty()) continue;
     CU(cudaStreamWaitEvent(k.stream, m->ev[2], 0));
     const int threads = k.G * k.W;
-    const size_t smem = k.global ? 0 : (size_t)(k.region * k.W);
-    void (*kern)(const DevProg *, const int *, int, const long long *, long long, char *, double, int, int, int,
-                 double *, int *, int *) = nullptr;
+    const size_t smem = k.global ? (size_t)k.gsm * k.W : (size_t)(k.region * k.W);
+    void (*kern)(const DevProg *, const int *, int, const long long *, long long, char *, int, int, double, int, int,
+                 int, double *, int *, int *) = nullptr;
     if (k.global) kern = k_multi_tran<256, true>;
     else if (k.G == 32) kern = k_multi_tran<32, false>;
     else if (k.G == 64) kern = k_multi_tran<64, false>;
     else kern = k_multi_tran<128, false>;
-    if (!k.global) CU(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CU(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<k.grid, threads, smem, k.stream>>>(m->d_views, m->d_items + base, (int)k.items.size(), m->d_xoff, k.region,
-                                             m->gscratch, m->h, n_steps, m->method, source_lag, (double *)dx,
-                                             m->d_status, m->d_queue + qi);
+                                             m->gscratch, (int)k.gsm, k.x_smem ? 1 : 0, m->h, n_steps, m->method,
+                                             source_lag, (double *)dx, m->d_status, m->d_queue + qi);
     g_launches++;
     CU(cudaGetLastError());
     CU(cudaEventRecord(k.done, k.stream));
@@ -1531,6 +1549,8 @@ krets_status krets_multi_tran(krets_multi *m, int32_t n_steps, int32_t source_la
   CU(cudaStreamSynchronize(m->stream));
   cudaEventElapsedTime(&m->kernel_ms, m->ev[2], m->ev[3]);
   cudaEventElapsedTime(&m->call_ms, m->ev[0], m->ev[1]);
+  for (auto &k : m->classes)
+    if (!k.items.empty()) cudaEventElapsedTime(&k.ms, m->ev[2], k.done);
   int any = 0;
   for (int c = 0; c < N; ++c) {
     if (circuit_status) circuit_status[c] = map_status(st[c], 0);

@@ -109,6 +109,7 @@ struct DevProg {
   int tp_off[8];
   int n_utlev, n_ltlev;
   const int *prow;  // [n] position -> pivot row (unknown index of the row)
+  int tail0, tail_m;  // dense trailing block of the LU (tail_m = 0: none)
 };
 
 // status bits written by the engine

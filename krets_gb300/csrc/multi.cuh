@@ -45,16 +45,24 @@ __host__ __device__ inline MLay multi_lay(int nnz_lu, int n, int ndyn, int ncap,
   return L;
 }
 
+// GLOBAL: shared memory per group = a 32 x 33 staging tile for the diagonal blocks of the
+// dense trailing block, then (x_smem) the solution and rhs-coefficient vectors, whose
+// gathers are the latency-critical accesses; the LU and the step program stay in global
+// memory.
+constexpr int kStageBytes = 32 * 33 * 8;
+
 template <int G, bool GLOBAL>
 __global__ void __launch_bounds__(512, 1)
     k_multi_tran(const DevProg *__restrict__ progs, const int *__restrict__ items, int n_items,
-                 const long long *__restrict__ x_off, long long region_bytes, char *gscratch, double h, int n_steps,
-                 int method, int lag, double *x_out, int *circ_status, int *queue) {
+                 const long long *__restrict__ x_off, long long region_bytes, char *gscratch, int gsm_bytes,
+                 int x_smem, double h, int n_steps, int method, int lag, double *x_out, int *circ_status,
+                 int *queue) {
   extern __shared__ __align__(16) char smem[];
   const int gl = threadIdx.x % G, gid = threadIdx.x / G;
   const int W = blockDim.x / G;
   char *region = GLOBAL ? gscratch + ((long long)blockIdx.x * W + gid) * region_bytes
                         : smem + (long long)gid * region_bytes;
+  char *gsm = smem + (long long)gid * gsm_bytes;  // GLOBAL only
   int *slot = reinterpret_cast<int *>(region);
   while (true) {
     if (gl == 0) slot[0] = atomicAdd(queue, 1);
@@ -75,12 +83,14 @@ __global__ void __launch_bounds__(512, 1)
         for (int i = gl; i < spw / 4; i += G) dst[i] = src[i];
         gsync<G>(gid);
       }
-      const SProg S = sprog_view(P, GLOBAL ? P.sprog : reinterpret_cast<const int *>(region + L.sp));
+      SProg S = sprog_view(P, GLOBAL ? P.sprog : reinterpret_cast<const int *>(region + L.sp));
+      if (GLOBAL) S.dense_stage = reinterpret_cast<df *>(gsm);
+      const bool xs = GLOBAL && x_smem;
       df *lu = reinterpret_cast<df *>(region + L.lu);
       double *lu64 = reinterpret_cast<double *>(region + L.lu);
-      df *x = reinterpret_cast<df *>(region + L.x);
+      df *x = reinterpret_cast<df *>(xs ? gsm + kStageBytes : region + L.x);
       df *cdyn = reinterpret_cast<df *>(region + L.cdyn);
-      df *cb = reinterpret_cast<df *>(region + L.cb);
+      df *cb = reinterpret_cast<df *>(xs ? gsm + kStageBytes + mlay_al16(8ll * P.n) : region + L.cb);
       df *icap = reinterpret_cast<df *>(region + L.icap);
       double *coef64 = reinterpret_cast<double *>(region + L.coef64);
       st |= dfd_setup<G, true>(P, S, nullptr, h, method, lu, lu64, coef64, cdyn, gl, gid);

@@ -141,7 +141,8 @@ struct GP {
   double min_ratio = 1.0;
 };
 
-constexpr int kFillCapExceeded = -100;  // gp_factor gave up: more L+U entries than the cap
+constexpr int kFillCapExceeded = -100;
+constexpr int kMinDenseTail = 64;  // smallest dense trailing block solved as a dense block  // gp_factor gave up: more L+U entries than the cap
 
 template <typename T>
 int gp_factor(int n, const std::vector<int> &ap, const std::vector<int> &ai, const std::vector<T> &ax,
@@ -406,13 +407,18 @@ static void pack_step_program(const krets_element *el, Program &P) {
   S.insert(S.end(), P.lev_ptr.begin(), P.lev_ptr.end());
   mark(1);
   S.insert(S.end(), P.ulev_ptr.begin(), P.ulev_ptr.end());
+  // L entries a row's descriptor covers: the whole L part, or for a row of the dense
+  // trailing block only its columns before the block
+  auto lcount = [&](int k) {
+    return (P.tail_m && k >= P.tail0) ? P.lu_rowptr[k + 1] - P.tail_m - P.lu_rowptr[k] : P.lu_diag[k] - P.lu_rowptr[k];
+  };
   mark(2);
-  for (int t = 0; t < n; ++t) {
+  for (size_t t = 0; t < P.lev_rows.size(); ++t) {
     int k = P.lev_rows[t];
-    desc(k, P.lu_rowptr[k], P.lu_diag[k] - P.lu_rowptr[k], P.lu_rowptr[k]);
+    desc(k, P.lu_rowptr[k], lcount(k), P.lu_rowptr[k]);
   }
   mark(3);
-  for (int t = 0; t < n; ++t) {
+  for (size_t t = 0; t < P.ulev_rows.size(); ++t) {
     int k = P.ulev_rows[t];
     desc(k, P.lu_diag[k] + 1, P.lu_rowptr[k + 1] - P.lu_diag[k] - 1, P.lu_diag[k]);
   }
@@ -440,7 +446,7 @@ static void pack_step_program(const krets_element *el, Program &P) {
     int mx = 0;
     for (int t = P.lev_ptr[l]; t < P.lev_ptr[l + 1]; ++t) {
       const int k = P.lev_rows[t];
-      mx = std::max(mx, P.lu_diag[k] - P.lu_rowptr[k]);
+      mx = std::max(mx, lcount(k));
     }
     S.push_back(mx);
   }
@@ -549,7 +555,7 @@ static void pack_transposed_program(Program &P) {
 static int build_with_order(const krets_element *el, int ne, int n, int mode, int method, double h, double f,
                             const std::vector<MEntry> &M, const std::vector<BEntry> &B,
                             const std::vector<int> &q, Program &P, std::string &msg, bool rep_diode_zero,
-                            size_t fill_cap = 0, bool update_list = true) {
+                            size_t fill_cap = 0, bool update_list = true, bool dense_tail = false) {
   P = Program();
   P.mode = mode;
   P.method = method;
@@ -671,16 +677,42 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
     }
     P.piv_ptr[k + 1] = (int)P.piv.size() / 4;
   }
-  // ---- level schedules
+  // ---- dense trailing block: the largest m whose trailing m x m block is fully dense
+  // (row k holds every column from cstart[k] to n-1; a trailing block is dense when each
+  // of its rows starts its run at or before the block start, and density of a block
+  // implies density of every smaller trailing block)
+  if (dense_tail && n > 0) {
+    int t0 = n, runmax = 0;
+    for (int k = n - 1; k >= 0; --k) {
+      int expect = n - 1, s = P.lu_rowptr[k + 1] - 1;
+      while (s >= P.lu_rowptr[k] && P.lu_col[s] == expect) { --s; --expect; }
+      runmax = std::max(runmax, expect + 1);
+      if (runmax > k) break;
+      t0 = k;
+    }
+    if (n - t0 >= kMinDenseTail) {
+      P.tail0 = t0;
+      P.tail_m = n - t0;
+    }
+  }
+  const int tail0 = P.tail_m ? P.tail0 : n;
+  // ---- level schedules (rows of the dense block: one last L level of their sparse
+  // parts; no U level)
   std::vector<int> lev(n, 0), ulev(n, 0);
   int nl = 0, nu = 0;
-  for (int k = 0; k < n; ++k) {
+  for (int k = 0; k < tail0; ++k) {
     int l = 0;
     for (int s = P.lu_rowptr[k]; s < P.lu_diag[k]; ++s) l = std::max(l, lev[P.lu_col[s]] + 1);
     lev[k] = l;
     nl = std::max(nl, l + 1);
   }
+  for (int k = tail0; k < n; ++k) lev[k] = nl;
+  if (tail0 < n) ++nl;
   for (int k = n - 1; k >= 0; --k) {
+    if (k >= tail0) {
+      ulev[k] = -1;
+      continue;
+    }
     int l = 0;
     for (int s = P.lu_diag[k] + 1; s < P.lu_rowptr[k + 1]; ++s) l = std::max(l, ulev[P.lu_col[s]] + 1);
     ulev[k] = l;
@@ -688,11 +720,14 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
   }
   auto bucket = [&](const std::vector<int> &lv, int nlev, std::vector<int> &ptr, std::vector<int> &rws) {
     ptr.assign(nlev + 1, 0);
-    for (int k = 0; k < n; ++k) ptr[lv[k] + 1]++;
+    int cnt = 0;
+    for (int k = 0; k < n; ++k)
+      if (lv[k] >= 0) { ptr[lv[k] + 1]++; ++cnt; }
     for (int l = 0; l < nlev; ++l) ptr[l + 1] += ptr[l];
-    rws.assign(n, 0);
+    rws.assign(cnt, 0);
     std::vector<int> fill(ptr.begin(), ptr.end() - 1);
-    for (int k = 0; k < n; ++k) rws[fill[lv[k]]++] = k;
+    for (int k = 0; k < n; ++k)
+      if (lv[k] >= 0) rws[fill[lv[k]]++] = k;
   };
   if (n == 0) { nl = nu = 0; }
   bucket(lev, nl, P.lev_ptr, P.lev_rows);
@@ -734,11 +769,11 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
     for (int t = 0; t < 4; ++t) P.el_pos[4 * e + t] = idx[t] >= 0 ? P.qinv[idx[t]] : -1;
   }
   // ---- step program
-  for (int t = 0; t < n; ++t) {
+  for (size_t t = 0; t < P.lev_rows.size(); ++t) {
     int k = P.lev_rows[t];
     P.ldesc.insert(P.ldesc.end(), {k, P.lu_rowptr[k], P.lu_diag[k], P.lu_rowptr[k + 1]});
   }
-  for (int t = 0; t < n; ++t) {
+  for (size_t t = 0; t < P.ulev_rows.size(); ++t) {
     int k = P.ulev_rows[t];
     P.udesc.insert(P.udesc.end(), {k, P.lu_rowptr[k], P.lu_diag[k], P.lu_rowptr[k + 1]});
   }
@@ -774,7 +809,7 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
     P.bd_ptr[r + 1] = (int)P.bd_op.size();
   }
   pack_step_program(el, P);
-  if (mode == MODE_TRAN) pack_transposed_program(P);
+  if (mode == MODE_TRAN && !P.tail_m) pack_transposed_program(P);
   uint64_t sig = 1469598103934665603ull;
   sig = fnv1a(sig, (uint64_t)mode);
   sig = fnv1a(sig, (uint64_t)n);
@@ -796,7 +831,9 @@ static double program_cost(const Program &P) {
       int mx = 0;
       for (int t = ptr[l]; t < ptr[l + 1]; ++t) {
         int k = rws[t];
-        int len = lower ? P.lu_diag[k] - P.lu_rowptr[k] : P.lu_rowptr[k + 1] - P.lu_diag[k];
+        int len = lower ? ((P.tail_m && k >= P.tail0) ? P.lu_rowptr[k + 1] - P.tail_m - P.lu_rowptr[k]
+                                                      : P.lu_diag[k] - P.lu_rowptr[k])
+                        : P.lu_rowptr[k + 1] - P.lu_diag[k];
         mx = std::max(mx, len);
       }
       c += ((cnt + T - 1) / T) * (2.0 * mx + 4.0) + sync;
@@ -804,13 +841,17 @@ static double program_cost(const Program &P) {
   };
   levels(P.lev_ptr, P.lev_rows, true);
   levels(P.ulev_ptr, P.ulev_rows, false);
+  if (P.tail_m) {  // blocked dense solves of the trailing block (forward and backward)
+    const double m = P.tail_m, blocks = std::ceil(m / 32.0);
+    c += 2.0 * blocks * (2.0 * sync + 32.0 * 4.0 + (m / 2.0) * 32.0 * 2.0 / T);
+  }
   c *= 3.0;  // solves dominate (several per step) relative to one factorisation
   c += (double)P.factor_flops / T;
   return c;
 }
 
 int build_program(const krets_element *el, int ne, int n, int mode, int method, double h, double f,
-                  int forced_ordering, Program &out, std::string &msg, bool update_list) {
+                  int forced_ordering, Program &out, std::string &msg, bool update_list, bool dense_tail) {
   if (n <= 0) {
     msg = "circuit has no unknowns";
     return KRETS_ERR_MATRIX_BUILD;
@@ -867,9 +908,11 @@ int build_program(const krets_element *el, int ne, int n, int mode, int method, 
     }
     Program P;
     std::string m2;
-    int st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, true, fill_cap, update_list);
+    int st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, true, fill_cap, update_list,
+                              dense_tail);
     if (st == KRETS_ERR_DECOMPOSITION_FAILED)  // only singular without diode conductances
-      st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, false, fill_cap, update_list);
+      st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, false, fill_cap, update_list,
+                            dense_tail);
     if (st == kFillCapExceeded) continue;
     if (st != KRETS_OK) {
       if (best_st != KRETS_OK) { best_st = st; best_msg = m2; }
@@ -899,10 +942,14 @@ extern "C" krets_status krets_symbolic_export(const krets_element *elems, int32_
   if (!elems || n_elem < 0 || n_unknowns <= 0 || !len) return KRETS_ERR_INVALID_ARGUMENT;
   Program P;
   std::string msg;
-  int st = build_program(elems, n_elem, n_unknowns, mode, method, h, freq, ordering, P, msg);
+  const bool multi = ordering >= 0 && (ordering & KRETS_PROG_MULTI);
+  if (multi) ordering &= ~KRETS_PROG_MULTI;
+  if (ordering == 0xff) ordering = -1;
+  int st = build_program(elems, n_elem, n_unknowns, mode, method, h, freq, ordering, P, msg, !multi, multi);
   if (st != KRETS_OK) return st;
   std::vector<long long> meta{P.ordering, P.n, (long long)P.a_col.size(), (long long)P.lu_col.size(),
-                              (long long)P.lev_ptr.size() - 1, (long long)P.ulev_ptr.size() - 1, P.factor_flops};
+                              (long long)P.lev_ptr.size() - 1, (long long)P.ulev_ptr.size() - 1, P.factor_flops,
+                              P.tail0, P.tail_m};
   const std::vector<int> *arrs[] = {&P.q, &P.prow, &P.lu_rowptr, &P.lu_col, &P.lu_diag, &P.a_rowptr, &P.a_col,
                                     &P.a_slot, &P.a_cptr, &P.a_contrib, &P.b_cptr, &P.b_contrib, &P.piv_ptr,
                                     &P.piv, &P.upd, &P.lev_ptr, &P.lev_rows, &P.ulev_ptr, &P.ulev_rows,

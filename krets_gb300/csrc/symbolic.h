@@ -71,7 +71,12 @@ struct Program {
   std::vector<int> tprog;
   int tp_off[8] = {0};
   int n_utlev = 0, n_ltlev = 0;
-  // per element: 1 when it is a capacitor whose TR history current is state
+  // dense trailing block (multi-circuit programs only): positions tail0 .. n-1 form a
+  // fully dense m x m block of the LU (m = tail_m, 0 = none).  Its rows sit in the last L
+  // level with descriptors covering only their columns < tail0; the U levels hold rows
+  // < tail0 only.  Row k of the block keeps its dense part at slots
+  // lu_rowptr[k+1] - m .. lu_rowptr[k+1] - 1 (columns tail0 .. n-1).
+  int tail0 = 0, tail_m = 0;
   long long factor_flops = 0;
   int max_row_lu = 0;
   uint64_t signature = 0;
@@ -82,7 +87,7 @@ struct Program {
 // evaluate values for pivot selection.  Returns KRETS_OK or an error code (msg filled).
 int build_program(const krets_element *el, int ne, int n, int mode, int method, double h, double freq,
                   int forced_ordering, Program &out, std::string &msg,
-                  bool update_list = true);
+                  bool update_list = true, bool dense_tail = false);
 
 // Exposed for tests of the symbolic pass itself.
 std::vector<int> order_min_degree(int n, const std::vector<std::vector<int>> &adj);

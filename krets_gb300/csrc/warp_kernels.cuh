@@ -20,6 +20,7 @@
 #pragma once
 
 #include "kernels.cuh"
+#include "df.cuh"
 
 namespace krets {
 
@@ -41,6 +42,8 @@ struct SProg {
   const int *bd_ptr, *bd_op, *qinv;
   const int *lmax, *umax;  // longest row of each L / U level
   int nlev, nulev;
+  int tail0, tail_m;  // dense trailing block (tail_m = 0: none)
+  df *dense_stage;    // 32 x 33 shared-memory tile for diagonal blocks read from global memory (or null)
 };
 
 __device__ __forceinline__ SProg sprog_view(const DevProg &P, const int *sp) {
@@ -60,6 +63,9 @@ __device__ __forceinline__ SProg sprog_view(const DevProg &P, const int *sp) {
   S.umax = sp + P.sp_off[13];
   S.nlev = P.nlev;
   S.nulev = P.nulev;
+  S.tail0 = P.tail0;
+  S.tail_m = P.tail_m;
+  S.dense_stage = nullptr;
   return S;
 }
 
@@ -456,7 +462,6 @@ __global__ void __launch_bounds__(256, 1) k_tran_warp(DevProg P, KCfg cfg, WarpL
 // right-hand side, companion state and solution held in double-float (df.cuh) so the inner
 // loop runs on FP32 pipes.  FP64 is used at set-up (coefficients, LU values before rounding
 // to FP32), for source waveforms, and to write each solution row as FP64.
-#include "df.cuh"
 namespace krets {
 
 __device__ __forceinline__ float warp_maxf(float v) {
@@ -674,11 +679,13 @@ __device__ int g_coef_pass(const DevProg &P, const double *values, double h, int
 template <int G>
 __device__ int g_factor64_merge(const DevProg &P, double *lu, int gl, int gid) {
   int bad = 0;
+  const int m = P.tail_m;
   for (int l = 0; l < P.nlev; ++l) {
     const int r0 = P.lev_ptr[l], r1 = P.lev_ptr[l + 1];
+    const bool tail_level = m && l == P.nlev - 1;  // rows of the dense block: sparse columns only
     for (int t = r0 + gl; t < r1; t += G) {
       const int k = P.ldesc[t].x;
-      const int dk = P.lu_diag[k], re = P.lu_rowptr[k + 1];
+      const int dk = tail_level ? P.lu_rowptr[k + 1] - m : P.lu_diag[k], re = P.lu_rowptr[k + 1];
       for (int s = P.lu_rowptr[k]; s < dk; ++s) {
         const int j = P.lu_col[s];
         const double l_kj = lu[s] / lu[P.lu_diag[j]];
@@ -695,11 +702,36 @@ __device__ int g_factor64_merge(const DevProg &P, double *lu, int gl, int gid) {
           lu[p] -= l_kj * lu[u];
         }
       }
-      const double d = lu[dk];
-      if (!(fabs(d) > 0)) bad |= KS_SINGULAR;
-      else if (!isfinite(d)) bad |= KS_NONFINITE;
+      if (!tail_level) {
+        const double d = lu[dk];
+        if (!(fabs(d) > 0)) bad |= KS_SINGULAR;
+        else if (!isfinite(d)) bad |= KS_NONFINITE;
+      }
     }
     gsync<G>(gid);
+  }
+  if (m) {
+    // dense right-looking LU of the trailing block, row i of the block at slots
+    // lu_rowptr[tail0 + i + 1] - m .. (column j of the block at offset j)
+    const int t0 = P.tail0;
+    for (int kk = 0; kk < m; ++kk) {
+      const double *pr = lu + (P.lu_rowptr[t0 + kk + 1] - m);
+      const double piv = pr[kk];
+      if (!(fabs(piv) > 0)) bad |= KS_SINGULAR;
+      else if (!isfinite(piv)) bad |= KS_NONFINITE;
+      for (int i = kk + 1 + gl; i < m; i += G) {
+        double *ri = lu + (P.lu_rowptr[t0 + i + 1] - m);
+        ri[kk] = ri[kk] / piv;
+      }
+      gsync<G>(gid);
+      const int w = m - kk - 1;  // rows and columns below / right of the pivot
+      for (long long q = gl; q < (long long)w * w; q += G) {
+        const int i = kk + 1 + (int)(q / w), c = kk + 1 + (int)(q % w);
+        double *ri = lu + (P.lu_rowptr[t0 + i + 1] - m);
+        ri[c] -= ri[kk] * pr[c];
+      }
+      gsync<G>(gid);
+    }
   }
   for (int k = gl; k < P.n; k += G) {
     const int sl = P.lu_diag[k];
@@ -818,6 +850,116 @@ __device__ __forceinline__ void df_level_split(const SProg &S, const df *__restr
 
 // SG: group size the row splits are chosen for (a caller that must reproduce another
 // group size's arithmetic bit for bit passes that size)
+// Blocked dense triangular solves of the trailing block (positions tail0 ..).  Row i of the
+// block keeps its dense part (columns tail0 ..) at slot `base` from the descriptor of the
+// last L level: first entry + entries before the block.  Blocks of 32 rows: the diagonal
+// block on the group's first warp (a lane per row, values broadcast by shuffles), then
+// the rows after (lower) or before (upper) it updated in parallel, 8 lanes per row.
+__device__ __forceinline__ int dense_base(const int4 d) { return d.y + d.w + (int)((unsigned)d.x >> 16); }
+
+template <int G, bool UPPER>
+__device__ __forceinline__ void df_dense_update(const int4 *td, const df *__restrict__ lu, df *y, int t0, int kb,
+                                                int nb, int r_begin, int r_end, int gl) {
+  const int sub = gl & 7;
+  const unsigned mask = 0xffu << ((threadIdx.x & 31) & ~7);
+  df yv[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) yv[q] = sub + 8 * q < nb ? y[t0 + kb + sub + 8 * q] : df{0.f, 0.f};
+  for (int r = r_begin + (gl >> 3); r < r_end; r += G / 8) {
+    const int base = dense_base(td[r]);
+    df a[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) a[q] = sub + 8 * q < nb ? lu[base + kb + sub + 8 * q] : df{0.f, 0.f};
+    df s{0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) s = df_fma(a[q], yv[q], s);
+    s = df_lane_sum(s, 8, mask);
+    if (sub == 0) y[t0 + r] = df_sub(y[t0 + r], s);
+  }
+}
+
+// Diagonal block rows of the first warp: lane i holds row kb + i; with a staging tile the
+// block is loaded once (all loads in flight) and read from shared memory.
+__device__ __forceinline__ const df *dense_diag_rows(const SProg &S, const df *__restrict__ lu, int base, int kb,
+                                                     int nb, int i) {
+  if (!S.dense_stage) return lu + base + kb;
+  df *t = S.dense_stage + i * 33;
+  if (i < nb) {
+    df v[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = j < nb ? lu[base + kb + j] : df{0.f, 0.f};
+#pragma unroll
+    for (int j = 0; j < 32; ++j) t[j] = v[j];
+  }
+  __syncwarp();
+  return t;
+}
+
+template <int G>
+__device__ __forceinline__ void df_dense_lower(const SProg &S, const df *__restrict__ lu, df *y, int gl, int gid) {
+  const int m = S.tail_m, t0 = S.tail0;
+  const int4 *td = S.ldesc + S.lev_ptr[S.nlev - 1];
+  for (int kb = 0; kb < m; kb += 32) {
+    const int nb = min(32, m - kb);
+    if (gl < 32) {
+      const int i = gl;
+      df yi{0.f, 0.f};
+      int base = 0;
+      if (i < nb) {
+        base = dense_base(td[kb + i]);
+        yi = y[t0 + kb + i];
+      }
+      const df *row = dense_diag_rows(S, lu, base, kb, nb, i);
+      for (int j = 0; j < nb - 1; ++j) {
+        df yj;
+        yj.hi = __shfl_sync(kFull, yi.hi, j);
+        yj.lo = __shfl_sync(kFull, yi.lo, j);
+        if (i > j && i < nb) yi = df_fma(df_neg(row[j]), yj, yi);
+      }
+      if (i < nb) y[t0 + kb + i] = yi;
+      __syncwarp();  // staging tile free for the next block
+    }
+    gsync<G>(gid);
+    if (kb + nb < m) {
+      df_dense_update<G, false>(td, lu, y, t0, kb, nb, kb + nb, m, gl);
+      gsync<G>(gid);
+    }
+  }
+}
+
+template <int G>
+__device__ __forceinline__ void df_dense_upper(const SProg &S, const df *__restrict__ lu, df *y, int gl, int gid) {
+  const int m = S.tail_m, t0 = S.tail0;
+  const int4 *td = S.ldesc + S.lev_ptr[S.nlev - 1];
+  for (int kb = ((m - 1) / 32) * 32; kb >= 0; kb -= 32) {
+    const int nb = min(32, m - kb);
+    if (gl < 32) {
+      const int i = gl;
+      df yi{0.f, 0.f};
+      int base = 0;
+      if (i < nb) {
+        base = dense_base(td[kb + i]);
+        yi = y[t0 + kb + i];
+      }
+      const df *row = dense_diag_rows(S, lu, base, kb, nb, i);
+      for (int j = nb - 1; j >= 0; --j) {
+        if (i == j) yi = df_mul(yi, row[j]);  // reciprocal diagonal
+        df xj;
+        xj.hi = __shfl_sync(kFull, yi.hi, j);
+        xj.lo = __shfl_sync(kFull, yi.lo, j);
+        if (i < j) yi = df_fma(df_neg(row[j]), xj, yi);
+      }
+      if (i < nb) y[t0 + kb + i] = yi;
+      __syncwarp();  // staging tile free for the next block
+    }
+    gsync<G>(gid);
+    if (kb > 0) {
+      df_dense_update<G, true>(td, lu, y, t0, kb, nb, 0, kb, gl);
+      gsync<G>(gid);
+    }
+  }
+}
+
 template <int G, bool UPPER, int SG = G>
 __device__ __forceinline__ void df_solve(const SProg &S, const df *__restrict__ lu, df *y, int gl, int gid, int nar) {
   const int nl = UPPER ? S.nulev : S.nlev;
@@ -826,12 +968,14 @@ __device__ __forceinline__ void df_solve(const SProg &S, const df *__restrict__ 
   const int *mx = UPPER ? S.umax : S.lmax;
   const bool w0 = gl < 32;
   if (nar < 0) {  // no narrow-level split: every level on the whole group
+    if (UPPER && S.tail_m) df_dense_upper<G>(S, lu, y, gl, gid);
     for (int l = UPPER ? 0 : 1; l < nl; ++l) {
       const int spl = split_lanes<SG>(ptr[l + 1] - ptr[l], mx[l]);
       if (spl > 1) df_level_split<UPPER>(S, lu, y, ptr, desc, l, gl, G, spl);
       else df_level<G, UPPER>(S, lu, y, ptr, desc, l, gl, G);
       gsync<G>(gid);
     }
+    if (!UPPER && S.tail_m) df_dense_lower<G>(S, lu, y, gl, gid);
     return;
   }
   if (!UPPER) {

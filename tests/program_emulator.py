@@ -177,3 +177,88 @@ def transposed_solve(prog, n, lu, c):
     y = np.zeros(n)
     y[prog["prow"]] = z                                      # position k <-> row prow[k]
     return y
+
+
+def export_multi(table, n, mode, method="be", h=1e-9):
+    """Program of the multi-circuit engine (dense trailing block, no update list)."""
+    return _lib.symbolic_export(table, n, mode, method, h, 1e3, 0xff | 0x100)
+
+
+def factor_multi(prog, n, ca):
+    """Device factorisation of a multi-circuit program: rows merged in level order (rows of
+    the dense trailing block only over their columns before it), then a dense LU of the
+    block.  Returns the LU values (plain diagonal)."""
+    lu = np.zeros(len(prog["lu_col"]))
+    for t in range(len(prog["a_col"])):
+        s = 0.0
+        for u in range(prog["a_cptr"][t], prog["a_cptr"][t + 1]):
+            code = int(prog["a_contrib"][u])
+            val = 1.0 if code & 2 else ca[code >> 2].real
+            s += -val if code & 1 else val
+        lu[prog["a_slot"][t]] = s
+    rp, col, dg = prog["lu_rowptr"], prog["lu_col"], prog["lu_diag"]
+    t0, m = int(prog["meta"][7]), int(prog["meta"][8])
+    lev_ptr, lev_rows = prog["lev_ptr"], prog["lev_rows"]
+    nlev = len(lev_ptr) - 1
+    done = np.zeros(n, dtype=bool)
+    for lv in range(nlev):
+        rows = lev_rows[lev_ptr[lv]:lev_ptr[lv + 1]]
+        tail = m > 0 and lv == nlev - 1
+        for k in rows:
+            pos = {int(col[s]): s for s in range(rp[k], rp[k + 1])}
+            lim = rp[k + 1] - m if tail else dg[k]
+            for s in range(rp[k], lim):
+                j = int(col[s])
+                assert done[j], "factor level order violated"
+                l = lu[s] / lu[dg[j]]
+                lu[s] = l
+                for u in range(dg[j] + 1, rp[j + 1]):
+                    lu[pos[int(col[u])]] -= l * lu[u]
+        for k in rows:
+            done[k] = True
+    if m:
+        A = np.array([lu[rp[t0 + i + 1] - m:rp[t0 + i + 1]] for i in range(m)])
+        for kk in range(m):
+            A[kk + 1:, kk] /= A[kk, kk]
+            A[kk + 1:, kk + 1:] -= np.outer(A[kk + 1:, kk], A[kk, kk + 1:])
+        for i in range(m):
+            lu[rp[t0 + i + 1] - m:rp[t0 + i + 1]] = A[i]
+    return lu
+
+
+def solve_multi(prog, n, lu, b):
+    """Solve with the factors of factor_multi in the device's order: L levels (the last one
+    = sparse parts of the dense block's rows), dense forward, dense backward, U levels.
+    b in position-row order; returns x in unknown order."""
+    rp, col, dg = prog["lu_rowptr"], prog["lu_col"], prog["lu_diag"]
+    t0, m = int(prog["meta"][7]), int(prog["meta"][8])
+    y = np.asarray(b, dtype=float).copy()
+    lev_ptr, lev_rows = prog["lev_ptr"], prog["lev_rows"]
+    nlev = len(lev_ptr) - 1
+    for lv in range(1, nlev):
+        tail = m > 0 and lv == nlev - 1
+        new = {}
+        for k in lev_rows[lev_ptr[lv]:lev_ptr[lv + 1]]:
+            lim = rp[k + 1] - m if tail else dg[k]
+            new[k] = y[k] - sum(lu[s] * y[col[s]] for s in range(rp[k], lim))
+        for k, v in new.items():      # a level's rows are independent
+            y[k] = v
+    if m:
+        D = np.array([lu[rp[t0 + i + 1] - m:rp[t0 + i + 1]] for i in range(m)])
+        z = y[t0:].copy()
+        for i in range(m):
+            z[i] -= D[i, :i] @ z[:i]
+        for i in range(m - 1, -1, -1):
+            z[i] = (z[i] - D[i, i + 1:] @ z[i + 1:]) / D[i, i]
+        y[t0:] = z
+    ulp, ulr = prog["ulev_ptr"], prog["ulev_rows"]
+    assert not m or not np.any(ulr >= t0)
+    for lv in range(len(ulp) - 1):
+        new = {}
+        for k in ulr[ulp[lv]:ulp[lv + 1]]:
+            new[k] = (y[k] - sum(lu[s] * y[col[s]] for s in range(dg[k] + 1, rp[k + 1]))) / lu[dg[k]]
+        for k, v in new.items():
+            y[k] = v
+    x = np.zeros(n)
+    x[prog["q"]] = y
+    return x

@@ -146,3 +146,27 @@ def test_monte_carlo_values_deterministic():
     np.testing.assert_array_equal(v1, v2)
     assert v1.shape == (4, len(c.elements))
     assert np.all(v1[:, 0] == 0.0)            # the source value is not perturbed
+
+
+def test_multi_circuit_program_dense_tail_solves(built_lib, oracle_lib):
+    """Multi-circuit programs of a random netlist: the fully dense trailing block is found,
+    its rows leave the U schedule, and factor + solve in the device's order (levels, dense
+    block) reproduce a dense solve."""
+    from krets_gb300.generators import uneven_table
+    t, n = uneven_table(4)
+    p = PE.export_multi(t, n, 2)
+    t0, m = int(p["meta"][7]), int(p["meta"][8])
+    assert m >= 64 and t0 + m == n
+    rp, col = p["lu_rowptr"], p["lu_col"]
+    for k in range(t0, n):                      # every block row holds columns t0 .. n-1
+        assert np.array_equal(col[rp[k + 1] - m:rp[k + 1]], np.arange(t0, n))
+    lv = p["lev_ptr"]
+    assert np.array_equal(p["lev_rows"][lv[-2]:lv[-1]], np.arange(t0, n))
+    assert len(p["ulev_rows"]) == t0
+    ca, _ = PE.element_coefs(t, 2, "be", 1e-9, prev=np.zeros(n), icap=np.zeros(len(t)))
+    lu = PE.factor_multi(p, n, ca)
+    A, _ = oracle_lib.assemble(t, n, "tran", 1e-9, "be", sol=np.zeros(n))
+    rhs = np.sin(np.arange(n) * 0.37)
+    x = PE.solve_multi(p, n, lu, rhs[p["prow"]])
+    xd = np.linalg.solve(A.reshape(n, n), rhs)
+    np.testing.assert_allclose(x, xd, rtol=0, atol=1e-10 * np.abs(xd).max())
