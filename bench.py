@@ -6,10 +6,18 @@ Workload (one "step" = one full pass): 2048 instances of a 200-section RLC ladde
 unknown (602) is written at every step.  Metric: circuit-timesteps/sec.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload mc_transient|op|ac|uneven|adjoint]
 
 --impl reference times the reference's CPU algorithm (the C restatement in oracle/,
 rebuilding and refactoring the matrix every step as krets does) on the host cores.
-Prints ONE JSON line on rank 0.
+Prints ONE JSON line on rank 0.  The default workload is the headline above; the others
+are the remaining measured configurations of the solve path:
+  op       plain operating point of a 1000-resistor ladder with shunts (n = 1001), solves/s
+  ac       4096-point AC sweep (Decade 455, 1 Hz - 1 GHz) of a 500-section RC ladder, points/s
+  uneven   4096 distinct random netlists (10-5000 nodes), operating point + 2000 BE steps
+           at 1 ns each, circuit-timesteps/s
+  adjoint  1024 x 1000-section RC ladder, TR 1 ns x 2000 steps, loss sum V(n20)^2 and its
+           gradient w.r.t. every R and C (checkpoint every 100 steps), gradients/s
 """
 from __future__ import annotations
 
@@ -332,12 +340,305 @@ def run_ours(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ other workloads
+def _timed(args, step, flush, timing):
+    """W >= 3 untimed steps, then K steps each bracketed by device synchronisation, L2
+    flushed in between; returns per-step (kernel ms, call ms) from the library's events."""
+    from krets_gb300 import _lib
+    for _ in range(max(3, args.warmup)):
+        step()
+        flush()
+    ks, cs = [], []
+    for _ in range(args.steps):
+        _lib.lib().krets_device_synchronize()
+        step()
+        _lib.lib().krets_device_synchronize()
+        k, c = timing()
+        ks.append(k)
+        cs.append(c)
+        flush()
+    return ks, cs
+
+
+def _line(args, world, metric, value, unit, workload, extra):
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "data": "synthetic (seeded splitmix64)", "config": {"workload": workload}}
+    line.update(extra)
+    return line
+
+
+def _cpu_pool(fn, items, threads):
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(fn, items))
+    return time.perf_counter() - t0
+
+
+def workload_op(args, world, reference):
+    from krets_gb300 import _lib
+    from krets_gb300.generators import config1_circuit
+    from krets_gb300.table import element_table
+    from oracle import oracle as O
+    c = config1_circuit()
+    t = element_table(c)
+    wl = "plain_op_resistor_ladder_1000_with_shunts_n1001"
+    threads = os.cpu_count() or 1
+    if reference:
+        O.lib()
+        reps = 200
+        dt = _cpu_pool(lambda _: O.op(t, c.size), range(reps * threads), threads)
+        v = reps * threads / dt
+        return _line(args, world, "OP solves/sec", v, "solves/s", wl,
+                     {"impl": "reference", "dtype": "f64", "cpu_baseline": {"value": v, "unit": "solves/s",
+                      "cores": threads, "kind": "port", "sample": f"{reps * threads} OP solves"},
+                      "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+    g = _lib.GpuCircuit(t, c.size)
+    l0 = _lib.launch_count()
+    with ClockSampler() as clk:
+        ks, cs = _timed(args, g.op, g.flush_l2, g.timing)
+    launches = _lib.launch_count() - l0
+    x, _ = g.op()
+    ref = O.op(t, c.size)
+    err = float(np.abs(x - ref).max() / np.abs(ref).max())
+    reps = 200
+    dt = _cpu_pool(lambda _: O.op(t, c.size), range(reps), 1)
+    alg = (2000 * 8 + c.size * 8)
+    k_s = statistics.mean(ks) / 1e3
+    peak, pk = measured_peak_hbm()
+    return _line(args, world, "OP solves/sec", 1e3 / statistics.mean(ks), "solves/s", wl, {
+        "ms_per_step": statistics.mean(cs), "dtype": "f64", "max_rel_err_vs_fp64": err,
+        "roofline": {"bound": "hbm", "achieved": alg / k_s / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": alg / k_s / 1e9 / peak, "traffic": None, "peak_kind": pk, "kernel": "k_op",
+                     "algorithmic_bytes_per_launch": alg, "note": "latency bound (one 1001-unknown solve)"},
+        "cpu_baseline": {"value": reps / dt, "unit": "solves/s", "cores": 1, "kind": "port",
+                         "sample": f"{reps} OP solves, oracle/ C restatement"},
+        "e2e": {"value": 1e3 / statistics.mean(cs), "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": c.size * 8},
+        "gpu_launches": int(launches), "clocks": clk.summary()})
+
+
+def workload_ac(args, world, reference):
+    from krets_gb300 import _lib
+    from krets_gb300.analyses import AcAnalysis, Decade, generate_frequencies
+    from krets_gb300.generators import rc_ladder_ac
+    from krets_gb300.table import element_table, is_current_mask
+    from oracle import oracle as O
+    c = rc_ladder_ac()
+    t = element_table(c)
+    f = np.array(generate_frequencies(AcAnalysis(Decade(455), 1.0, 1e9)))
+    wl = f"ac_sweep_rc_ladder_500sec_{len(f)}pts_decade455_1Hz_1GHz"
+    threads = os.cpu_count() or 1
+    if reference:
+        O.lib()
+        chunks = [f[i::threads * 4] for i in range(threads * 4)]
+        dt = _cpu_pool(lambda fr: O.ac(t, c.size, fr), chunks, threads)
+        v = len(f) / dt
+        return _line(args, world, "AC points/sec", v, "points/s", wl,
+                     {"impl": "reference", "dtype": "c128", "cpu_baseline": {"value": v, "unit": "points/s",
+                      "cores": threads, "kind": "port", "sample": f"all {len(f)} points"},
+                      "e2e": {"value": v, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+    g = _lib.GpuCircuit(t, c.size)
+    d_out = _lib.DeviceArray((1, len(f), c.size, 2))
+    l0 = _lib.launch_count()
+    with ClockSampler() as clk:
+        ks, cs = _timed(args, lambda: g.batch_ac(None, f, precision=_lib.PREC_MIXED, out=d_out), g.flush_l2,
+                        g.timing)
+    launches = _lib.launch_count() - l0
+    z = g.batch_ac(None, f, precision=_lib.PREC_MIXED)[0]
+    e2e_ms = g.timing()[1]
+    mask = is_current_mask(c)
+    sample = np.arange(0, len(f), 97)
+    refz = O.ac(t, c.size, f[sample])
+    err = 0.0
+    for j, i in enumerate(sample):
+        d = np.abs(z[i] - refz[j])
+        r = np.abs(refz[j])
+        err = max(err, d[mask].max() / r[mask].max(), d[~mask].max() / r[~mask].max())
+    dt = _cpu_pool(lambda fr: O.ac(t, c.size, fr), [f[:256]], 1)
+    alg = len(f) * c.size * 16 + 1000 * 8
+    k_s = statistics.mean(ks) / 1e3
+    peak, pk = measured_peak_hbm()
+    return _line(args, world, "AC points/sec", len(f) / k_s, "points/s", wl, {
+        "ms_per_step": statistics.mean(cs), "dtype": "c64 factor, c128 refinement", "max_rel_err_vs_fp64": err,
+        "roofline": {"bound": "hbm", "achieved": alg / k_s / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": alg / k_s / 1e9 / peak, "traffic": None, "peak_kind": pk, "kernel": "k_ac_batch<1>",
+                     "algorithmic_bytes_per_launch": alg},
+        "cpu_baseline": {"value": 256 / dt, "unit": "points/s", "cores": 1, "kind": "port",
+                         "sample": "256 points, oracle/ C restatement"},
+        "e2e": {"value": len(f) / (e2e_ms / 1e3), "unit": "points/s", "h2d_bytes_per_step": int(f.nbytes),
+                "d2h_bytes_per_step": int(z.nbytes)},
+        "gpu_launches": int(launches), "clocks": clk.summary()})
+
+
+UNEVEN_CIRCUITS, UNEVEN_STEPS, UNEVEN_H = 4096, 2000, 1e-9
+
+
+def workload_uneven(args, world, reference):
+    from krets_gb300 import _lib
+    from krets_gb300.generators import uneven_table
+    from oracle import oracle as O
+    wl = f"uneven_random_netlists_{UNEVEN_CIRCUITS}x10-5000nodes_op_be_1ns_{UNEVEN_STEPS}steps"
+    threads = os.cpu_count() or 1
+    metric = "circuit-timesteps/sec"
+    if reference:
+        O.lib()
+        # bounded sample: every 64th netlist (sizes across the whole range), 200 steps
+        idx = list(range(0, UNEVEN_CIRCUITS, 64))
+        tabs = {i: uneven_table(i) for i in idx}
+        steps = 200
+        dt = _cpu_pool(lambda i: O.tran(tabs[i][0], tabs[i][1], UNEVEN_H, steps, method="be", lag=True), idx,
+                       threads)
+        v = len(idx) * steps / dt
+        return _line(args, world, metric, v, "circuit-timesteps/s", wl,
+                     {"impl": "reference", "dtype": "f64", "cpu_baseline": {"value": v, "unit": "circuit-timesteps/s",
+                      "cores": threads, "kind": "port",
+                      "sample": f"{len(idx)} netlists (every 64th) x {steps} BE steps, factor once"},
+                      "e2e": {"value": v, "unit": "circuit-timesteps/s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}})
+    tabs = [uneven_table(i) for i in range(UNEVEN_CIRCUITS)]
+    t0 = time.perf_counter()
+    m = _lib.MultiCircuit([t for t, _ in tabs], [n for _, n in tabs], method="be", h=UNEVEN_H)
+    create_s = time.perf_counter() - t0
+    out = _lib.DeviceArray(m.total(UNEVEN_STEPS))
+    l0 = _lib.launch_count()
+    g_flush = _lib.GpuCircuit(tabs[0][0], tabs[0][1])
+    with ClockSampler() as clk:
+        ks, cs = _timed(args, lambda: m.tran(UNEVEN_STEPS, out=out), g_flush.flush_l2, m.timing)
+    launches = _lib.launch_count() - l0
+    info = m.info()
+    value = UNEVEN_CIRCUITS * UNEVEN_STEPS / (statistics.mean(ks) / 1e3)
+    offs = m.offsets(UNEVEN_STEPS)
+    errs = []
+    for i in (0, 1, 2, 3, 7):
+        t, n = tabs[i]
+        ref = O.tran(t, n, UNEVEN_H, UNEVEN_STEPS, method="be", lag=True)
+        x = np.empty((UNEVEN_STEPS + 1) * n)
+        _lib.check(_lib.lib().krets_memcpy_d2h(x.ctypes.data_as(_lib.ctypes.c_void_p),
+                                               _lib.ctypes.c_void_p(out.ptr + 8 * int(offs[i])), x.nbytes))
+        x = x.reshape(UNEVEN_STEPS + 1, n)
+        cur = np.zeros(n, bool)
+        cur[t["b"][t["b"] >= 0]] = True
+        e = 0.0
+        for mm in (cur, ~cur):
+            if mm.any():
+                e = max(e, np.abs(x[:, mm] - ref[:, mm]).max() / np.abs(ref[:, mm]).max())
+        errs.append(e)
+    # CPU baseline: the same bounded sample as the reference arm, factor once
+    idx = list(range(0, UNEVEN_CIRCUITS, 64))
+    cdt = _cpu_pool(lambda i: O.tran(tabs[i][0], tabs[i][1], UNEVEN_H, 200, method="be", lag=True), idx, threads)
+    # end to end with a host output buffer: the first circuits up to 8 GB of waveforms
+    k = 0
+    tot = 0
+    while k < len(tabs) and tot + (UNEVEN_STEPS + 1) * tabs[k][1] * 8 < 8e9:
+        tot += (UNEVEN_STEPS + 1) * tabs[k][1] * 8
+        k += 1
+    m2 = _lib.MultiCircuit([t for t, _ in tabs[:k]], [n for _, n in tabs[:k]], method="be", h=UNEVEN_H)
+    host = np.empty(m2.total(UNEVEN_STEPS))
+    m2.tran(UNEVEN_STEPS, out=host)
+    m2.tran(UNEVEN_STEPS, out=host)
+    e2e = k * UNEVEN_STEPS / (m2.timing()[1] / 1e3)
+    alg = (int(info[1]) * UNEVEN_STEPS + int(info[1])) * 8
+    k_s = statistics.mean(ks) / 1e3
+    peak, pk = measured_peak_hbm()
+    return _line(args, world, metric, value, "circuit-timesteps/s", wl, {
+        "ms_per_step": statistics.mean(cs), "dtype": "f64-factor, double-float (2xfp32) solves",
+        "max_rel_err_vs_fp64": max(errs), "circuits": UNEVEN_CIRCUITS, "sum_unknowns": int(info[1]),
+        "sum_lu_entries": int(info[2]), "circuits_per_class": info[4:10].tolist(),
+        "class_end_ms": (info[10:16] / 1e3).tolist(), "symbolic_s": create_s,
+        "roofline": {"bound": "hbm", "achieved": alg / k_s / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": alg / k_s / 1e9 / peak, "traffic": None, "peak_kind": pk,
+                     "kernel": "k_multi_tran (all classes)", "algorithmic_bytes_per_launch": alg},
+        "cpu_baseline": {"value": len(idx) * 200 / cdt, "unit": "circuit-timesteps/s", "cores": threads,
+                         "kind": "port", "sample": f"{len(idx)} netlists (every 64th) x 200 BE steps, factor once"},
+        "e2e": {"value": e2e, "unit": "circuit-timesteps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(host.nbytes), "circuits": k},
+        "gpu_launches": int(launches), "clocks": clk.summary()})
+
+
+ADJ_INST, ADJ_SECTIONS, ADJ_STEPS, ADJ_H, ADJ_K = 1024, 1000, 2000, 1e-9, 100
+
+
+def workload_adjoint(args, world, reference):
+    from krets_gb300 import _lib
+    from krets_gb300.generators import rc_ladder_step
+    from krets_gb300.table import element_table
+    from oracle import oracle as O
+    c = rc_ladder_step(ADJ_SECTIONS)
+    t = element_table(c)
+    out = c.index_map["V(n20)"]
+    wl = f"adjoint_rc_ladder_{ADJ_INST}x{ADJ_SECTIONS}sec_tr_1ns_{ADJ_STEPS}steps_K{ADJ_K}_loss_sum_Vn20_sq"
+    threads = os.cpu_count() or 1
+    metric = "gradients/sec (loss + d loss / d every R and C)"
+    if reference:
+        O.lib()
+        n_s = 2 * threads
+        dt = _cpu_pool(lambda _: O.adjoint_tran(t, c.size, ADJ_H, ADJ_STEPS, out), range(n_s), threads)
+        v = n_s / dt
+        return _line(args, world, metric, v, "gradients/s", wl,
+                     {"impl": "reference", "dtype": "f64", "cpu_baseline": {"value": v, "unit": "gradients/s",
+                      "cores": threads, "kind": "port", "sample": f"{n_s} FP64 adjoint gradients (oracle/)"},
+                      "e2e": {"value": v, "unit": "gradients/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+    vals = np.tile(t["value"], (ADJ_INST, 1))
+    g = _lib.GpuCircuit(t, c.size)
+    l0 = _lib.launch_count()
+    res = {}
+    with ClockSampler() as clk:
+        ks, cs = _timed(args, lambda: res.__setitem__("r", g.adjoint_tran(vals, ADJ_H, ADJ_STEPS, out,
+                                                                           checkpoint_every=ADJ_K)),
+                        g.flush_l2, g.timing)
+    launches = _lib.launch_count() - l0
+    loss, grad = res["r"]
+    fwd = _lib.DeviceArray((ADJ_INST, ADJ_STEPS + 1, c.size))
+    fks, _ = _timed(args, lambda: g.batch_tran(vals, ADJ_H, ADJ_STEPS, "tr", lag=False, precision=_lib.PREC_DF,
+                                                 out=fwd), g.flush_l2, g.timing)
+    del fwd
+    L, gref = O.adjoint_tran(t, c.size, ADJ_H, ADJ_STEPS, out)
+    gerr = float(np.max(np.abs(grad[0] - gref)) / np.max(np.abs(gref)))
+    # central differences (h = 1e-6 relative) of the FP64 oracle loss on the 8 largest gradients
+    top = np.argsort(-np.abs(gref))[:8]
+    fd = []
+    for e in top:
+        d = 1e-6 * t["value"][e]
+        tp, tm = t.copy(), t.copy()
+        tp["value"][e] += d
+        tm["value"][e] -= d
+        fd.append((np.sum(O.tran(tp, c.size, ADJ_H, ADJ_STEPS, method="tr", lag=False)[1:, out] ** 2)
+                   - np.sum(O.tran(tm, c.size, ADJ_H, ADJ_STEPS, method="tr", lag=False)[1:, out] ** 2)) / (2 * d))
+    fd = np.array(fd)
+    fd_err = float(np.max(np.abs(grad[0][top] - fd) / np.abs(fd)))
+    fd_floor = float(np.max(np.abs(gref[top] - fd) / np.abs(fd)))  # FP64 adjoint vs the same differences
+    n_s = 2 * threads
+    cdt = _cpu_pool(lambda _: O.adjoint_tran(t, c.size, ADJ_H, ADJ_STEPS, out), range(n_s), threads)
+    k_s = statistics.mean(ks) / 1e3
+    J = (ADJ_STEPS + ADJ_K - 1) // ADJ_K
+    alg = ADJ_INST * (2 * c.elements.__len__() * 8 + 2 * J * c.size * 8)
+    peak, pk = measured_peak_hbm()
+    return _line(args, world, metric, ADJ_INST / k_s, "gradients/s", wl, {
+        "ms_per_step": statistics.mean(cs), "dtype": "f64-factor, double-float (2xfp32) solves",
+        "forward_ms": statistics.mean(fks), "gradient_over_forward": statistics.mean(ks) / statistics.mean(fks),
+        "loss_rel_err_vs_fp64_adjoint": abs(loss[0] - L) / L, "grad_rel_err_vs_fp64_adjoint": gerr,
+        "grad_rel_err_vs_central_fd_1e-6": fd_err, "fp64_adjoint_rel_err_vs_central_fd_1e-6": fd_floor,
+        "roofline": {"bound": "hbm", "achieved": alg / k_s / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": alg / k_s / 1e9 / peak, "traffic": None, "peak_kind": pk, "kernel": "k_adjoint_dfd",
+                     "algorithmic_bytes_per_launch": alg},
+        "cpu_baseline": {"value": n_s / cdt, "unit": "gradients/s", "cores": threads, "kind": "port",
+                         "sample": f"{n_s} FP64 adjoint gradients (oracle/)"},
+        "e2e": {"value": ADJ_INST / (statistics.mean(cs) / 1e3), "unit": "gradients/s",
+                "h2d_bytes_per_step": int(vals.nbytes), "d2h_bytes_per_step": int(grad.nbytes + loss.nbytes)},
+        "gpu_launches": int(launches), "clocks": clk.summary()})
+
+
+WORKLOADS = {"op": workload_op, "ac": workload_ac, "uneven": workload_uneven, "adjoint": workload_adjoint}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="mc_transient", choices=["mc_transient"] + sorted(WORKLOADS))
     args = ap.parse_args()
     rank, world, local = dist_env()
     if world > 1:
@@ -346,6 +647,11 @@ def main():
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
         import torch.distributed as dist
         dist.init_process_group("gloo")
+    if args.workload != "mc_transient":
+        line = WORKLOADS[args.workload](args, world, args.impl == "reference")
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
     else:

@@ -100,7 +100,8 @@ __device__ __forceinline__ void df_tsolve(const int *T, const int *toff, int nut
 }
 
 // One forward step of the double-float engine on x (in place), as k_tran_dfd; row splits
-// chosen for a group of SG threads, so groups of different sizes give identical states.
+// chosen for a group of SG threads (the forward pass splits rows for the whole CTA, the
+// recomputation for its half, so recomputed states match the forward pass's to rounding).
 template <int G, int SG>
 __device__ __forceinline__ void adj_forward_step(const DevProg &P, const SProg &S, const df *lu, df *x, const df *cdyn,
                                                  df *cb, df *icap, const double *vals, int method, double t_src,
@@ -267,7 +268,7 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
       }
       if (mode == 1 && s - 1 == last0)
         for (int k = tid; k < n; k += GF) last_seg[k] = x[k];
-      adj_forward_step<GF, GH>(P, S, lu, x, cdyn, cb, icap, vals, method, (double)s * h, tid, 0);
+      adj_forward_step<GF, GF>(P, S, lu, x, cdyn, cb, icap, vals, method, (double)s * h, tid, 0);
       if (tid == 0) loss = df_fma(x[out_pos], x[out_pos], loss);
       if (mode == 1 && s > last0)
         for (int k = tid; k < n; k += GF) last_seg[(size_t)(s - last0) * n + k] = x[k];

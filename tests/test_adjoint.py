@@ -81,8 +81,8 @@ def test_adjoint_checkpoint_interval_does_not_change_result():
     l1, g1 = g.adjoint_tran(vals, 1e-9, 200, out, checkpoint_every=200)
     l2, g2 = g.adjoint_tran(vals, 1e-9, 200, out, checkpoint_every=7)
     l3, g3 = g.adjoint_tran(vals, 1e-9, 200, out, checkpoint_every=7)
-    # recomputed segments reproduce the forward states bit for bit (same loss); the
-    # gradient sums are formed segment by segment, so only their rounding differs
+    # the loss comes from the forward pass alone; recomputed segments and the segment-wise
+    # gradient sums differ from a single segment only in rounding
     assert np.array_equal(l1, l2)
     assert np.max(np.abs(g1 - g2)) <= 1e-12 * np.max(np.abs(g1))
     assert np.array_equal(l2, l3) and np.array_equal(g2, g3)      # run to run
