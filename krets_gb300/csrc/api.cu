@@ -1461,7 +1461,7 @@ krets_status krets_multi_create(int32_t n_circuits, const krets_element *elems, 
       for (int c : k.items)
         for (int ph = 0; ph < 2; ++ph) {
           const DevProg &V = views[2 * c + ph];
-          xb = std::max<long long>(xb, mlay_al16(8ll * V.n) + mlay_al16(8ll * V.ndyn));
+          xb = std::max<long long>(xb, mlay_al16(8ll * V.n) + mlay_al16(8ll * V.ndyn) + mlay_al16(4ll * V.tail_m));
         }
       k.x_smem = kStageBytes + xb <= smax / 2;
       k.gsm = kStageBytes + (k.x_smem ? xb : 0);

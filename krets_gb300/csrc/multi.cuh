@@ -84,8 +84,17 @@ __global__ void __launch_bounds__(512, 1)
         gsync<G>(gid);
       }
       SProg S = sprog_view(P, GLOBAL ? P.sprog : reinterpret_cast<const int *>(region + L.sp));
-      if (GLOBAL) S.dense_stage = reinterpret_cast<df *>(gsm);
       const bool xs = GLOBAL && x_smem;
+      if (GLOBAL) {
+        S.dense_stage = reinterpret_cast<df *>(gsm);
+        if (xs && P.tail_m) {
+          // slots of the dense-block rows, after x and the rhs coefficients
+          int *rows = reinterpret_cast<int *>(gsm + kStageBytes + mlay_al16(8ll * P.n) + mlay_al16(8ll * P.ndyn));
+          for (int i = gl; i < P.tail_m; i += G) rows[i] = P.lu_rowptr[P.tail0 + i + 1] - P.tail_m;
+          gsync<G>(gid);
+          S.dense_rows = rows;
+        }
+      }
       df *lu = reinterpret_cast<df *>(region + L.lu);
       double *lu64 = reinterpret_cast<double *>(region + L.lu);
       df *x = reinterpret_cast<df *>(xs ? gsm + kStageBytes : region + L.x);
@@ -93,7 +102,7 @@ __global__ void __launch_bounds__(512, 1)
       df *cb = reinterpret_cast<df *>(xs ? gsm + kStageBytes + mlay_al16(8ll * P.n) : region + L.cb);
       df *icap = reinterpret_cast<df *>(region + L.icap);
       double *coef64 = reinterpret_cast<double *>(region + L.coef64);
-      st |= dfd_setup<G, true>(P, S, nullptr, h, method, lu, lu64, coef64, cdyn, gl, gid);
+      st |= dfd_setup<G, GLOBAL ? 2 : 1>(P, S, nullptr, h, method, lu, lu64, coef64, cdyn, gl, gid);
       if (gany<G>((st & (KS_SINGULAR | KS_NONFINITE | KS_NOTIMPL)) != 0, gid)) break;
       if (phase == 0) {
         // operating point: sources at their DC values (op.rs: capacitors removed,

@@ -44,6 +44,7 @@ struct SProg {
   int nlev, nulev;
   int tail0, tail_m;  // dense trailing block (tail_m = 0: none)
   df *dense_stage;    // 32 x 33 shared-memory tile for diagonal blocks read from global memory (or null)
+  const int *dense_rows;  // slot of column tail0 of each dense-block row, in shared memory (or null)
 };
 
 __device__ __forceinline__ SProg sprog_view(const DevProg &P, const int *sp) {
@@ -66,6 +67,7 @@ __device__ __forceinline__ SProg sprog_view(const DevProg &P, const int *sp) {
   S.tail0 = P.tail0;
   S.tail_m = P.tail_m;
   S.dense_stage = nullptr;
+  S.dense_rows = nullptr;
   return S;
 }
 
@@ -673,6 +675,90 @@ __device__ int g_coef_pass(const DevProg &P, const double *values, double h, int
   return err;
 }
 
+// As g_factor64_merge with a warp per row and the dense LU by rows over lanes: for LU
+// values in global memory, where the thread-per-row merge is a chain of dependent loads.
+// Row k eliminates its L entries in order; the lanes share each U row j, finding their
+// column in row k by binary search (or directly in the dense block).
+__device__ __forceinline__ int row_find(const int *__restrict__ col, int lo, int hi, int c) {
+  while (lo < hi) {  // first position in [lo, hi) with col >= c
+    const int mid = (lo + hi) >> 1;
+    if (col[mid] < c) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <int G>
+__device__ int g_factor64_warp(const DevProg &P, double *lu, int gl, int gid) {
+  int bad = 0;
+  const int m = P.tail_m, t0 = P.tail0;
+  const int lane = gl & 31, warp = gl >> 5;
+  constexpr int NW = G / 32;
+  for (int l = 0; l < P.nlev; ++l) {
+    const int r0 = P.lev_ptr[l], r1 = P.lev_ptr[l + 1];
+    const bool tail_level = m && l == P.nlev - 1;  // rows of the dense block: sparse columns only
+    for (int t = r0 + warp; t < r1; t += NW) {
+      const int k = P.ldesc[t].x;
+      const int re = P.lu_rowptr[k + 1];
+      const int dense0 = tail_level ? re - m : re;  // first slot of the dense part (tail rows)
+      const int dk = tail_level ? dense0 : P.lu_diag[k];
+      for (int s = P.lu_rowptr[k]; s < dk; ++s) {
+        const int j = P.lu_col[s];
+        const double l_kj = lu[s] / lu[P.lu_diag[j]];
+        __syncwarp();
+        if (lane == 0) lu[s] = l_kj;
+        const int ue = P.lu_rowptr[j + 1];
+        for (int u = P.lu_diag[j] + 1 + lane; u < ue; u += 32) {
+          const int c = P.lu_col[u];
+          int p;
+          if (tail_level && c >= t0) {
+            p = dense0 + (c - t0);
+          } else {
+            p = row_find(P.lu_col, s + 1, dense0, c);
+            if (p >= dense0 || P.lu_col[p] != c) {
+              bad |= KS_SINGULAR;  // not in the pattern: an inconsistent program
+              continue;
+            }
+          }
+          lu[p] -= l_kj * lu[u];
+        }
+        __syncwarp();
+      }
+      if (!tail_level && lane == 0) {
+        const double d = lu[dk];
+        if (!(fabs(d) > 0)) bad |= KS_SINGULAR;
+        else if (!isfinite(d)) bad |= KS_NONFINITE;
+      }
+    }
+    gsync<G>(gid);
+  }
+  if (m) {
+    // dense right-looking LU of the trailing block: a warp per row, lanes over columns
+    for (int kk = 0; kk < m; ++kk) {
+      const double *pr = lu + (P.lu_rowptr[t0 + kk + 1] - m);
+      const double piv = pr[kk];
+      if (gl == 0) {
+        if (!(fabs(piv) > 0)) bad |= KS_SINGULAR;
+        else if (!isfinite(piv)) bad |= KS_NONFINITE;
+      }
+      for (int i = kk + 1 + warp; i < m; i += NW) {
+        double *ri = lu + (P.lu_rowptr[t0 + i + 1] - m);
+        const double l_ik = ri[kk] / piv;
+        __syncwarp();
+        if (lane == 0) ri[kk] = l_ik;
+        for (int c = kk + 1 + lane; c < m; c += 32) ri[c] -= l_ik * pr[c];
+      }
+      gsync<G>(gid);
+    }
+  }
+  for (int k = gl; k < P.n; k += G) {
+    const int sl = P.lu_diag[k];
+    lu[sl] = 1.0 / lu[sl];
+  }
+  gsync<G>(gid);
+  return bad;
+}
+
 // As g_factor64, without an update list: row k merges each U row j (columns ascending)
 // into its own sorted pattern.  The host checked that every update lands in the pattern;
 // an entry not found (an inconsistent program) stops the row and reports it singular.
@@ -857,24 +943,39 @@ __device__ __forceinline__ void df_level_split(const SProg &S, const df *__restr
 // the rows after (lower) or before (upper) it updated in parallel, 8 lanes per row.
 __device__ __forceinline__ int dense_base(const int4 d) { return d.y + d.w + (int)((unsigned)d.x >> 16); }
 
+// Two rows per 8-lane group per pass, so their loads are in flight together.
 template <int G, bool UPPER>
-__device__ __forceinline__ void df_dense_update(const int4 *td, const df *__restrict__ lu, df *y, int t0, int kb,
-                                                int nb, int r_begin, int r_end, int gl) {
+__device__ __forceinline__ void df_dense_update(const SProg &S, const int4 *td, const df *__restrict__ lu, df *y,
+                                                int t0, int kb, int nb, int r_begin, int r_end, int gl) {
   const int sub = gl & 7;
   const unsigned mask = 0xffu << ((threadIdx.x & 31) & ~7);
   df yv[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) yv[q] = sub + 8 * q < nb ? y[t0 + kb + sub + 8 * q] : df{0.f, 0.f};
-  for (int r = r_begin + (gl >> 3); r < r_end; r += G / 8) {
-    const int base = dense_base(td[r]);
-    df a[4];
+  constexpr int R = G / 8;  // rows per pass of the group
+  for (int r = r_begin + (gl >> 3); r < r_end; r += 2 * R) {
+    const bool two = r + R < r_end;
+    const int b0 = S.dense_rows ? S.dense_rows[r] : dense_base(td[r]);
+    const int b1 = two ? (S.dense_rows ? S.dense_rows[r + R] : dense_base(td[r + R])) : b0;
+    df a0[4], a1[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) a[q] = sub + 8 * q < nb ? lu[base + kb + sub + 8 * q] : df{0.f, 0.f};
-    df s{0.f, 0.f};
+    for (int q = 0; q < 4; ++q) {
+      const bool in = sub + 8 * q < nb;
+      a0[q] = in ? lu[b0 + kb + sub + 8 * q] : df{0.f, 0.f};
+      a1[q] = in && two ? lu[b1 + kb + sub + 8 * q] : df{0.f, 0.f};
+    }
+    df s0{0.f, 0.f}, s1{0.f, 0.f};
 #pragma unroll
-    for (int q = 0; q < 4; ++q) s = df_fma(a[q], yv[q], s);
-    s = df_lane_sum(s, 8, mask);
-    if (sub == 0) y[t0 + r] = df_sub(y[t0 + r], s);
+    for (int q = 0; q < 4; ++q) {
+      s0 = df_fma(a0[q], yv[q], s0);
+      s1 = df_fma(a1[q], yv[q], s1);
+    }
+    s0 = df_lane_sum(s0, 8, mask);
+    s1 = df_lane_sum(s1, 8, mask);
+    if (sub == 0) {
+      y[t0 + r] = df_sub(y[t0 + r], s0);
+      if (two) y[t0 + r + R] = df_sub(y[t0 + r + R], s1);
+    }
   }
 }
 
@@ -906,7 +1007,7 @@ __device__ __forceinline__ void df_dense_lower(const SProg &S, const df *__restr
       df yi{0.f, 0.f};
       int base = 0;
       if (i < nb) {
-        base = dense_base(td[kb + i]);
+        base = S.dense_rows ? S.dense_rows[kb + i] : dense_base(td[kb + i]);
         yi = y[t0 + kb + i];
       }
       const df *row = dense_diag_rows(S, lu, base, kb, nb, i);
@@ -921,7 +1022,7 @@ __device__ __forceinline__ void df_dense_lower(const SProg &S, const df *__restr
     }
     gsync<G>(gid);
     if (kb + nb < m) {
-      df_dense_update<G, false>(td, lu, y, t0, kb, nb, kb + nb, m, gl);
+      df_dense_update<G, false>(S, td, lu, y, t0, kb, nb, kb + nb, m, gl);
       gsync<G>(gid);
     }
   }
@@ -938,7 +1039,7 @@ __device__ __forceinline__ void df_dense_upper(const SProg &S, const df *__restr
       df yi{0.f, 0.f};
       int base = 0;
       if (i < nb) {
-        base = dense_base(td[kb + i]);
+        base = S.dense_rows ? S.dense_rows[kb + i] : dense_base(td[kb + i]);
         yi = y[t0 + kb + i];
       }
       const df *row = dense_diag_rows(S, lu, base, kb, nb, i);
@@ -954,7 +1055,7 @@ __device__ __forceinline__ void df_dense_upper(const SProg &S, const df *__restr
     }
     gsync<G>(gid);
     if (kb > 0) {
-      df_dense_update<G, true>(td, lu, y, t0, kb, nb, 0, kb, gl);
+      df_dense_update<G, true>(S, td, lu, y, t0, kb, nb, 0, kb, gl);
       gsync<G>(gid);
     }
   }
@@ -1023,7 +1124,8 @@ struct DfdLay {
 // coefficients of the rhs elements (C/h or 2C/h, L/h or 2L/h, source values) to cdyn.
 // coef64 may alias x / cdyn / cb / icap: it is dead once the LU is formed, and the
 // rhs-element coefficients are recomputed with the same expressions as g_coef_pass.
-template <int G, bool MERGE = false>
+// MERGE: 0 = update list, 1 = thread-per-row merge, 2 = warp-per-row (global memory)
+template <int G, int MERGE = 0>
 __device__ __forceinline__ int dfd_setup(const DevProg &P, const SProg &S, const double *vals, double h, int method,
                                          df *lu, double *lu64, double *coef64, df *cdyn, int gl, int gid) {
   int st = g_coef_pass<G>(P, vals, h, method, coef64, gl);
@@ -1033,7 +1135,9 @@ __device__ __forceinline__ int dfd_setup(const DevProg &P, const SProg &S, const
     lu64[sl] = t < 0 ? 0.0 : sum_entry<double>(P, t, coef64, nullptr);
   }
   gsync<G>(gid);
-  st |= MERGE ? g_factor64_merge<G>(P, lu64, gl, gid) : g_factor64<G>(P, lu64, gl, gid);
+  st |= MERGE == 2   ? g_factor64_warp<G>(P, lu64, gl, gid)
+        : MERGE == 1 ? g_factor64_merge<G>(P, lu64, gl, gid)
+                     : g_factor64<G>(P, lu64, gl, gid);
   for (int sl = gl; sl < P.nnz_lu; sl += G) lu[sl] = df_from_double(lu64[sl]);
   for (int d = gl; d < P.ndyn; d += G) {
     const int e = S.dyn[d].x & 0xffffff;
