@@ -11,6 +11,7 @@
  *   krets_ac               ac::solve                             crates/krets-solver/src/solver/ac.rs:17-109
  *   krets_tran             transient::solve                      crates/krets-solver/src/solver/transient.rs:14-114
  *   krets_batch_*          (no counterpart: many instances of one topology per launch)
+ *   krets_multi_*          (no counterpart: many distinct netlists per launch set)
  *   krets_adjoint_tran     (no counterpart: adjoint sensitivities)
  *   krets_status_string /  Display of krets_solver::Error        crates/krets-solver/src/error.rs:4-36
  *   krets_last_error_message
