@@ -99,3 +99,39 @@ def test_workload_sizes():
     assert rc_ladder_ac().size == 502
     assert rlc_ladder().size == 602
     assert "R5000 5000 0 1000" in resistor_ladder_netlist(5000)
+
+
+def _write_case(tmp_path, case):
+    (tmp_path / "krets.toml").write_text(case["toml"])
+    import tomllib
+    circ = tomllib.loads(case["toml"])["circuit_path"]
+    (tmp_path / circ).write_text(case["netlist"])
+    return tmp_path / "krets.toml"
+
+
+def test_cli_ac_parquet_matches_reference_file(tmp_path, golden, oracle_lib):
+    """The CLI path (krets.toml -> netlist -> solve -> result.parquet, main.rs:27-138) with
+    the parquet layout of krets-result (lib.rs:127-208) reproduces the reference's own
+    circuits/low_pass_filter/ac/result.parquet: column names, order and values."""
+    pq = pytest.importorskip("pyarrow.parquet")
+    from oracle_solver import OracleSolver
+    from krets_gb300.__main__ import run
+    case = golden["parquet"]["low_pass_ac"]
+    out = run(_write_case(tmp_path, case), solver_factory=OracleSolver)
+    t = pq.read_table(out)
+    ref = case["columns"]
+    assert t.column_names == list(ref)
+    for k, v in ref.items():
+        np.testing.assert_allclose(t.column(k).to_numpy(), v, rtol=1e-12, atol=1e-15)
+
+
+def test_transient_and_dc_writers_put_keys_in_order(tmp_path):
+    pq = pytest.importorskip("pyarrow.parquet")
+    from krets_gb300.results import write_dc_results_to_parquet, write_tran_results_to_parquet
+    rows = [{"V(b)": 1.0, "time": 0.0, "I(V1)": 2.0}, {"V(b)": 3.0, "time": 1e-3}]
+    name = write_tran_results_to_parquet(rows, tmp_path / "tran")
+    t = pq.read_table(name)
+    assert name.endswith(".parquet") and t.column_names == ["time", "I(V1)", "V(b)"]
+    assert t.column("I(V1)").to_pylist() == [2.0, None]
+    t = pq.read_table(write_dc_results_to_parquet([{"step": 0.0, "V(a)": 1.5}], tmp_path / "dc.parquet"))
+    assert t.column_names == ["V(a)", "step"]
