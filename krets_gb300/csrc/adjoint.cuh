@@ -42,9 +42,9 @@ __device__ __forceinline__ df df_trow(const int4 d, const int2 *ent, const df *_
   df s = sub == 0 ? z[r] : df{0.f, 0.f};
   for (int e = d.y + sub; e < d.y + cnt; e += spl) {
     const int2 en = ent[e];
-    s = df_fma(df_neg(lu[en.x]), z[en.y], s);
+    s = df_fma_acc(df_neg(lu[en.x]), z[en.y], s);
   }
-  return s;
+  return df_norm(s);
 }
 
 // One level of a transposed solve: rows split over `spl` lanes as in df_level_split, or,
@@ -90,11 +90,11 @@ __device__ __forceinline__ void df_tsolve(const int *T, const int *toff, int nut
   const int2 *ent = reinterpret_cast<const int2 *>(T + toff[4]);
   const int *ut_max = T + toff[6], *lt_max = T + toff[7];
   for (int l = 0; l < nut; ++l) {
-    df_tlevel<true>(ut_ptr, ut_desc, ent, l, lu, z, gl, G, split_lanes<G>(ut_ptr[l + 1] - ut_ptr[l], ut_max[l]));
+    df_tlevel<true>(ut_ptr, ut_desc, ent, l, lu, z, gl, G, split_lanes<G>(ut_max[l]));
     gsync<G>(gid);
   }
   for (int l = 0; l < nlt; ++l) {
-    df_tlevel<false>(lt_ptr, lt_desc, ent, l, lu, z, gl, G, split_lanes<G>(lt_ptr[l + 1] - lt_ptr[l], lt_max[l]));
+    df_tlevel<false>(lt_ptr, lt_desc, ent, l, lu, z, gl, G, split_lanes<G>(lt_max[l]));
     gsync<G>(gid);
   }
 }

@@ -139,6 +139,19 @@ __device__ __forceinline__ df df_fma(df a, df b, df acc) {
   return fast_two_sum(s.hi, s.lo);
 }
 
+// acc + a * b with the result left unnormalised: hi is the rounded running sum (TwoSum
+// keeps every step exact), lo collects the error terms.  For dot products over a row;
+// df_norm() renormalises once at the end (TwoSum, so |lo| > |hi| is also handled).
+__device__ __forceinline__ df df_fma_acc(df a, df b, df acc) {
+  df p = two_prod(a.hi, b.hi);
+  p.lo = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, p.lo));
+  df s = two_sum(acc.hi, p.hi);
+  s.lo = __fadd_rn(s.lo, __fadd_rn(acc.lo, p.lo));
+  return s;
+}
+
+__device__ __forceinline__ df df_norm(df a) { return two_sum(a.hi, a.lo); }
+
 // acc - x (x exact +-1 multiple: incidence entries of the MNA matrix)
 __device__ __forceinline__ float df_approx(df a) { return __fadd_rn(a.hi, a.lo); }
 

@@ -382,12 +382,31 @@ std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<in
 //   [4] lu_col[nnz_lu] as uint16 pairs
 //   [7] dyn[ndyn] int4 {e | kind << 24, p, m, b} (positions, -1 absent)
 //   [8] bd_ptr[n+1]   [9] bd_op (dyn << 1 | neg)   [10] qinv[n]
-//   [12] lmax[nlev], [13] umax[nulev]: longest row of each L / U level (off-diagonal entries)
+//   [12] lmax[nlev], [13] umax[nulev]: split code of each L / U level (split_code: lanes per
+//        row by group size, longest row)
 //   [5] res_row[n] int2 {first op, n_unit | n_total << 16}
 //   [6] res_op: col | neg << 15 | slot << 16 (slot 0 = incidence +-1 entries, listed first;
 //       slot e+1 = coefficient of element e)
 //   [11] end
 // (in this physical order: sp_off[5] ends the part that the direct engines stage)
+// Per-level split code: bits 3g..3g+2 hold log2 of the lanes per row a group of 32 << g
+// threads uses (g = 0..4), bits 16.. the longest row (clamped).  A level's rows are
+// split over more lanes while a row has more than two entries per lane and the level
+// still fits the group (the device reads the code; the rule lives here only).
+static int split_code(int rows, int mx) {
+  int code = std::min(mx, 65535) << 16;
+  for (int g = 0; g < 5; ++g) {
+    const int G = 32 << g;
+    int s = 1, lg = 0;
+    while (s < 8 && mx > 2 * s && rows * s * 2 <= G) {
+      s *= 2;
+      ++lg;
+    }
+    code |= lg << (3 * g);
+  }
+  return code;
+}
+
 static void pack_step_program(const krets_element *el, Program &P) {
   const int n = P.n;
   P.sprog.clear();
@@ -448,7 +467,7 @@ static void pack_step_program(const krets_element *el, Program &P) {
       const int k = P.lev_rows[t];
       mx = std::max(mx, lcount(k));
     }
-    S.push_back(mx);
+    S.push_back(split_code(P.lev_ptr[l + 1] - P.lev_ptr[l], mx));
   }
   mark(13);
   for (size_t l = 0; l + 1 < P.ulev_ptr.size(); ++l) {
@@ -457,7 +476,7 @@ static void pack_step_program(const krets_element *el, Program &P) {
       const int k = P.ulev_rows[t];
       mx = std::max(mx, P.lu_rowptr[k + 1] - P.lu_diag[k] - 1);
     }
-    S.push_back(mx);
+    S.push_back(split_code(P.ulev_ptr[l + 1] - P.ulev_ptr[l], mx));
   }
   // the residual operators come last: the direct engines stage only the words before them
   mark(5);
@@ -487,7 +506,7 @@ static void pack_step_program(const krets_element *el, Program &P) {
 // U(k,j) != 0; L^T row k waits for the rows j > k with L(j,k) != 0.  Sections, in order:
 //   [0] ut_ptr[nut+1]  [1] ut_desc[n] int4 {row | cnt << 16, first entry, diagonal slot, 0}
 //   [2] lt_ptr[nlt+1]  [3] lt_desc[n] int4 {row | cnt << 16, first entry, -1, 0}
-//   [6] utmax[nut], [7] ltmax[nlt]: longest row of each level
+//   [6] utmax[nut], [7] ltmax[nlt]: split code of each level (split_code)
 //   [4] entries int2 {LU slot, position}   [5] end
 static void pack_transposed_program(Program &P) {
   const int n = P.n;
@@ -541,10 +560,14 @@ static void pack_transposed_program(Program &P) {
   for (int pass = 0; pass < 2; ++pass) {
     const std::vector<int> &lv = pass ? llev : ulev;
     const auto &rows = pass ? lt : ut;
-    std::vector<int> mx(pass ? nl : nu, 0);
-    for (int k = 0; k < n; ++k) mx[lv[k]] = std::max(mx[lv[k]], (int)rows[k].size());
+    const int nlev = pass ? nl : nu;
+    std::vector<int> mx(nlev, 0), cnt(nlev, 0);
+    for (int k = 0; k < n; ++k) {
+      mx[lv[k]] = std::max(mx[lv[k]], (int)rows[k].size());
+      cnt[lv[k]]++;
+    }
     mark(6 + pass);
-    T.insert(T.end(), mx.begin(), mx.end());
+    for (int l = 0; l < nlev; ++l) T.push_back(split_code(cnt[l], mx[l]));
   }
   mark(4);
   T.insert(T.end(), ent.begin(), ent.end());

@@ -40,7 +40,7 @@ struct SProg {
   const int *res_op;
   const int4 *dyn;
   const int *bd_ptr, *bd_op, *qinv;
-  const int *lmax, *umax;  // longest row of each L / U level
+  const int *lmax, *umax;  // split code of each L / U level (lanes per row, longest row)
   int nlev, nulev;
   int tail0, tail_m;  // dense trailing block (tail_m = 0: none)
   df *dense_stage;    // 32 x 33 shared-memory tile for diagonal blocks read from global memory (or null)
@@ -867,9 +867,10 @@ __device__ __forceinline__ df df_row(const SProg &S, const df *__restrict__ lu, 
   const df a0 = d.w > 0 ? lu[first] : zero;
   const df a1 = d.w > 1 ? lu[first + 1] : zero;
   df s = y[k];
-  s = df_fma(df_neg(a0), y[c0], s);
-  s = df_fma(df_neg(a1), y[c1], s);
-  for (int j = 2; j < 2 + rest; ++j) s = df_fma(df_neg(lu[first + j]), y[S.lu_col[first + j]], s);
+  s = df_fma_acc(df_neg(a0), y[c0], s);
+  s = df_fma_acc(df_neg(a1), y[c1], s);
+  for (int j = 2; j < 2 + rest; ++j) s = df_fma_acc(df_neg(lu[first + j]), y[S.lu_col[first + j]], s);
+  s = df_norm(s);
   if (UPPER) s = df_mul(s, lu[d.y]);
   return s;
 }
@@ -892,14 +893,12 @@ __device__ __forceinline__ void df_level(const SProg &S, const df *__restrict__ 
   }
 }
 
-// Lanes per row for a level of `rows` rows whose longest row has `mx` entries: rows with
-// more than two entries per lane are split over up to 8 lanes of a warp while the level
-// still fits the group.
+// Lanes per row of a level for a group of G threads, from the level's split code (host
+// symbolic pass: split_code()).
 template <int G>
-__device__ __forceinline__ int split_lanes(int rows, int mx) {
-  int s = 1;
-  while (s < 8 && mx > 2 * s && rows * s * 2 <= G) s *= 2;
-  return s;
+__device__ __forceinline__ int split_lanes(int code) {
+  constexpr int g = G >= 512 ? 4 : G >= 256 ? 3 : G >= 128 ? 2 : G >= 64 ? 1 : 0;
+  return 1 << ((code >> (3 * g)) & 7);
 }
 
 // Sum a double-float over the `spl` aligned lanes of a row (xor butterfly: every lane ends
@@ -928,8 +927,8 @@ __device__ __forceinline__ void df_level_split(const SProg &S, const df *__restr
     const int cnt = d.w + (int)((unsigned)d.x >> 16);
     const int first = UPPER ? d.y + 1 : d.y;
     df s = sub == 0 ? y[k] : df{0.f, 0.f};
-    for (int j = sub; j < cnt; j += spl) s = df_fma(df_neg(lu[first + j]), y[S.lu_col[first + j]], s);
-    s = df_lane_sum(s, spl, mask);
+    for (int j = sub; j < cnt; j += spl) s = df_fma_acc(df_neg(lu[first + j]), y[S.lu_col[first + j]], s);
+    s = df_lane_sum(df_norm(s), spl, mask);
     if (sub == 0) y[k] = UPPER ? df_mul(s, lu[d.y]) : s;
   }
 }
@@ -967,11 +966,11 @@ __device__ __forceinline__ void df_dense_update(const SProg &S, const int4 *td, 
     df s0{0.f, 0.f}, s1{0.f, 0.f};
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      s0 = df_fma(a0[q], yv[q], s0);
-      s1 = df_fma(a1[q], yv[q], s1);
+      s0 = df_fma_acc(a0[q], yv[q], s0);
+      s1 = df_fma_acc(a1[q], yv[q], s1);
     }
-    s0 = df_lane_sum(s0, 8, mask);
-    s1 = df_lane_sum(s1, 8, mask);
+    s0 = df_lane_sum(df_norm(s0), 8, mask);
+    s1 = df_lane_sum(df_norm(s1), 8, mask);
     if (sub == 0) {
       y[t0 + r] = df_sub(y[t0 + r], s0);
       if (two) y[t0 + r + R] = df_sub(y[t0 + r + R], s1);
@@ -1071,7 +1070,7 @@ __device__ __forceinline__ void df_solve(const SProg &S, const df *__restrict__ 
   if (nar < 0) {  // no narrow-level split: every level on the whole group
     if (UPPER && S.tail_m) df_dense_upper<G>(S, lu, y, gl, gid);
     for (int l = UPPER ? 0 : 1; l < nl; ++l) {
-      const int spl = split_lanes<SG>(ptr[l + 1] - ptr[l], mx[l]);
+      const int spl = split_lanes<SG>(mx[l]);
       if (spl > 1) df_level_split<UPPER>(S, lu, y, ptr, desc, l, gl, G, spl);
       else df_level<G, UPPER>(S, lu, y, ptr, desc, l, gl, G);
       gsync<G>(gid);
