@@ -104,8 +104,8 @@ __device__ __forceinline__ void df_tsolve(const int *T, const int *toff, int nut
 // recomputation for its half, so recomputed states match the forward pass's to rounding).
 template <int G, int SG>
 __device__ __forceinline__ void adj_forward_step(const DevProg &P, const SProg &S, const df *lu, df *x, const df *cdyn,
-                                                 df *cb, df *icap, const double *vals, int method, double t_src,
-                                                 int gl, int gid) {
+                                                 df *cb, df *icap, const double *vals, int method, int step, double h,
+                                                 const WaveTab &wt, int gl, int gid) {
   for (int d = gl; d < P.ndyn; d += G) {
     const int4 dd = S.dyn[d];
     const int kind = (int)((unsigned)dd.x >> 24);
@@ -119,7 +119,10 @@ __device__ __forceinline__ void adj_forward_step(const DevProg &P, const SProg &
     } else if (kind == KRETS_ELEM_V) {
       const int e = dd.x & 0xffffff;
       const krets_element &E = P.el[e];
-      v = df_from_double(wave_value(E, vals ? vals[e] : E.value, t_src));
+      const int wr = wt.tab ? wt.row[d] : -1;
+      if (wr >= 0) v = df_from_double(wt.tab[(size_t)wr * wt.stride + step]);
+      else if (E.wave == KRETS_WAVE_NONE) v = cdyn[d];
+      else v = df_from_double(wave_value(E, vals ? vals[e] : E.value, (double)step * h));
     } else if (kind == KRETS_ELEM_I) {
       v = cdyn[d];
     }
@@ -177,7 +180,7 @@ template <int RK, int RD, int RE>
 __global__ void __launch_bounds__(kAdjThreads, 1)
     k_adjoint_dfd(DevProg P, AdjLay L, const double *values, int n_inst, double h, int n_steps, int method, int K,
                   int out_pos, const int4 *adj, const int *cc_ptr, const int *cc_op, df *ckpt, df *seg, df *hist,
-                  double *loss_out, double *grad_out, int *inst_status, int *queue, int mode) {
+                  double *loss_out, double *grad_out, int *inst_status, int *queue, int mode, WaveTab wt) {
   constexpr int GF = kAdjThreads, GH = kAdjHalf;
   extern __shared__ __align__(16) char smem[];
   const int tid = threadIdx.x;
@@ -268,7 +271,7 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
       }
       if (mode == 1 && s - 1 == last0)
         for (int k = tid; k < n; k += GF) last_seg[k] = x[k];
-      adj_forward_step<GF, GF>(P, S, lu, x, cdyn, cb, icap, vals, method, (double)s * h, tid, 0);
+      adj_forward_step<GF, GF>(P, S, lu, x, cdyn, cb, icap, vals, method, s, h, wt, tid, 0);
       if (tid == 0) loss = df_fma(x[out_pos], x[out_pos], loss);
       if (mode == 1 && s > last0)
         for (int k = tid; k < n; k += GF) last_seg[(size_t)(s - last0) * n + k] = x[k];
@@ -417,7 +420,7 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
             for (int d = hl; d < P.ncap; d += GH) icap[d] = ck[n + d];
             gsync<GH>(2);
             for (int s = s0 + 1; s <= s1; ++s) {
-              adj_forward_step<GH, GH>(P, S, lu, x, cdyn, cb, icap, vals, method, (double)s * h, hl, 2);
+              adj_forward_step<GH, GH>(P, S, lu, x, cdyn, cb, icap, vals, method, s, h, wt, hl, 2);
               for (int k = hl; k < n; k += GH) sg[(size_t)(s - s0) * n + k] = x[k];
             }
           }

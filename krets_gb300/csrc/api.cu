@@ -827,7 +827,7 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
   if (s != KRETS_OK) return s;
   CU(cudaEventRecord(c->ev[0], c->stream));
   size_t stride = (size_t)c->n * ((size_t)n_steps + 1);
-  DevBuf tv, tx, ts, tfb;
+  DevBuf tv, tx, ts, tfb, twave;
   void *dv, *dx;
   s = dev_view(values, sizeof(double) * c->ne * (size_t)n_inst, true, c->stream, tv, &dv);
   if (s) return s;
@@ -896,7 +896,8 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
     const size_t smem = DL.sprog_bytes + (size_t)W * DL.bytes;
     const char *oenv = getenv("KRETS_DFD_OPTS");
     const int opts = oenv ? atoi(oenv) : 0;
-    void (*kd)(DevProg, KCfg, DfdLay, const double *, int, double, int, int, int, double *, int *, int *, int) =
+    void (*kd)(DevProg, KCfg, DfdLay, const double *, int, double, int, int, int, double *, int *, int *, int,
+               WaveTab) =
         G == 32 ? k_tran_dfd<32> : (G == 64 ? k_tran_dfd<64> : k_tran_dfd<128>);
     CU(cudaFuncSetAttribute(kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
@@ -905,9 +906,33 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
     int grid = std::max(1, std::min((n_inst + W - 1) / W, per_sm * device_sm_count()));
     c->warps_per_cta = W * G / 32;
     c->grid = grid;
+    // PULSE / SIN sources tabulated per step (their parameters are not per-instance values)
+    const Program &H = Dtr->host;
+    std::vector<int> wrow(P.ndyn, -1), wsrc;
+    for (int d = 0; d < P.ndyn; ++d) {
+      const krets_element &E = c->el[H.dyn_e[d]];
+      if (E.kind == KRETS_ELEM_V && E.wave != KRETS_WAVE_NONE) {
+        wrow[d] = (int)wsrc.size();
+        wsrc.push_back(H.dyn_e[d]);
+      }
+    }
+    WaveTab wt{nullptr, nullptr, n_steps + 1};
+    if (!wsrc.empty()) {
+      const size_t tab_bytes = sizeof(double) * wsrc.size() * (size_t)(n_steps + 1);
+      CU(cudaMalloc(&twave.p, tab_bytes + sizeof(int) * (wrow.size() + wsrc.size())));
+      int *d_wrow = (int *)((char *)twave.p + tab_bytes), *d_wsrc = d_wrow + wrow.size();
+      CU(cudaMemcpyAsync(d_wrow, wrow.data(), sizeof(int) * wrow.size(), cudaMemcpyHostToDevice, c->stream));
+      CU(cudaMemcpyAsync(d_wsrc, wsrc.data(), sizeof(int) * wsrc.size(), cudaMemcpyHostToDevice, c->stream));
+      k_wave_table<<<256, 256, 0, c->stream>>>(c->d_el, d_wsrc, (int)wsrc.size(), h, n_steps, source_lag,
+                                              (double *)twave.p);
+      g_launches++;
+      CU(cudaGetLastError());
+      wt.tab = (const double *)twave.p;
+      wt.row = d_wrow;
+    }
     CU(cudaEventRecord(c->ev[2], c->stream));
     kd<<<grid, G * W, smem, c->stream>>>(P, c->cfg, DL, (const double *)dv, n_inst, h, n_steps, method, source_lag,
-                                        (double *)dx, d_st, queue, opts);
+                                        (double *)dx, d_st, queue, opts, wt);
   } else if (warp_engine) {
     const char *bud = getenv("KRETS_SMEM_BUDGET");
     size_t budget = bud ? (size_t)atol(bud) : max_smem_optin();
@@ -1103,11 +1128,36 @@ krets_status krets_adjoint_tran(krets_circuit *c, int32_t n_inst, const double *
   CU(cudaMemsetAsync(tst.p, 0, sizeof(int) * n_inst, c->stream));
   int *queue = c->d_small + 8;
   CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
+  // PULSE / SIN sources tabulated per step (sources at t_n, no lag)
+  DevBuf twave;
+  WaveTab wt{nullptr, nullptr, n_steps + 1};
+  {
+    std::vector<int> wrow(P.ndyn, -1), wsrc;
+    for (int d = 0; d < P.ndyn; ++d) {
+      const krets_element &E = c->el[H.dyn_e[d]];
+      if (E.kind == KRETS_ELEM_V && E.wave != KRETS_WAVE_NONE) {
+        wrow[d] = (int)wsrc.size();
+        wsrc.push_back(H.dyn_e[d]);
+      }
+    }
+    if (!wsrc.empty()) {
+      const size_t tab_bytes = sizeof(double) * wsrc.size() * (size_t)(n_steps + 1);
+      CU(cudaMalloc(&twave.p, tab_bytes + sizeof(int) * (wrow.size() + wsrc.size())));
+      int *d_wrow = (int *)((char *)twave.p + tab_bytes), *d_wsrc = d_wrow + wrow.size();
+      CU(cudaMemcpyAsync(d_wrow, wrow.data(), sizeof(int) * wrow.size(), cudaMemcpyHostToDevice, c->stream));
+      CU(cudaMemcpyAsync(d_wsrc, wsrc.data(), sizeof(int) * wsrc.size(), cudaMemcpyHostToDevice, c->stream));
+      k_wave_table<<<256, 256, 0, c->stream>>>(c->d_el, d_wsrc, (int)wsrc.size(), h, n_steps, 0, (double *)twave.p);
+      g_launches++;
+      CU(cudaGetLastError());
+      wt.tab = (const double *)twave.p;
+      wt.row = d_wrow;
+    }
+  }
   CU(cudaEventRecord(c->ev[2], c->stream));
   ka<<<grid, kAdjThreads, smem, c->stream>>>(P, AL, (const double *)dv, n_inst, h, n_steps, method, K,
                                              H.qinv[out_unknown], (const int4 *)d_adj, d_ccp, d_cco, (df *)tck.p,
                                              (df *)tseg.p, d_hist, (double *)d_loss, (double *)d_grad, (int *)tst.p,
-                                             queue, gradient ? 1 : 0);
+                                             queue, gradient ? 1 : 0, wt);
   g_launches++;
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[3], c->stream));

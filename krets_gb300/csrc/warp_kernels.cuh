@@ -1151,10 +1151,34 @@ __device__ __forceinline__ int dfd_setup(const DevProg &P, const SProg &S, const
 
 // Transient steps 1..n_steps of one instance from the state in x (position space), rows
 // of `out` (original unknown order, n per row) written with streaming stores.
+// Source waveforms tabulated per step (k_wave_table): row wrow[d] of wtab holds the
+// value of rhs element d's PULSE/SIN source at the source time of every step, so the
+// step loop reads one value instead of evaluating fmod and divisions on the FP64 pipe
+// (a latency on every step's critical path).  Without a table the waveform is evaluated.
+struct WaveTab {
+  const double *tab;  // [rows][n_steps + 1]
+  const int *row;     // [ndyn]: row of a tabulated source, -1 otherwise
+  int stride;         // n_steps + 1
+};
+
+// value of every PULSE / SIN source at each step's source time (transient.rs:49 timing
+// when lag is set), same expression as the step loop's wave_value call
+__global__ void k_wave_table(const krets_element *el, const int *src_elem, int n_src, double h, int n_steps, int lag,
+                             double *tab) {
+  const long long total = (long long)n_src * (n_steps + 1);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / (n_steps + 1)), s = (int)(i % (n_steps + 1));
+    const double t_src = lag ? (double)(s - 1) * h : (double)s * h;
+    const krets_element &E = el[src_elem[r]];
+    tab[i] = wave_value(E, E.value, t_src);
+  }
+}
+
 template <int G>
 __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const df *lu, df *x, const df *cdyn, df *cb,
                                          df *icap, const double *vals, double h, int n_steps, int method, int lag,
-                                         double *out, int lnar, int unar, bool int_cvt, int gl, int gid) {
+                                         double *out, int lnar, int unar, bool int_cvt, int gl, int gid,
+                                         WaveTab wt = WaveTab{nullptr, nullptr, 0}) {
   int st = 0;
   for (int s = 1; s <= n_steps; ++s) {
     const double t = (double)s * h;
@@ -1172,7 +1196,10 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
       } else if (kind == KRETS_ELEM_V) {
         const int e = dd.x & 0xffffff;
         const krets_element &E = P.el[e];
-        v = df_from_double(wave_value(E, vals ? vals[e] : E.value, t_src));
+        const int wr = wt.tab ? wt.row[d] : -1;
+        if (wr >= 0) v = df_from_double(wt.tab[(size_t)wr * wt.stride + s]);
+        else if (E.wave == KRETS_WAVE_NONE) v = cdyn[d];  // the DC value, split at set-up
+        else v = df_from_double(wave_value(E, vals ? vals[e] : E.value, t_src));
       } else if (kind == KRETS_ELEM_I) {
         v = cdyn[d];
       }
@@ -1213,7 +1240,7 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
 template <int G>
 __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay L, const double *values, int n_inst,
                                                      double h, int n_steps, int method, int lag, double *x_out,
-                                                     int *inst_status, int *queue, int opts) {
+                                                     int *inst_status, int *queue, int opts, WaveTab wt) {
   extern __shared__ __align__(16) char smem[];
   const int gl = threadIdx.x % G, gid = threadIdx.x / G;
   {
@@ -1252,7 +1279,7 @@ __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
     for (int d = gl; d < P.ncap; d += G) icap[d] = df{0.f, 0.f};
     const bool fatal = gany<G>((st & (KS_SINGULAR | KS_NONFINITE | KS_NOTIMPL)) != 0, gid);
     if (!fatal) st |= dfd_steps<G>(P, S, lu, x, cdyn, cb, icap, vals, h, n_steps, method, lag, out, lnar, unar, int_cvt,
-                                   gl, gid);
+                                   gl, gid, wt);
     if (gl == 0) slot[1] = 0;
     gsync<G>(gid);
     if (st) atomicOr(&slot[1], st);
