@@ -1231,7 +1231,10 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
       if (!isfinite(v)) st |= KS_NONFINITE;
       __stcs(row + k, v);
     }
-    gsync<G>(gid);
+    // no barrier: the next step's first phase reads x (final since the last solve level)
+    // and writes only this thread's cb / reads this thread's icap entries; its barrier
+    // orders every read of x before the gather overwrites it.  Callers synchronise the
+    // group after the last step.
   }
   return st;
 }
