@@ -45,6 +45,7 @@ SEED = 3
 METRIC = "circuit-timesteps/sec batched vs plain GPU form at <=1e-9 rel err vs FP64"
 UNIT = "circuit-timesteps/s"
 WORKLOAD = "mc_transient_rlc_ladder_2048x200sec_tr_1ps_10000steps"
+TRAFFIC_PER_CIRCUIT_STEP = (1.403939e9 + 3.843072e6) / (304 * 1000)  # bytes, ncu capture
 
 
 def dist_env():
@@ -279,6 +280,9 @@ def run_ours(args, rank, world):
 
     # roofline of the dominant kernel (the batched transient)
     alg_bytes = out_bytes - N_INST * n * 8 + vals.nbytes + N_INST * n * 8  # rows 1..N written, inputs read
+    # DRAM bytes per circuit-step of k_tran_dfd from an ncu capture of 304 instances x
+    # 1000 steps (profiles/k_tran_dfd_mc_transient_304x1000.md), scaled to this launch
+    traffic = TRAFFIC_PER_CIRCUIT_STEP * N_INST * N_STEPS
     k_s = statistics.mean(kern_ms) / 1e3
     peak, peak_kind = measured_peak_hbm()
     achieved = alg_bytes / k_s / 1e9
@@ -328,7 +332,8 @@ def run_ours(args, rank, world):
         "plain_form": {"value": plain_rate, "unit": UNIT, "what": "1 instance, FP64, per-step kernels (CUDA graph)"},
         "batched_over_plain": value / plain_rate,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "traffic_note": "ncu DRAM bytes of a 304 x 1000-step capture scaled per circuit-step",
                      "kernel": "k_tran_dfd<128>", "algorithmic_bytes_per_launch": alg_bytes},
         "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{n_sample} instances x {N_STEPS} TR steps, factor once, oracle/ C restatement"},
