@@ -119,12 +119,44 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def workload():
+# ------------------------------------------------------------------ replicas (N > 1)
+def select_device(local):
+    """One GPU per rank: restrict the process to its GPU before the first CUDA call (the
+    library uses the current device); an inherited device list is indexed by local rank."""
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    devs = [d for d in vis.split(",") if d.strip()] if vis else []
+    os.environ["CUDA_VISIBLE_DEVICES"] = devs[local % len(devs)] if devs else str(local)
+    return os.environ["CUDA_VISIBLE_DEVICES"]
+
+
+def shard_seed(rank):
+    """Seed of a rank's instances: each rank runs its own shard of a larger Monte Carlo
+    job (weak scaling), so no two ranks repeat the same values."""
+    return SEED + 7919 * rank
+
+
+def max_over_ranks(seconds, world):
+    """The job's time is the slowest rank's (gloo all-reduce; no data-path collective)."""
+    if world <= 1:
+        return seconds
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([seconds], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, steps, world, seconds):
+    """Whole-job throughput: the units every rank processed over the slowest rank's time."""
+    return units_per_rank * steps * world / seconds
+
+
+def workload(rank=0):
     from krets_gb300.generators import monte_carlo_values, rlc_ladder
     from krets_gb300.table import element_table
     c = rlc_ladder(SECTIONS)
     t = element_table(c)
-    vals = monte_carlo_values(c, N_INST, sigma=0.1, seed=SEED)
+    vals = monte_carlo_values(c, N_INST, sigma=0.1, seed=shard_seed(rank))
     return c, t, vals
 
 
@@ -195,7 +227,7 @@ def run_ours(args, rank, world):
     from krets_gb300 import _lib
     from krets_gb300.table import is_current_mask
 
-    c, t, vals = workload()
+    c, t, vals = workload(rank)
     n = c.size
     g = _lib.GpuCircuit(t, n)
     d_vals = _lib.DeviceArray(vals.shape).upload(vals)
@@ -226,15 +258,9 @@ def run_ours(args, rank, world):
     if world > 1:
         dist.barrier()
     launches = _lib.launch_count() - l0
-    total_s = sum(call_ms) / 1e3
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([total_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
+    total_s = max_over_ranks(sum(call_ms) / 1e3, world)
     ctsteps = N_INST * N_STEPS
-    value = ctsteps * args.steps * world / total_s
+    value = job_rate(ctsteps, args.steps, world, total_s)
 
     # accuracy: sampled instances against the FP64 oracle over the full 10000 steps
     from oracle import oracle as O
@@ -649,7 +675,7 @@ def main():
     if world > 1:
         # replicas: one process per GPU, instances sharded by replica, no data-path collective;
         # the process group is only for the barrier and the max-over-ranks time
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+        select_device(local)
         import torch.distributed as dist
         dist.init_process_group("gloo")
     if args.workload != "mc_transient":
