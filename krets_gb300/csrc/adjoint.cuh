@@ -70,7 +70,7 @@ __device__ __forceinline__ void df_tlevel(const int *ptr, const int4 *desc, cons
     return;
   }
   const int sub = gl & (spl - 1);
-  const unsigned mask = ((1u << spl) - 1u) << ((threadIdx.x & 31) & ~(spl - 1));
+  const unsigned mask = lane_mask(spl);
   for (int t = r0 + gl / spl; t < r1; t += nthreads / spl) {
     const int4 d = desc[t];
     df s = df_lane_sum(df_trow(d, ent, lu, z, sub, spl), spl, mask);

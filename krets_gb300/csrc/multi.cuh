@@ -123,8 +123,8 @@ __global__ void __launch_bounds__(512, 1)
           x[k] = acc;
         }
         gsync<G>(gid);
-        df_solve<G, false>(S, lu, x, gl, gid, -1);
-        df_solve<G, true>(S, lu, x, gl, gid, -1);
+        df_solve<G, false, GLOBAL ? 0 : G>(S, lu, x, gl, gid, -1);
+        df_solve<G, true, GLOBAL ? 0 : G>(S, lu, x, gl, gid, -1);
         for (int k = gl; k < P.n; k += G) {
           const double v = df_to_double(x[S.qinv[k]]);
           if (!isfinite(v)) st |= KS_NONFINITE;
@@ -135,7 +135,8 @@ __global__ void __launch_bounds__(512, 1)
         for (int k = gl; k < P.n; k += G) x[k] = df_from_double(out[P.q[k]]);
         for (int d = gl; d < P.ncap; d += G) icap[d] = df{0.f, 0.f};
         gsync<G>(gid);
-        st |= dfd_steps<G>(P, S, lu, x, cdyn, cb, icap, nullptr, h, n_steps, method, lag, out, -1, -1, false, gl, gid);
+        st |= dfd_steps<G, GLOBAL ? 0 : G>(P, S, lu, x, cdyn, cb, icap, nullptr, h, n_steps, method, lag, out, -1, -1,
+                                          false, gl, gid);
       }
     }
     if (gl == 0) slot[1] = 0;

@@ -390,15 +390,17 @@ std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<in
 //   [11] end
 // (in this physical order: sp_off[5] ends the part that the direct engines stage)
 // Per-level split code: bits 3g..3g+2 hold log2 of the lanes per row a group of 32 << g
-// threads uses (g = 0..4), bits 16.. the longest row (clamped).  A level's rows are
-// split over more lanes while a row has more than two entries per lane and the level
-// still fits the group (the device reads the code; the rule lives here only).
+// threads uses (g = 0..4, up to 8 lanes), bits 15..17 the same for a 256-thread group
+// allowed a whole warp per row (the multi-circuit engine's global-memory class, whose
+// long rows read global memory), bits 18.. the longest row (clamped).  A level's rows
+// are split over more lanes while a row has more than two entries per lane and the level
+// still fits the group.  The device reads the code; the rule lives here only.
 static int split_code(int rows, int mx) {
-  int code = std::min(mx, 65535) << 16;
-  for (int g = 0; g < 5; ++g) {
-    const int G = 32 << g;
+  int code = std::min(mx, 16383) << 18;
+  for (int g = 0; g < 6; ++g) {
+    const int G = g == 5 ? 256 : 32 << g, cap = g == 5 ? 32 : 8;
     int s = 1, lg = 0;
-    while (s < 8 && mx > 2 * s && rows * s * 2 <= G) {
+    while (s < cap && mx > 2 * s && rows * s * 2 <= G) {
       s *= 2;
       ++lg;
     }

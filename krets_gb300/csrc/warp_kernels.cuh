@@ -895,10 +895,16 @@ __device__ __forceinline__ void df_level(const SProg &S, const df *__restrict__ 
 
 // Lanes per row of a level for a group of G threads, from the level's split code (host
 // symbolic pass: split_code()).
+// G = 0: the wide 256-thread split (a warp per row allowed)
 template <int G>
 __device__ __forceinline__ int split_lanes(int code) {
-  constexpr int g = G >= 512 ? 4 : G >= 256 ? 3 : G >= 128 ? 2 : G >= 64 ? 1 : 0;
+  constexpr int g = G == 0 ? 5 : G >= 512 ? 4 : G >= 256 ? 3 : G >= 128 ? 2 : G >= 64 ? 1 : 0;
   return 1 << ((code >> (3 * g)) & 7);
+}
+
+// lanes of this thread's aligned group of spl lanes (spl a power of two <= 32)
+__device__ __forceinline__ unsigned lane_mask(int spl) {
+  return spl >= 32 ? 0xffffffffu : ((1u << spl) - 1u) << ((threadIdx.x & 31) & ~(spl - 1));
 }
 
 // Sum a double-float over the `spl` aligned lanes of a row (xor butterfly: every lane ends
@@ -920,14 +926,25 @@ __device__ __forceinline__ void df_level_split(const SProg &S, const df *__restr
                                                const int4 *desc, int l, int tid, int nthreads, int spl) {
   const int r0 = ptr[l], r1 = ptr[l + 1];
   const int sub = tid & (spl - 1);
-  const unsigned mask = ((1u << spl) - 1u) << ((threadIdx.x & 31) & ~(spl - 1));
+  const unsigned mask = lane_mask(spl);
   for (int t = r0 + tid / spl; t < r1; t += nthreads / spl) {
     const int4 d = desc[t];
     const int k = d.x & 0xffff;
     const int cnt = d.w + (int)((unsigned)d.x >> 16);
     const int first = UPPER ? d.y + 1 : d.y;
     df s = sub == 0 ? y[k] : df{0.f, 0.f};
-    for (int j = sub; j < cnt; j += spl) s = df_fma_acc(df_neg(lu[first + j]), y[S.lu_col[first + j]], s);
+    int j = sub;
+    for (; j + 3 * spl < cnt; j += 4 * spl) {  // four entries' loads in flight
+      df a[4], v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        a[q] = lu[first + j + q * spl];
+        v[q] = y[S.lu_col[first + j + q * spl]];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) s = df_fma_acc(df_neg(a[q]), v[q], s);
+    }
+    for (; j < cnt; j += spl) s = df_fma_acc(df_neg(lu[first + j]), y[S.lu_col[first + j]], s);
     s = df_lane_sum(df_norm(s), spl, mask);
     if (sub == 0) y[k] = UPPER ? df_mul(s, lu[d.y]) : s;
   }
@@ -1174,7 +1191,7 @@ __global__ void k_wave_table(const krets_element *el, const int *src_elem, int n
   }
 }
 
-template <int G>
+template <int G, int SG = G>
 __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const df *lu, df *x, const df *cdyn, df *cb,
                                          df *icap, const double *vals, double h, int n_steps, int method, int lag,
                                          double *out, int lnar, int unar, bool int_cvt, int gl, int gid,
@@ -1215,8 +1232,8 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
       x[k] = acc;
     }
     gsync<G>(gid);
-    df_solve<G, false>(S, lu, x, gl, gid, lnar);
-    df_solve<G, true>(S, lu, x, gl, gid, unar);
+    df_solve<G, false, SG>(S, lu, x, gl, gid, lnar);
+    df_solve<G, true, SG>(S, lu, x, gl, gid, unar);
     if (method == KRETS_METHOD_TR) {
       for (int d = gl; d < P.ncap; d += G) {
         const int4 dd = S.dyn[d];

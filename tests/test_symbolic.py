@@ -75,8 +75,8 @@ def test_transposed_program_solves_adjoint_systems(built_lib, oracle_lib, sectio
         rows = desc[:, 0] & 0xffff
         assert sorted(rows) == list(range(n))
         cnt, first = desc[:, 0] >> 16, desc[:, 1]
-        mx = T[off[msec]:off[msec] + nlev]        # split codes: longest row in bits 16..
-        assert all(mx[l] >> 16 == cnt[ptr[l]:ptr[l + 1]].max() for l in range(nlev))
+        mx = T[off[msec]:off[msec] + nlev]        # split codes: longest row in bits 18..
+        assert all(mx[l] >> 18 == cnt[ptr[l]:ptr[l + 1]].max() for l in range(nlev))
         assert np.all(first + cnt <= (off[5] - off[4]) // 2)
         if upper:
             assert np.all((desc[:, 2] >= 0) & (desc[:, 2] < nnz))
