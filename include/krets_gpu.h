@@ -278,7 +278,9 @@ krets_status krets_batch_tran_noalloc(krets_circuit *c, int32_t n_inst, const do
 #define KRETS_PROG_EL_POS 19
 #define KRETS_PROG_META 20 /* {ordering, n, nnz_a, nnz_lu, n_levels, n_ulevels, factor_flops, tail0, tail_m} */
 #define KRETS_PROG_TPROG 21 /* transposed-solve program (transient mode) */
-#define KRETS_PROG_TPOFF 22 /* its section offsets (6) and level counts of U^T and L^T */
+#define KRETS_PROG_TPOFF 22 /* its section offsets (8) and level counts of U^T and L^T */
+#define KRETS_PROG_SPROG 23 /* compact step program staged in shared memory */
+#define KRETS_PROG_SPOFF 24 /* its section offsets (16), border chunk and row counts */
 #define KRETS_MODE_DC 0
 #define KRETS_MODE_AC 1
 #define KRETS_MODE_TRAN 2

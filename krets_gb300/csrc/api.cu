@@ -229,7 +229,9 @@ static void place_program(const Program &H, const ProgramImage &X, const krets_e
   V.ndyn = (int)H.dyn_e.size();
   V.ncap = H.ncap;
   V.n_resop = (int)H.res_op.size() / 2;
-  for (int k = 0; k < 14; ++k) V.sp_off[k] = H.sp_off[k];
+  for (int k = 0; k < 16; ++k) V.sp_off[k] = H.sp_off[k];
+  V.n_bchunk = H.n_bchunk;
+  V.n_brow = H.n_brow;
   V.sprog_ok = H.sprog_ok;
   for (int k = 0; k < 8; ++k) V.tp_off[k] = H.tp_off[k];
   V.n_utlev = H.n_utlev;
@@ -1473,8 +1475,8 @@ krets_status krets_multi_create(int32_t n_circuits, const krets_element *elems, 
     long long a = 0, g = 0;
     for (int ph = 0; ph < 2; ++ph) {
       const DevProg &V = views[2 * c + ph];
-      a = std::max<long long>(a, multi_lay(V.nnz_lu, V.n, V.ndyn, V.ncap, V.ne, V.sp_off[5]).bytes);
-      g = std::max<long long>(g, multi_lay(V.nnz_lu, V.n, V.ndyn, V.ncap, V.ne, 0).bytes);
+      a = std::max<long long>(a, multi_lay(V.nnz_lu, V.n, V.ndyn, V.ncap, V.ne, V.sp_off[5], V.n_bchunk).bytes);
+      g = std::max<long long>(g, multi_lay(V.nnz_lu, V.n, V.ndyn, V.ncap, V.ne, 0, V.n_bchunk).bytes);
     }
     need[c] = a;
     need_g[c] = g;
@@ -1505,16 +1507,27 @@ krets_status krets_multi_create(int32_t n_circuits, const krets_element *elems, 
     k.grid = std::max(1, std::min(((int)k.items.size() + k.W - 1) / k.W, per_sm * device_sm_count()));
     if (k.global) {
       gscratch_bytes = k.region * k.grid * k.W;
-      // shared memory of a global-class group: staging tile, then x and the rhs
-      // coefficients when the largest circuit's fit in half an SM's shared memory
-      long long xb = 0;
+      // shared memory of a global-class group (half an SM's, two groups per SM): during the
+      // steps a staging tile, x and the rhs coefficients, with the dense-block row slots at
+      // the end; during the set-up the same bytes hold the factorisation's row staging
+      // (8 warps x (dense row + sparse row)) or its tiles.  Without room for the step
+      // layout, x stays in global memory.
+      long long need = 0;
       for (int c : k.items)
         for (int ph = 0; ph < 2; ++ph) {
           const DevProg &V = views[2 * c + ph];
-          xb = std::max<long long>(xb, mlay_al16(8ll * V.n) + mlay_al16(8ll * V.ndyn) + mlay_al16(4ll * V.tail_m));
+          const long long rows = mlay_al16(4ll * V.tail_m);
+          const long long step = kStageBytes + mlay_al16(8ll * V.n) + mlay_al16(8ll * V.ndyn) + rows;
+          long long stage = 0;
+          if (V.tail_m) {
+            const Program &H = progs[2 * c + ph];
+            const long long cap = H.sprog[H.sp_off[12] + V.nlev - 1] >> 18;
+            stage = 8 * (((2ll * V.tail_m + 3 * cap + 3) & ~3ll) * 4) + rows;
+          }
+          need = std::max(need, std::max(step, stage));
         }
-      k.x_smem = kStageBytes + xb <= smax / 2;
-      k.gsm = kStageBytes + (k.x_smem ? xb : 0);
+      k.x_smem = need <= smax / 2;
+      k.gsm = k.x_smem ? need : kStageBytes;
     }
     all_items.insert(all_items.end(), k.items.begin(), k.items.end());
   }

@@ -102,7 +102,8 @@ struct DevProg {
   int ndyn, ncap, n_resop;
   // compact step program (global copy; the warp engine stages it in shared memory)
   const int *sprog;
-  int sp_off[14];
+  int sp_off[16];
+  int n_bchunk, n_brow;  // border of the dense trailing block: chunks, rows
   int sprog_ok;
   // transposed-solve program (adjoint)
   const int *tprog;

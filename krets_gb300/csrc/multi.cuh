@@ -19,12 +19,12 @@ namespace krets {
 // Working arrays of one circuit phase inside its region: a 16-byte header (queue slot
 // and status words), the staged step program (SMEM only), then the instance arrays.
 struct MLay {
-  int sp, lu, x, cdyn, cb, icap, coef64, bytes;
+  int sp, lu, x, cdyn, cb, icap, bpart, coef64, bytes;
 };
 
 __host__ __device__ inline int mlay_al16(long long v) { return (int)((v + 15) & ~15ll); }
 
-__host__ __device__ inline MLay multi_lay(int nnz_lu, int n, int ndyn, int ncap, int ne, int sp_words) {
+__host__ __device__ inline MLay multi_lay(int nnz_lu, int n, int ndyn, int ncap, int ne, int sp_words, int n_bchunk) {
   MLay L;
   long long cur = 16;
   L.sp = (int)cur;
@@ -39,7 +39,9 @@ __host__ __device__ inline MLay multi_lay(int nnz_lu, int n, int ndyn, int ncap,
   cur = mlay_al16(cur + 8ll * ndyn);
   L.icap = (int)cur;
   cur = mlay_al16(cur + 8ll * ncap);
-  L.coef64 = L.x;  // set-up scratch over x / cdyn / cb / icap (+ padding if needed)
+  L.bpart = (int)cur;  // partial sums of the dense block's border chunks
+  cur = mlay_al16(cur + 8ll * n_bchunk);
+  L.coef64 = L.x;  // set-up scratch over x .. bpart (+ padding if needed)
   if (cur - L.x < 8ll * ne) cur = L.x + mlay_al16(8ll * ne);
   L.bytes = (int)cur;
   return L;
@@ -76,7 +78,7 @@ __global__ void __launch_bounds__(512, 1)
     for (int phase = 0; phase < 2; ++phase) {
       const DevProg P = progs[2 * c + phase];
       const int spw = GLOBAL ? 0 : P.sp_off[5];
-      const MLay L = multi_lay(P.nnz_lu, P.n, P.ndyn, P.ncap, P.ne, spw);
+      const MLay L = multi_lay(P.nnz_lu, P.n, P.ndyn, P.ncap, P.ne, spw, P.n_bchunk);
       if (!GLOBAL) {
         const int4 *src = reinterpret_cast<const int4 *>(P.sprog);
         int4 *dst = reinterpret_cast<int4 *>(region + L.sp);
@@ -84,12 +86,13 @@ __global__ void __launch_bounds__(512, 1)
         gsync<G>(gid);
       }
       SProg S = sprog_view(P, GLOBAL ? P.sprog : reinterpret_cast<const int *>(region + L.sp));
+      S.bpart = reinterpret_cast<df *>(region + L.bpart);
       const bool xs = GLOBAL && x_smem;
       if (GLOBAL) {
         S.dense_stage = reinterpret_cast<df *>(gsm);
         if (xs && P.tail_m) {
-          // slots of the dense-block rows, after x and the rhs coefficients
-          int *rows = reinterpret_cast<int *>(gsm + kStageBytes + mlay_al16(8ll * P.n) + mlay_al16(8ll * P.ndyn));
+          // slots of the dense-block rows, at the end of the group's shared memory
+          int *rows = reinterpret_cast<int *>(gsm + gsm_bytes - mlay_al16(4ll * P.tail_m));
           for (int i = gl; i < P.tail_m; i += G) rows[i] = P.lu_rowptr[P.tail0 + i + 1] - P.tail_m;
           gsync<G>(gid);
           S.dense_rows = rows;
@@ -102,7 +105,13 @@ __global__ void __launch_bounds__(512, 1)
       df *cb = reinterpret_cast<df *>(xs ? gsm + kStageBytes + mlay_al16(8ll * P.n) : region + L.cb);
       df *icap = reinterpret_cast<df *>(region + L.icap);
       double *coef64 = reinterpret_cast<double *>(region + L.coef64);
-      st |= dfd_setup<G, GLOBAL ? 2 : 1>(P, S, nullptr, h, method, lu, lu64, coef64, cdyn, gl, gid);
+      // global class: the factorisation's column map (sparse part) and 32 x tw tiles (dense
+      // block) use the shared memory that x and the rhs coefficients take later (free
+      // during the set-up)
+      const long long tile_bytes = xs ? gsm_bytes - mlay_al16(4ll * P.tail_m) : kStageBytes;
+      const int tw = (int)min(128ll, (tile_bytes / (32 * 8)) / 32 * 32);
+      st |= dfd_setup<G, GLOBAL ? 2 : 1>(P, S, nullptr, h, method, lu, lu64, coef64, cdyn, gl, gid,
+                                         reinterpret_cast<double *>(gsm), tw, tile_bytes);
       if (gany<G>((st & (KS_SINGULAR | KS_NONFINITE | KS_NOTIMPL)) != 0, gid)) break;
       if (phase == 0) {
         // operating point: sources at their DC values (op.rs: capacitors removed,

@@ -384,6 +384,7 @@ std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<in
 //   [8] bd_ptr[n+1]   [9] bd_op (dyn << 1 | neg)   [10] qinv[n]
 //   [12] lmax[nlev], [13] umax[nulev]: split code of each L / U level (split_code: lanes per
 //        row by group size, longest row)
+//   [14] border chunks, [15] border rows (dense trailing block only; see below)
 //   [5] res_row[n] int2 {first op, n_unit | n_total << 16}
 //   [6] res_op: col | neg << 15 | slot << 16 (slot 0 = incidence +-1 entries, listed first;
 //       slot e+1 = coefficient of element e)
@@ -438,10 +439,18 @@ static void pack_step_program(const krets_element *el, Program &P) {
     int k = P.lev_rows[t];
     desc(k, P.lu_rowptr[k], lcount(k), P.lu_rowptr[k]);
   }
+  // U entries a row's descriptor covers: for rows before a dense trailing block, only the
+  // columns before it (the block's columns, the border, are a separate parallel phase)
+  auto ucount = [&](int k) {
+    int e = P.lu_rowptr[k + 1];
+    if (P.tail_m)
+      while (e > P.lu_diag[k] + 1 && P.lu_col[e - 1] >= P.tail0) --e;
+    return e - P.lu_diag[k] - 1;
+  };
   mark(3);
   for (size_t t = 0; t < P.ulev_rows.size(); ++t) {
     int k = P.ulev_rows[t];
-    desc(k, P.lu_diag[k] + 1, P.lu_rowptr[k + 1] - P.lu_diag[k] - 1, P.lu_diag[k]);
+    desc(k, P.lu_diag[k] + 1, ucount(k), P.lu_diag[k]);
   }
   mark(4);
   for (size_t u = 0; u < P.lu_col.size(); u += 2) {
@@ -476,10 +485,29 @@ static void pack_step_program(const krets_element *el, Program &P) {
     int mx = 0;
     for (int t = P.ulev_ptr[l]; t < P.ulev_ptr[l + 1]; ++t) {
       const int k = P.ulev_rows[t];
-      mx = std::max(mx, P.lu_rowptr[k + 1] - P.lu_diag[k] - 1);
+      mx = std::max(mx, ucount(k));
     }
     S.push_back(split_code(P.ulev_ptr[l + 1] - P.ulev_ptr[l], mx));
   }
+  // [14] border chunks {first slot, count <= 16}, [15] border rows {row, first chunk,
+  // chunks, 0}, for rows before a dense trailing block with entries in its columns
+  P.n_bchunk = P.n_brow = 0;
+  std::vector<int> chunks, brows;
+  if (P.tail_m) {
+    for (int k = 0; k < P.tail0; ++k) {
+      const int b0 = P.lu_diag[k] + 1 + ucount(k), b1 = P.lu_rowptr[k + 1];
+      if (b0 >= b1) continue;
+      brows.insert(brows.end(), {k, (int)chunks.size() / 2, 0, 0});
+      for (int c = b0; c < b1; c += 16) chunks.insert(chunks.end(), {c, std::min(16, b1 - c)});
+      brows[brows.size() - 2] = (int)chunks.size() / 2 - brows[brows.size() - 3];
+    }
+    P.n_bchunk = (int)chunks.size() / 2;
+    P.n_brow = (int)brows.size() / 4;
+  }
+  mark(14);
+  S.insert(S.end(), chunks.begin(), chunks.end());
+  mark(15);
+  S.insert(S.end(), brows.begin(), brows.end());
   // the residual operators come last: the direct engines stage only the words before them
   mark(5);
   std::vector<int> ops;
@@ -979,11 +1007,17 @@ extern "C" krets_status krets_symbolic_export(const krets_element *elems, int32_
                                     &P.a_slot, &P.a_cptr, &P.a_contrib, &P.b_cptr, &P.b_contrib, &P.piv_ptr,
                                     &P.piv, &P.upd, &P.lev_ptr, &P.lev_rows, &P.ulev_ptr, &P.ulev_rows,
                                     &P.el_pos};
-  if (which < 0 || which > KRETS_PROG_TPOFF) return KRETS_ERR_INVALID_ARGUMENT;
-  if (which == KRETS_PROG_TPROG || which == KRETS_PROG_TPOFF) {
+  if (which < 0 || which > KRETS_PROG_SPOFF) return KRETS_ERR_INVALID_ARGUMENT;
+  if (which == KRETS_PROG_TPROG || which == KRETS_PROG_TPOFF || which == KRETS_PROG_SPROG ||
+      which == KRETS_PROG_SPOFF) {
     std::vector<long long> v;
     if (which == KRETS_PROG_TPROG) v.assign(P.tprog.begin(), P.tprog.end());
-    else {
+    else if (which == KRETS_PROG_SPROG) v.assign(P.sprog.begin(), P.sprog.end());
+    else if (which == KRETS_PROG_SPOFF) {
+      v.assign(P.sp_off, P.sp_off + 16);
+      v.push_back(P.n_bchunk);
+      v.push_back(P.n_brow);
+    } else {
       v.assign(P.tp_off, P.tp_off + 8);
       v.push_back(P.n_utlev);
       v.push_back(P.n_ltlev);

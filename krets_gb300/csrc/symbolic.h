@@ -62,7 +62,8 @@ struct Program {
   // compact step program, copied into shared memory by the warp engine (sprog_ok = the
   // sizes fit its 16-bit packing).  Layout and packing: see pack_step_program().
   std::vector<int> sprog;
-  int sp_off[14] = {0};
+  int sp_off[16] = {0};
+  int n_bchunk = 0, n_brow = 0;  // border of the dense block (see pack_step_program)
   bool sprog_ok = false;
   // transposed-solve program (adjoint): A^T y = c  <=>  U^T z = c[q], then L^T y' = z, y = y'[pinv]
   //   tprog sections: [0] ut_ptr (levels of U^T, forward)  [1] ut_desc int4 {row | cnt << 16,

@@ -45,6 +45,13 @@ struct SProg {
   int tail0, tail_m;  // dense trailing block (tail_m = 0: none)
   df *dense_stage;    // 32 x 33 shared-memory tile for diagonal blocks read from global memory (or null)
   const int *dense_rows;  // slot of column tail0 of each dense-block row, in shared memory (or null)
+  // border of the dense block (U entries of rows before it in its columns): chunks of
+  // <= 16 entries {first slot, count}, rows {row, first chunk, chunks, 0}, and scratch
+  // for the chunks' partial sums (set by the kernel)
+  const int2 *bchunk;
+  const int4 *brow;
+  int n_bchunk, n_brow;
+  df *bpart;
 };
 
 __device__ __forceinline__ SProg sprog_view(const DevProg &P, const int *sp) {
@@ -68,6 +75,11 @@ __device__ __forceinline__ SProg sprog_view(const DevProg &P, const int *sp) {
   S.tail_m = P.tail_m;
   S.dense_stage = nullptr;
   S.dense_rows = nullptr;
+  S.bchunk = reinterpret_cast<const int2 *>(sp + P.sp_off[14]);
+  S.brow = reinterpret_cast<const int4 *>(sp + P.sp_off[15]);
+  S.n_bchunk = P.n_bchunk;
+  S.n_brow = P.n_brow;
+  S.bpart = nullptr;
   return S;
 }
 
@@ -688,12 +700,29 @@ __device__ __forceinline__ int row_find(const int *__restrict__ col, int lo, int
   return lo;
 }
 
+// smem (scratch, may be null): room for a per-warp map from the dense block's columns to
+// the slots of the row being factored (rows before the block keep their entries in those
+// columns, the border, at the end of the row); without room the border is searched too.
 template <int G>
-__device__ int g_factor64_warp(const DevProg &P, double *lu, int gl, int gid) {
+__device__ int g_factor64_warp(const DevProg &P, double *lu, int gl, int gid, double *tile, int tw, int *smem_map,
+                               long long smem_bytes) {
   int bad = 0;
   const int m = P.tail_m, t0 = P.tail0;
   const int lane = gl & 31, warp = gl >> 5;
   constexpr int NW = G / 32;
+  int *wmap = (m && smem_map && (long long)NW * m * 4 <= smem_bytes) ? smem_map + warp * m : nullptr;
+  if (wmap) {
+    for (int i = lane; i < m; i += 32) wmap[i] = -1;
+    __syncwarp();
+  }
+  // dense-block rows (last level): each warp stages its row in shared memory — the dense
+  // part (m values) and the sparse part (values and columns, at most cap entries) — so the
+  // eliminations of the sparse columns (the Schur update of the block) update shared
+  // memory instead of chaining global read-modify-writes
+  const int cap = m ? (P.sprog[P.sp_off[12] + P.nlev - 1] >> 18) : 0;
+  const long long st_words = ((long long)m * 2 + cap * 3 + 3) & ~3ll;  // 4-byte words; 16-byte aligned per warp
+  double *wst = (m && smem_map && (long long)NW * st_words * 4 <= smem_bytes)
+                    ? reinterpret_cast<double *>(smem_map + warp * st_words) : nullptr;
   for (int l = 0; l < P.nlev; ++l) {
     const int r0 = P.lev_ptr[l], r1 = P.lev_ptr[l + 1];
     const bool tail_level = m && l == P.nlev - 1;  // rows of the dense block: sparse columns only
@@ -702,9 +731,70 @@ __device__ int g_factor64_warp(const DevProg &P, double *lu, int gl, int gid) {
       const int re = P.lu_rowptr[k + 1];
       const int dense0 = tail_level ? re - m : re;  // first slot of the dense part (tail rows)
       const int dk = tail_level ? dense0 : P.lu_diag[k];
+      if (tail_level && wst && dense0 - P.lu_rowptr[k] <= cap) {
+        const int s0 = P.lu_rowptr[k], ns = dense0 - s0;
+        double *D = wst, *Sv = wst + m;
+        int *Sc = reinterpret_cast<int *>(Sv + cap);
+        for (int i = lane; i < m; i += 32) D[i] = lu[dense0 + i];
+        for (int i = lane; i < ns; i += 32) {
+          Sv[i] = lu[s0 + i];
+          Sc[i] = P.lu_col[s0 + i];
+        }
+        __syncwarp();
+        int dj = ns > 0 ? P.lu_diag[Sc[0]] : 0;  // diagonal slot of the next column, loaded ahead
+        for (int q = 0; q < ns; ++q) {
+          const int j = Sc[q];
+          const int ub = dj + 1, ue = P.lu_rowptr[j + 1];
+          const double rpiv = lu[dj];  // rows before the block hold reciprocal pivots
+          if (q + 1 < ns) dj = P.lu_diag[Sc[q + 1]];
+          const double l_kj = Sv[q] * rpiv;
+          __syncwarp();
+          if (lane == 0) Sv[q] = l_kj;
+          for (int u0 = ub + lane; u0 < ue; u0 += 128) {  // four entries of U row j in flight per lane
+            int cs[4];
+            double vs[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+              const int u = u0 + 32 * r;
+              cs[r] = u < ue ? P.lu_col[u] : -1;
+              vs[r] = u < ue ? lu[u] : 0.0;
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+              const int c = cs[r];
+              if (c < 0) continue;
+              const double v = l_kj * vs[r];
+              if (c >= t0) {
+                D[c - t0] -= v;
+              } else {
+                int lo = q + 1, hi = ns;  // c > j: among this row's later sparse columns
+                while (lo < hi) {
+                  const int mid = (lo + hi) >> 1;
+                  if (Sc[mid] < c) lo = mid + 1;
+                  else hi = mid;
+                }
+                if (lo < ns && Sc[lo] == c) Sv[lo] -= v;
+                else bad |= KS_SINGULAR;  // not in the pattern: an inconsistent program
+              }
+            }
+          }
+          __syncwarp();
+        }
+        for (int i = lane; i < m; i += 32) lu[dense0 + i] = D[i];
+        for (int i = lane; i < ns; i += 32) lu[s0 + i] = Sv[i];
+        __syncwarp();
+        continue;
+      }
+      // row before the block: map its border columns to their slots
+      int b0 = dense0;
+      if (!tail_level && wmap) {
+        b0 = row_find(P.lu_col, dk + 1, re, t0);
+        for (int q = b0 + lane; q < re; q += 32) wmap[P.lu_col[q] - t0] = q;
+        __syncwarp();
+      }
       for (int s = P.lu_rowptr[k]; s < dk; ++s) {
         const int j = P.lu_col[s];
-        const double l_kj = lu[s] / lu[P.lu_diag[j]];
+        const double l_kj = lu[s] * lu[P.lu_diag[j]];  // reciprocal pivot of the finished row j
         __syncwarp();
         if (lane == 0) lu[s] = l_kj;
         const int ue = P.lu_rowptr[j + 1];
@@ -713,10 +803,16 @@ __device__ int g_factor64_warp(const DevProg &P, double *lu, int gl, int gid) {
           int p;
           if (tail_level && c >= t0) {
             p = dense0 + (c - t0);
-          } else {
-            p = row_find(P.lu_col, s + 1, dense0, c);
-            if (p >= dense0 || P.lu_col[p] != c) {
+          } else if (wmap && c >= t0) {
+            p = wmap[c - t0];
+            if (p < 0) {
               bad |= KS_SINGULAR;  // not in the pattern: an inconsistent program
+              continue;
+            }
+          } else {
+            p = row_find(P.lu_col, s + 1, b0, c);
+            if (p >= b0 || P.lu_col[p] != c) {
+              bad |= KS_SINGULAR;
               continue;
             }
           }
@@ -724,34 +820,76 @@ __device__ int g_factor64_warp(const DevProg &P, double *lu, int gl, int gid) {
         }
         __syncwarp();
       }
+      if (!tail_level && wmap) {
+        for (int q = b0 + lane; q < re; q += 32) wmap[P.lu_col[q] - t0] = -1;
+        __syncwarp();
+      }
       if (!tail_level && lane == 0) {
+        // the row is final: check its pivot and keep its reciprocal, so later rows
+        // multiply instead of dividing (FP64 division is a long chain on this GPU)
         const double d = lu[dk];
         if (!(fabs(d) > 0)) bad |= KS_SINGULAR;
         else if (!isfinite(d)) bad |= KS_NONFINITE;
+        lu[dk] = 1.0 / d;
       }
     }
     gsync<G>(gid);
   }
   if (m) {
-    // dense right-looking LU of the trailing block: a warp per row, lanes over columns
-    for (int kk = 0; kk < m; ++kk) {
-      const double *pr = lu + (P.lu_rowptr[t0 + kk + 1] - m);
-      const double piv = pr[kk];
-      if (gl == 0) {
-        if (!(fabs(piv) > 0)) bad |= KS_SINGULAR;
-        else if (!isfinite(piv)) bad |= KS_NONFINITE;
+    // blocked right-looking LU of the dense block (rows in global memory), panels of 32
+    // columns: (1) the panel by columns (a warp per row, lanes over the panel's columns);
+    // (2) per tile of tw columns right of it: the tile staged in shared memory, the unit
+    // lower 32 x 32 solve on it (a thread per column), the tile written back as U12, and
+    // (3) the rows below updated from it, A22 -= L21 U12 (a warp per row, lanes over the
+    // tile's columns, L21 broadcast by shuffles).  Each trailing element is read and
+    // written once per panel instead of once per column.
+    auto row = [&](int i) { return lu + (P.lu_rowptr[t0 + i + 1] - m); };
+    for (int kb = 0; kb < m; kb += 32) {
+      const int nb = min(32, m - kb);
+      for (int kk = kb; kk < kb + nb; ++kk) {
+        const double *pr = row(kk);
+        const double piv = pr[kk];
+        if (gl == 0) {
+          if (!(fabs(piv) > 0)) bad |= KS_SINGULAR;
+          else if (!isfinite(piv)) bad |= KS_NONFINITE;
+        }
+        for (int i = kk + 1 + warp; i < m; i += NW) {
+          double *ri = row(i);
+          const double l_ik = ri[kk] / piv;
+          __syncwarp();
+          if (lane == 0) ri[kk] = l_ik;
+          for (int c = kk + 1 + lane; c < kb + nb; c += 32) ri[c] -= l_ik * row(kk)[c];
+        }
+        gsync<G>(gid);
       }
-      for (int i = kk + 1 + warp; i < m; i += NW) {
-        double *ri = lu + (P.lu_rowptr[t0 + i + 1] - m);
-        const double l_ik = ri[kk] / piv;
-        __syncwarp();
-        if (lane == 0) ri[kk] = l_ik;
-        for (int c = kk + 1 + lane; c < m; c += 32) ri[c] -= l_ik * pr[c];
+      for (int c0 = kb + nb; c0 < m; c0 += tw) {
+        const int w = min(tw, m - c0);
+        for (int q = gl; q < nb * w; q += G) tile[(q / w) * tw + q % w] = row(kb + q / w)[c0 + q % w];
+        gsync<G>(gid);
+        for (int c = gl; c < w; c += G)
+          for (int r = 1; r < nb; ++r) {
+            const double *lr = row(kb + r) + kb;
+            double acc = tile[r * tw + c];
+            for (int q = 0; q < r; ++q) acc -= lr[q] * tile[q * tw + c];
+            tile[r * tw + c] = acc;
+          }
+        gsync<G>(gid);
+        for (int q = gl; q < nb * w; q += G) row(kb + q / w)[c0 + q % w] = tile[(q / w) * tw + q % w];
+        for (int i = kb + nb + warp; i < m; i += NW) {
+          double *ri = row(i);
+          const double lq = lane < nb ? ri[kb + lane] : 0.0;
+          for (int cb = 0; cb < w; cb += 32) {  // every lane takes part in the shuffles
+            const int c = cb + lane;
+            double acc = 0.0;
+            for (int q = 0; q < nb; ++q) acc += __shfl_sync(kFull, lq, q) * (c < w ? tile[q * tw + c] : 0.0);
+            if (c < w) ri[c0 + c] -= acc;
+          }
+        }
+        gsync<G>(gid);
       }
-      gsync<G>(gid);
     }
   }
-  for (int k = gl; k < P.n; k += G) {
+  for (int k = (m ? t0 : P.n) + gl; k < P.n; k += G) {  // pivots of the dense block
     const int sl = P.lu_diag[k];
     lu[sl] = 1.0 / lu[sl];
   }
@@ -1077,6 +1215,38 @@ __device__ __forceinline__ void df_dense_upper(const SProg &S, const df *__restr
   }
 }
 
+// Border of the dense block, after its backward solve: every row before the block
+// subtracts its U entries in the block's columns (x there is final), all rows at once.
+// Pass 1: chunks of <= 16 entries over all threads (four loads in flight); pass 2: each
+// row sums its chunks' partial sums in order.
+template <int G>
+__device__ __forceinline__ void df_border(const SProg &S, const df *__restrict__ lu, df *y, int gl, int gid) {
+  for (int c = gl; c < S.n_bchunk; c += G) {
+    const int2 ch = S.bchunk[c];
+    df s{0.f, 0.f};
+    for (int e = 0; e < ch.y; e += 4) {
+      df a[4], v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const bool in = e + q < ch.y;
+        a[q] = in ? lu[ch.x + e + q] : df{0.f, 0.f};
+        v[q] = in ? y[S.lu_col[ch.x + e + q]] : df{0.f, 0.f};
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) s = df_fma_acc(a[q], v[q], s);
+    }
+    S.bpart[c] = df_norm(s);
+  }
+  gsync<G>(gid);
+  for (int r = gl; r < S.n_brow; r += G) {
+    const int4 br = S.brow[r];
+    df s = S.bpart[br.y];
+    for (int c = br.y + 1; c < br.y + br.z; ++c) s = df_add(s, S.bpart[c]);
+    y[br.x] = df_sub(y[br.x], s);
+  }
+  gsync<G>(gid);
+}
+
 template <int G, bool UPPER, int SG = G>
 __device__ __forceinline__ void df_solve(const SProg &S, const df *__restrict__ lu, df *y, int gl, int gid, int nar) {
   const int nl = UPPER ? S.nulev : S.nlev;
@@ -1086,6 +1256,7 @@ __device__ __forceinline__ void df_solve(const SProg &S, const df *__restrict__ 
   const bool w0 = gl < 32;
   if (nar < 0) {  // no narrow-level split: every level on the whole group
     if (UPPER && S.tail_m) df_dense_upper<G>(S, lu, y, gl, gid);
+    if (UPPER && S.n_brow) df_border<G>(S, lu, y, gl, gid);
     for (int l = UPPER ? 0 : 1; l < nl; ++l) {
       const int spl = split_lanes<SG>(mx[l]);
       if (spl > 1) df_level_split<UPPER>(S, lu, y, ptr, desc, l, gl, G, spl);
@@ -1143,7 +1314,8 @@ struct DfdLay {
 // MERGE: 0 = update list, 1 = thread-per-row merge, 2 = warp-per-row (global memory)
 template <int G, int MERGE = 0>
 __device__ __forceinline__ int dfd_setup(const DevProg &P, const SProg &S, const double *vals, double h, int method,
-                                         df *lu, double *lu64, double *coef64, df *cdyn, int gl, int gid) {
+                                         df *lu, double *lu64, double *coef64, df *cdyn, int gl, int gid,
+                                         double *tile = nullptr, int tw = 0, long long tile_bytes = 0) {
   int st = g_coef_pass<G>(P, vals, h, method, coef64, gl);
   gsync<G>(gid);
   for (int sl = gl; sl < P.nnz_lu; sl += G) {
@@ -1151,7 +1323,7 @@ __device__ __forceinline__ int dfd_setup(const DevProg &P, const SProg &S, const
     lu64[sl] = t < 0 ? 0.0 : sum_entry<double>(P, t, coef64, nullptr);
   }
   gsync<G>(gid);
-  st |= MERGE == 2   ? g_factor64_warp<G>(P, lu64, gl, gid)
+  st |= MERGE == 2   ? g_factor64_warp<G>(P, lu64, gl, gid, tile, tw, reinterpret_cast<int *>(tile), tile_bytes)
         : MERGE == 1 ? g_factor64_merge<G>(P, lu64, gl, gid)
                      : g_factor64<G>(P, lu64, gl, gid);
   for (int sl = gl; sl < P.nnz_lu; sl += G) lu[sl] = df_from_double(lu64[sl]);

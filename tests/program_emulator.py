@@ -253,10 +253,25 @@ def solve_multi(prog, n, lu, b):
         y[t0:] = z
     ulp, ulr = prog["ulev_ptr"], prog["ulev_rows"]
     assert not m or not np.any(ulr >= t0)
+    # border of the dense block (step program sections 14/15), then the U levels with the
+    # entry counts of the step program's U descriptors
+    sp, off = prog["sprog"], prog["spoff"]
+    n_bchunk, n_brow = int(off[16]), int(off[17])
+    chunks = sp[off[14]:off[14] + 2 * n_bchunk].reshape(-1, 2)
+    brows = sp[off[15]:off[15] + 4 * n_brow].reshape(-1, 4)
+    for row, first, nch, _ in brows:
+        acc = 0.0
+        for start, cnt in chunks[first:first + nch]:
+            assert 0 < cnt <= 16 and np.all(col[start:start + cnt] >= t0)
+            acc += sum(lu[q] * y[col[q]] for q in range(start, start + cnt))
+        y[row] -= acc
+    udesc = sp[off[3]:off[3] + 4 * len(ulr)].reshape(-1, 4)
+    ucnt = {int(d[0]) & 0xffff: int(d[3]) + (int(d[0]) >> 16) for d in udesc}
     for lv in range(len(ulp) - 1):
         new = {}
         for k in ulr[ulp[lv]:ulp[lv + 1]]:
-            new[k] = (y[k] - sum(lu[s] * y[col[s]] for s in range(dg[k] + 1, rp[k + 1]))) / lu[dg[k]]
+            e1 = dg[k] + 1 + ucnt[k]
+            new[k] = (y[k] - sum(lu[s] * y[col[s]] for s in range(dg[k] + 1, e1))) / lu[dg[k]]
         for k, v in new.items():
             y[k] = v
     x = np.zeros(n)

@@ -47,10 +47,12 @@ def test_uneven_netlists_have_regular_dc_systems(oracle_lib):
 @pytest.mark.gpu
 def test_multi_circuit_transient_matches_oracle(oracle_lib):
     idx = [i for i in range(40) if uneven_table(i)[1] <= 2600][:20]
+    idx += [i for i in range(40, 80) if 2000 <= uneven_table(i)[1] <= 2600][:2]
     tabs = [uneven_table(i) for i in idx]
     m = _lib.MultiCircuit([t for t, _ in tabs], [n for _, n in tabs], method="be", h=1e-9)
     info = m.info()
     assert info[0] == len(idx) and (info[4:10] > 0).sum() >= 3    # several size classes used
+    assert info[9] > 0                                               # and the global-memory class
     steps = 200
     flat, st = m.tran(steps)
     assert np.all(st == 0)

@@ -163,6 +163,12 @@ def test_multi_circuit_program_dense_tail_solves(built_lib, oracle_lib):
     lv = p["lev_ptr"]
     assert np.array_equal(p["lev_rows"][lv[-2]:lv[-1]], np.arange(t0, n))
     assert len(p["ulev_rows"]) == t0
+    # the border (U entries of earlier rows in the block's columns) is listed once, whole
+    sp, off = p["sprog"], p["spoff"]
+    chunks = sp[off[14]:off[14] + 2 * int(off[16])].reshape(-1, 2)
+    dg = p["lu_diag"]
+    border = sum(int((col[dg[k] + 1:rp[k + 1]] >= t0).sum()) for k in range(t0))
+    assert int(chunks[:, 1].sum()) == border > 0
     ca, _ = PE.element_coefs(t, 2, "be", 1e-9, prev=np.zeros(n), icap=np.zeros(len(t)))
     lu = PE.factor_multi(p, n, ca)
     A, _ = oracle_lib.assemble(t, n, "tran", 1e-9, "be", sol=np.zeros(n))
