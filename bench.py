@@ -331,13 +331,14 @@ def run_ours(args, rank, world):
     except Exception:
         e2e_inst = 256
     host_out = np.empty((e2e_inst, N_STEPS + 1, n))
+    host_out.fill(0.0)  # a caller's buffer is resident (touched) before it is handed over
     host_vals = np.ascontiguousarray(vals[:e2e_inst])
     e2e_ms = []
-    for r in range(1 + max(1, min(args.steps, 2))):
+    for r in range(2 + max(1, min(args.steps, 2))):
         _lib.lib().krets_device_synchronize()
         g.batch_tran(host_vals, H, N_STEPS, "tr", lag=False, precision=_lib.PREC_DF, out=host_out)
         _lib.lib().krets_device_synchronize()
-        if r > 0:
+        if r > 1:
             e2e_ms.append(g.timing()[1])
     e2e_val = e2e_inst * N_STEPS * len(e2e_ms) / (sum(e2e_ms) / 1e3)
 
@@ -364,7 +365,8 @@ def run_ours(args, rank, world):
         "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{n_sample} instances x {N_STEPS} TR steps, factor once, oracle/ C restatement"},
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(host_vals.nbytes),
-                "d2h_bytes_per_step": int(host_out.nbytes), "instances": e2e_inst},
+                "d2h_bytes_per_step": int(host_out.nbytes), "instances": e2e_inst,
+                "host_buffers_in_place": bool(_lib.lib().krets_direct_host_access())},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
@@ -566,8 +568,9 @@ def workload_uneven(args, world, reference):
         k += 1
     m2 = _lib.MultiCircuit([t for t, _ in tabs[:k]], [n for _, n in tabs[:k]], method="be", h=UNEVEN_H)
     host = np.empty(m2.total(UNEVEN_STEPS))
-    m2.tran(UNEVEN_STEPS, out=host)
-    m2.tran(UNEVEN_STEPS, out=host)
+    host.fill(0.0)
+    for _ in range(3):
+        m2.tran(UNEVEN_STEPS, out=host)
     e2e = k * UNEVEN_STEPS / (m2.timing()[1] / 1e3)
     alg = (int(info[1]) * UNEVEN_STEPS + int(info[1])) * 8
     k_s = statistics.mean(ks) / 1e3

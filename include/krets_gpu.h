@@ -196,6 +196,11 @@ krets_status krets_multi_tran(krets_multi *m, int32_t n_steps, int32_t source_la
                               const int64_t *x_offsets, int32_t *circuit_status);
 krets_status krets_multi_last_timing(const krets_multi *m, float *kernel_ms, float *call_ms);
 
+/* 1 when kernels read and write caller host buffers in place (a GPU sharing the host's page
+ * tables, as on Grace systems), 0 when host buffers go through device copies.  Set
+ * KRETS_NO_DIRECT_HOST=1 before the first call to force the copies. */
+int32_t krets_direct_host_access(void);
+
 /* Batched operating points: x_out[n_inst][n]. */
 krets_status krets_batch_op(krets_circuit *c, int32_t n_inst, const double *values, double *x_out,
                             int32_t *inst_status);

@@ -75,6 +75,7 @@ def lib():
             "krets_multi_info": [_P, _P, _I],
             "krets_multi_tran": [_P, _I, _I, _P, _P, _P],
             "krets_multi_last_timing": [_P, _P, _P],
+            "krets_direct_host_access": [],
             "krets_batch_op": [_P, _I, _P, _P, _P],
             "krets_last_timing": [_P, _P, _P],
             "krets_last_refine_stats": [_P, _P, _P],

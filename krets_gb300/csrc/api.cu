@@ -95,6 +95,23 @@ bool is_device_ptr(const void *p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Kernels may read and write pageable host memory directly on systems whose GPU shares the
+// host's page tables (Grace: NVLink-C2C with address translation); then host buffers are
+// used in place instead of through a device copy.  KRETS_NO_DIRECT_HOST=1 turns it off.
+bool direct_host_access() {
+  static int cached = -1;
+  if (cached < 0) {
+    int dev = 0, v = 0;
+    cached = 0;
+    const char *off = getenv("KRETS_NO_DIRECT_HOST");
+    if (!(off && off[0] == '1') && cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) == cudaSuccess)
+      cached = v ? 1 : 0;
+    cudaGetLastError();
+  }
+  return cached == 1;
+}
+
 }  // namespace
 
 struct krets_circuit {
@@ -373,7 +390,7 @@ krets_status dev_view(const void *user, size_t bytes, bool in, cudaStream_t s, D
     *dptr = nullptr;
     return KRETS_OK;
   }
-  if (is_device_ptr(user)) {
+  if (is_device_ptr(user) || direct_host_access()) {
     *dptr = const_cast<void *>(user);
     return KRETS_OK;
   }
@@ -1621,6 +1638,8 @@ krets_status krets_multi_tran(krets_multi *m, int32_t n_steps, int32_t source_la
   }
   return map_status(any, 0);
 }
+
+int32_t krets_direct_host_access(void) { return direct_host_access() ? 1 : 0; }
 
 krets_status krets_multi_last_timing(const krets_multi *m, float *kernel_ms, float *call_ms) {
   if (!m) return fail(KRETS_ERR_INVALID_ARGUMENT, "null multi-circuit handle");

@@ -207,3 +207,17 @@ def test_errors_are_reported():
     c = parse_circuit_description("V1 a 0 1\nR1 a 0 1\n")
     with pytest.raises(ElementNotFound):
         Solver(c).solve(DcAnalysis("V9", 0, 1, 0.5))
+
+
+def test_batched_transient_host_and_device_outputs_identical():
+    """Host output buffers (used in place when the GPU shares the host page tables, else
+    through a device copy) give the same bits as a device buffer."""
+    c = rlc_ladder(20)
+    t = element_table(c)
+    vals = monte_carlo_values(c, 5, seed=2)
+    g = _lib.GpuCircuit(t, c.size)
+    host = g.batch_tran(vals, 1e-12, 300, "tr", lag=False, precision=_lib.PREC_DF)
+    dev = _lib.DeviceArray((5, 301, c.size))
+    g.batch_tran(vals, 1e-12, 300, "tr", lag=False, precision=_lib.PREC_DF, out=dev)
+    assert np.array_equal(host, dev.download())
+    assert _lib.lib().krets_direct_host_access() in (0, 1)

@@ -19,7 +19,8 @@ ROOT = Path(__file__).resolve().parents[1]
 def test_library_exports_every_declared_symbol(built_lib):
     import ctypes
     hdr = (ROOT / "include" / "krets_gpu.h").read_text()
-    names = set(re.findall(r"^(?:krets_status|const char \*|int64_t)\s*(krets_[a-z0-9_]+)\s*\(", hdr, re.M))
+    names = set(re.findall(r"^(?:krets_status|const char \*|int64_t|int32_t)\s*(krets_[a-z0-9_]+)\s*\(", hdr,
+                           re.M))
     assert len(names) > 15
     lib = ctypes.CDLL(str(built_lib.LIB_PATH))
     for nm in sorted(names):
