@@ -110,6 +110,15 @@ def check(status: int, what: str = ""):
     raise cls(f"{what}: {L.krets_status_string(status).decode()} ({msg})")
 
 
+def host_buffer(shape, dtype=np.float64) -> np.ndarray:
+    """Zeroed output buffer whose pages are resident (written by the CPU): the library may
+    have the GPU write host buffers in place, and a GPU first touch of fresh pages is far
+    slower than the CPU's."""
+    a = np.empty(shape, dtype)
+    a.fill(0)
+    return a
+
+
 def ptr(a) -> ctypes.c_void_p:
     if a is None:
         return None
@@ -188,7 +197,7 @@ class MultiCircuit:
         if lag is None:
             lag = self.method == "be"
         if out is None:
-            out = np.zeros(self.total(n_steps))
+            out = host_buffer(self.total(n_steps))
         st = np.zeros(len(self.sizes), dtype=np.int32)
         check(lib().krets_multi_tran(self.h, n_steps, int(bool(lag)), ptr(out), None, ptr(st)), "multi_tran")
         return out, st
@@ -239,21 +248,21 @@ class GpuCircuit:
 
     # -------------------------------------------------------------- analyses
     def op(self):
-        x = np.zeros(self.n)
+        x = host_buffer(self.n)
         it = ctypes.c_int32(0)
         check(lib().krets_op(self.h, ptr(x), ctypes.byref(it)), "op")
         return x, it.value
 
     def dc(self, sweep_index, start, stop, step):
         npts = int(abs((stop - start) / step)) + 1
-        x = np.zeros((npts, self.n))
+        x = host_buffer((npts, self.n))
         got = ctypes.c_int32(0)
         check(lib().krets_dc(self.h, sweep_index, start, stop, step, ptr(x), npts, ctypes.byref(got)), "dc")
         return x[:got.value]
 
     def ac(self, freqs):
         f = np.ascontiguousarray(freqs, dtype=np.float64)
-        x = np.zeros((max(len(f), 1), self.n, 2))
+        x = host_buffer((max(len(f), 1), self.n, 2))
         kept = ctypes.c_int32(0)
         check(lib().krets_ac(self.h, ptr(f), len(f), ptr(x), ctypes.byref(kept)), "ac")
         return x[:kept.value, :, 0] + 1j * x[:kept.value, :, 1]
@@ -262,7 +271,7 @@ class GpuCircuit:
         m = METHOD[method]
         if lag is None:
             lag = m == 0
-        x = np.zeros((n_steps + 1, self.n))
+        x = host_buffer((n_steps + 1, self.n))
         check(lib().krets_tran(self.h, h, n_steps, m, int(bool(lag)), int(bool(refactor_each_step)), ptr(x)),
               "tran")
         return x
@@ -270,7 +279,7 @@ class GpuCircuit:
     def batch_op(self, values):
         v = np.ascontiguousarray(values, dtype=np.float64)
         ni = v.shape[0]
-        x = np.zeros((ni, self.n))
+        x = host_buffer((ni, self.n))
         st = np.zeros(ni, dtype=np.int32)
         check(lib().krets_batch_op(self.h, ni, ptr(v), ptr(x), ptr(st)), "batch_op")
         return x
@@ -288,7 +297,7 @@ class GpuCircuit:
             values = np.ascontiguousarray(values, dtype=np.float64)
             ni = values.shape[0]
         if out is None:
-            out = np.zeros((ni, n_steps + 1, self.n))
+            out = host_buffer((ni, n_steps + 1, self.n))
         st = np.zeros(ni, dtype=np.int32)
         check(lib().krets_batch_tran(self.h, ni, ptr(values), h, n_steps, m, int(bool(lag)), precision, ptr(out),
                                      ptr(st)), "batch_tran")
@@ -313,8 +322,8 @@ class GpuCircuit:
         else:
             values = np.ascontiguousarray(values, dtype=np.float64)
             ni = values.shape[0]
-        loss = np.zeros(ni)
-        grad = np.zeros((ni, self.ne)) if gradient else None
+        loss = host_buffer(ni)
+        grad = host_buffer((ni, self.ne)) if gradient else None
         check(lib().krets_adjoint_tran(self.h, ni, ptr(values), h, n_steps, METHOD[method], out_unknown,
                                        checkpoint_every, int(bool(gradient)), ptr(loss), ptr(grad)),
               "adjoint_tran")
@@ -331,7 +340,7 @@ class GpuCircuit:
             ni = values.shape[0]
         host_out = out is None
         if host_out:
-            out = np.zeros((ni, len(f), self.n, 2))
+            out = host_buffer((ni, len(f), self.n, 2))
         st = np.zeros(ni * len(f), dtype=np.int32)
         check(lib().krets_batch_ac(self.h, ni, ptr(values), ptr(f), len(f), precision, ptr(out), ptr(st)),
               "batch_ac")
