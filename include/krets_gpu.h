@@ -201,6 +201,15 @@ krets_status krets_multi_last_timing(const krets_multi *m, float *kernel_ms, flo
  * KRETS_NO_DIRECT_HOST=1 before the first call to force the copies. */
 int32_t krets_direct_host_access(void);
 
+/* Batched DC sweep (dc.rs:14-124 per instance): every instance sweeps element `sweep_elem`
+ * over the same points, warm-started point to point; values [n_inst][n_elem] replaces the
+ * elements' values per instance (the swept element's value is overwritten per point).
+ * x_out[n_inst][max_points][n]; *n_points = points per instance; an instance stops at its
+ * first failing point (its status in inst_status). */
+krets_status krets_batch_dc(krets_circuit *c, int32_t n_inst, const double *values, int32_t sweep_elem,
+                            double start, double stop, double step, double *x_out, int32_t max_points,
+                            int32_t *n_points, int32_t *inst_status);
+
 /* Batched operating points: x_out[n_inst][n]. */
 krets_status krets_batch_op(krets_circuit *c, int32_t n_inst, const double *values, double *x_out,
                             int32_t *inst_status);

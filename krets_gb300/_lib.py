@@ -77,6 +77,7 @@ def lib():
             "krets_multi_last_timing": [_P, _P, _P],
             "krets_direct_host_access": [],
             "krets_batch_op": [_P, _I, _P, _P, _P],
+            "krets_batch_dc": [_P, _I, _P, _I, _D, _D, _D, _P, _I, _P, _P],
             "krets_last_timing": [_P, _P, _P],
             "krets_last_refine_stats": [_P, _P, _P],
             "krets_device_alloc": [ctypes.c_size_t, _P],
@@ -283,6 +284,18 @@ class GpuCircuit:
         st = np.zeros(ni, dtype=np.int32)
         check(lib().krets_batch_op(self.h, ni, ptr(v), ptr(x), ptr(st)), "batch_op")
         return x
+
+    def batch_dc(self, values, sweep_index, start, stop, step):
+        """Warm-started DC sweep of every instance: [n_inst][points][n], statuses."""
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        ni = v.shape[0]
+        npts = int(abs((stop - start) / step)) + 1
+        x = host_buffer((ni, npts, self.n))
+        st = np.zeros(ni, dtype=np.int32)
+        got = ctypes.c_int32(0)
+        check(lib().krets_batch_dc(self.h, ni, ptr(v), sweep_index, start, stop, step, ptr(x), npts,
+                                   ctypes.byref(got), ptr(st)), "batch_dc")
+        return x[:, :got.value], st
 
     def batch_tran(self, values, h, n_steps, method="tr", lag=None, precision=PREC_MIXED, out=None,
                    n_inst=None):

@@ -641,39 +641,63 @@ krets_status krets_batch_op(krets_circuit *c, int32_t n_inst, const double *valu
   return map_status(any, 0);
 }
 
-krets_status krets_dc(krets_circuit *c, int32_t sweep_elem, double start, double stop, double step, double *x_out,
-                      int32_t max_points, int32_t *n_points) {
-  if (!c || !x_out) return fail(KRETS_ERR_INVALID_ARGUMENT, "null argument");
+namespace {
+
+// Shared by krets_dc and krets_batch_dc: checks the sweep and returns its point count
+// (|(stop-start)/step| + 1, truncated: dc.rs:153-154).
+krets_status dc_points(krets_circuit *c, int32_t sweep_elem, double start, double stop, double step, int &np) {
   if (sweep_elem < 0 || sweep_elem >= c->ne) return fail(KRETS_ERR_ELEMENT_NOT_FOUND, "sweep element not found");
   int kind = c->el[sweep_elem].kind;
   if (kind != KRETS_ELEM_V && kind != KRETS_ELEM_I)
     return fail(KRETS_ERR_INVALID_ELEMENT, "DC sweep element must be a voltage or current source");
   double np_d = std::fabs((stop - start) / step);
   if (!(np_d < 1e9)) return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid sweep range");
-  int np = (int)np_d + 1;  // dc.rs:153-154 (truncation)
-  if (n_points) *n_points = np;
-  if (np > max_points) return fail(KRETS_ERR_INVALID_ARGUMENT, "x_out too small for the sweep");
+  np = (int)np_d + 1;
+  return KRETS_OK;
+}
+
+krets_status run_dc(krets_circuit *c, int32_t sweep_elem, double start, double step, int np, int n_inst,
+                    const double *values, double *x_out, int *d_status) {
   DevProgram *D;
   krets_status s = get_program(c, MODE_DC, 0, 0, 0, &D);
   if (s != KRETS_OK) return s;
-  CU(cudaEventRecord(c->ev[0], c->stream));
-  DevBuf tx;
-  void *dx;
-  s = dev_view(x_out, sizeof(double) * c->n * (size_t)np, false, c->stream, tx, &dx);
+  const size_t out_bytes = sizeof(double) * c->n * (size_t)np * n_inst;
+  DevBuf tv, tx;
+  void *dv, *dx;
+  s = dev_view(values, sizeof(double) * c->ne * (size_t)n_inst, true, c->stream, tv, &dv);
+  if (s) return s;
+  s = dev_view(x_out, out_bytes, false, c->stream, tx, &dx);
   if (s) return s;
   Lay L = layout_op(D->view);
   int threads = plain_threads(D->view), grid;
   size_t smem;
   char *gws;
-  s = plan_launch(c, k_dc_sweep, L, threads, 1, grid, smem, gws);
+  s = plan_launch(c, k_dc_sweep, L, threads, n_inst, grid, smem, gws);
   if (s) return s;
   CU(cudaEventRecord(c->ev[2], c->stream));
-  k_dc_sweep<<<1, threads, smem, c->stream>>>(D->view, c->cfg, L, gws, sweep_elem, start, step, np, (double *)dx,
-                                              c->d_small);
+  k_dc_sweep<<<grid, threads, smem, c->stream>>>(D->view, c->cfg, L, gws, sweep_elem, start, step, np,
+                                                 (const double *)dv, n_inst, (size_t)c->n * np, (double *)dx,
+                                                 d_status);
   g_launches++;
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[3], c->stream));
-  if (tx.p) CU(cudaMemcpyAsync(x_out, dx, sizeof(double) * c->n * (size_t)np, cudaMemcpyDeviceToHost, c->stream));
+  if (tx.p) CU(cudaMemcpyAsync(x_out, dx, out_bytes, cudaMemcpyDeviceToHost, c->stream));
+  return KRETS_OK;
+}
+
+}  // namespace
+
+krets_status krets_dc(krets_circuit *c, int32_t sweep_elem, double start, double stop, double step, double *x_out,
+                      int32_t max_points, int32_t *n_points) {
+  if (!c || !x_out) return fail(KRETS_ERR_INVALID_ARGUMENT, "null argument");
+  int np;
+  krets_status s = dc_points(c, sweep_elem, start, stop, step, np);
+  if (s != KRETS_OK) return s;
+  if (n_points) *n_points = np;
+  if (np > max_points) return fail(KRETS_ERR_INVALID_ARGUMENT, "x_out too small for the sweep");
+  CU(cudaEventRecord(c->ev[0], c->stream));
+  s = run_dc(c, sweep_elem, start, step, np, 1, nullptr, x_out, c->d_small);
+  if (s != KRETS_OK) return s;
   int h = 0;
   CU(cudaMemcpyAsync(&h, c->d_small, sizeof h, cudaMemcpyDeviceToHost, c->stream));
   CU(cudaEventRecord(c->ev[1], c->stream));
@@ -681,6 +705,35 @@ krets_status krets_dc(krets_circuit *c, int32_t sweep_elem, double start, double
   cudaEventElapsedTime(&c->kernel_ms, c->ev[2], c->ev[3]);
   cudaEventElapsedTime(&c->call_ms, c->ev[0], c->ev[1]);
   return map_status(h, 1);
+}
+
+krets_status krets_batch_dc(krets_circuit *c, int32_t n_inst, const double *values, int32_t sweep_elem,
+                            double start, double stop, double step, double *x_out, int32_t max_points,
+                            int32_t *n_points, int32_t *inst_status) {
+  if (!c || !x_out || n_inst <= 0) return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments");
+  int np;
+  krets_status s = dc_points(c, sweep_elem, start, stop, step, np);
+  if (s != KRETS_OK) return s;
+  if (n_points) *n_points = np;
+  if (np > max_points) return fail(KRETS_ERR_INVALID_ARGUMENT, "x_out too small for the sweep");
+  CU(cudaEventRecord(c->ev[0], c->stream));
+  DevBuf ts;
+  CU(cudaMalloc(&ts.p, sizeof(int) * n_inst));
+  CU(cudaMemsetAsync(ts.p, 0, sizeof(int) * n_inst, c->stream));
+  s = run_dc(c, sweep_elem, start, step, np, n_inst, values, x_out, (int *)ts.p);
+  if (s != KRETS_OK) return s;
+  std::vector<int> st(n_inst);
+  CU(cudaMemcpyAsync(st.data(), ts.p, sizeof(int) * n_inst, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaEventRecord(c->ev[1], c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  cudaEventElapsedTime(&c->kernel_ms, c->ev[2], c->ev[3]);
+  cudaEventElapsedTime(&c->call_ms, c->ev[0], c->ev[1]);
+  int any = 0;
+  for (int i = 0; i < n_inst; ++i) {
+    if (inst_status) inst_status[i] = st[i];
+    any |= st[i];
+  }
+  return map_status(any, 1);
 }
 
 krets_status krets_batch_ac(krets_circuit *c, int32_t n_inst, const double *values, const double *freqs,

@@ -145,8 +145,12 @@ __global__ void k_op(DevProg P, KCfg cfg, Lay L, char *gws, const double *values
 }
 
 // ============================================================== k_dc_sweep
+// Warm-started source sweep (dc.rs:14-124).  One CTA per instance (values NULL: the
+// nominal values, one instance); instance i writes its points at x_out + i * inst_stride
+// and stops at its first failing point, as dc::solve returns on the first error.
 __global__ void k_dc_sweep(DevProg P, KCfg cfg, Lay L, char *gws, int sweep_elem, double start, double step,
-                           int n_points, double *x_out, int *out_status) {
+                           int n_points, const double *values, int n_inst, size_t inst_stride, double *x_out,
+                           int *out_status) {
   extern __shared__ __align__(16) char smem[];
   char *base = gws ? gws + (size_t)blockIdx.x * L.bytes : smem;
   ARR(double, lu, 0);
@@ -157,20 +161,25 @@ __global__ void k_dc_sweep(DevProg P, KCfg cfg, Lay L, char *gws, int sweep_elem
   ARR(double, cb, 5);
   ARR(int, status, 6);
   ARR(double, vals, 7);
-  for (int e = threadIdx.x; e < P.ne; e += blockDim.x) vals[e] = P.el[e].value;
-  if (threadIdx.x == 0) *status = 0;
-  __syncthreads();
-  for (int i = 0; i < n_points; ++i) {
-    if (threadIdx.x == 0) vals[sweep_elem] = start + ((double)i * step);  // dc.rs:157-164
-    // warm start from the previous point's solution (dc.rs:167)
-    for (int k = threadIdx.x; k < P.n; k += blockDim.x) guess[k] = x[k];
+  for (int inst = blockIdx.x; inst < n_inst; inst += gridDim.x) {
+    const double *src = values ? values + (size_t)inst * P.ne : nullptr;
+    for (int e = threadIdx.x; e < P.ne; e += blockDim.x) vals[e] = src ? src[e] : P.el[e].value;
+    if (threadIdx.x == 0) *status = 0;
     __syncthreads();
-    newton_dc(P, cfg, vals, lu, b, x, guess, ca, cb, status, i == 0, (double)i, nullptr);
-    for (int k = threadIdx.x; k < P.n; k += blockDim.x) x_out[(size_t)i * P.n + P.q[k]] = x[k];
+    double *out = x_out + (size_t)inst * inst_stride;
+    for (int i = 0; i < n_points; ++i) {
+      if (threadIdx.x == 0) vals[sweep_elem] = start + ((double)i * step);  // dc.rs:157-164
+      // warm start from the previous point's solution (dc.rs:167)
+      for (int k = threadIdx.x; k < P.n; k += blockDim.x) guess[k] = x[k];
+      __syncthreads();
+      newton_dc(P, cfg, vals, lu, b, x, guess, ca, cb, status, i == 0, (double)i, nullptr);
+      for (int k = threadIdx.x; k < P.n; k += blockDim.x) out[(size_t)i * P.n + P.q[k]] = x[k];
+      __syncthreads();
+      if (*status) break;
+    }
+    if (threadIdx.x == 0) out_status[inst] = *status;
     __syncthreads();
-    if (*status) break;
   }
-  if (threadIdx.x == 0) *out_status = *status;
 }
 
 // ============================================================== k_tran_step (plain form)

@@ -188,6 +188,40 @@ def test_batch_op_monte_carlo(oracle_lib):
         assert rel_err(x[i], oracle_lib.op(ti, c.size), is_current_mask(c)) < TOL
 
 
+DIODE_LADDER = """* diode ladder, DC sweep of V1
+V1 in 0 1
+R1 in a 1000
+D1 a 0 DMOD
+R2 a b 2200
+D2 b 0 DMOD
+R3 b c 470
+D3 c 0 DMOD
+R4 c 0 10000
+.model DMOD D (is=1e-12)
+"""
+
+
+def test_batch_dc_monte_carlo(oracle_lib):
+    """Warm-started nonlinear sweeps of 16 parameter sets: each instance against the oracle's
+    dc::solve restatement with that instance's values."""
+    c = parse_circuit_description(DIODE_LADDER)
+    t = element_table(c)
+    vals = monte_carlo_values(c, 16, seed=7)
+    g = _lib.GpuCircuit(t, c.size)
+    sweep = int(np.nonzero(t["kind"] == 4)[0][0])
+    x, st = g.batch_dc(vals, sweep, -0.5, 3.0, 0.05)
+    assert x.shape == (16, 71, c.size) and not st.any()
+    mask = is_current_mask(c)
+    for i in range(len(vals)):
+        ti = t.copy()
+        ti["value"] = vals[i]
+        ref = oracle_lib.dc(ti, c.size, sweep, -0.5, 3.0, 0.05)
+        assert rel_err(x[i], ref, mask) < TOL, i
+    # one instance with the nominal values equals the single-instance sweep
+    x1, _ = g.batch_dc(t["value"][None, :], sweep, -0.5, 3.0, 0.05)
+    np.testing.assert_array_equal(x1[0], g.dc(sweep, -0.5, 3.0, 0.05))
+
+
 def test_batched_transient_is_deterministic():
     c = rlc_ladder(100)
     t = element_table(c)
