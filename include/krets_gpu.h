@@ -62,10 +62,16 @@ typedef int32_t krets_status;
 #define KRETS_ELEM_I 5 /* current source    value = amperes                                */
 #define KRETS_ELEM_D 6 /* diode             value = saturation current, wp[0] = emission n */
 #define KRETS_ELEM_M 7 /* NMOS level 1      wp = {vto, kp, lambda, w, l}; stamps nothing,
-                          as the reference's bare-name index lookups never match           */
+                          as the reference's bare-name index lookups never match, unless
+                          flags holds KRETS_FLAG_NMOS_RESOLVED                              */
 #define KRETS_ELEM_Q 8 /* BJT               parsed only; solving reports NOT_IMPLEMENTED   */
 
 #define KRETS_FLAG_G2 1
+/* NMOS: resolve drain / source / gate as their V(<node>) unknowns (the reference looks the
+ * bare node names up and stamps nothing: stampable.rs:842-844).  The stamp is then the
+ * reference's own entries and values (stampable.rs:846-866, rhs :870-899) with the
+ * level-1 g_m, g_ds and i_d of nmosfet.rs:51-103, evaluated at the Newton guess. */
+#define KRETS_FLAG_NMOS_RESOLVED 2
 
 #define KRETS_WAVE_NONE 0
 #define KRETS_WAVE_PULSE 1 /* wp = {v1, v2, td, tr, tf, pw, per}  voltage_source.rs:70-93 */

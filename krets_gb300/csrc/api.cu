@@ -183,7 +183,7 @@ static void for_each_array(const Program &H, const ProgramImage &X, F &&f) {
   f(H.el_pos); f(X.is_cur);
   f(H.qinv); f(H.ldesc); f(H.udesc); f(H.res_ptr); f(H.res_op);
   f(H.dyn_e); f(H.bd_ptr); f(H.bd_op); f(H.sprog);
-  f(H.tprog); f(H.prow);
+  f(H.tprog); f(H.prow); f(H.xslot);
 }
 
 static size_t program_bytes(const Program &H, const ProgramImage &X) {
@@ -242,6 +242,8 @@ static void place_program(const Program &H, const ProgramImage &X, const krets_e
   V.sprog = (const int *)nx();
   V.tprog = (const int *)nx();
   V.prow = (const int *)nx();
+  V.xslot = (const int *)nx();
+  V.n_coef = H.n_coef;
   V.el = d_el;
   V.ndyn = (int)H.dyn_e.size();
   V.ncap = H.ncap;
@@ -302,7 +304,7 @@ Lay layout_op(const DevProg &P) {
   B.add(1, sizeof(double) * P.n);
   B.add(2, sizeof(double) * P.n);
   B.add(3, sizeof(double) * P.n);
-  B.add(4, sizeof(double) * P.ne);
+  B.add(4, sizeof(double) * P.n_coef);
   B.add(5, sizeof(double) * P.ne);
   B.add(6, sizeof(int) * 4);
   B.add(7, sizeof(double) * P.ne);
@@ -319,7 +321,7 @@ Lay layout_tran(const DevProg &P, bool mixed) {
   B.add(5, P.nonlinear ? sizeof(double) * P.n : 0);
   B.add(6, sizeof(double) * P.n);
   B.add(7, mixed ? sizeof(float) * P.n : 0);
-  B.add(8, sizeof(double) * P.ne);
+  B.add(8, sizeof(double) * P.n_coef);
   B.add(9, sizeof(double) * P.ne);
   B.add(10, sizeof(double) * P.ne);
   B.add(11, sizeof(double) * 32);
@@ -336,8 +338,8 @@ Lay layout_ac(const DevProg &P, bool mixed) {
   B.add(3, 16 * (size_t)P.n);
   B.add(4, 16 * (size_t)P.n);
   B.add(5, mixed ? 8 * (size_t)P.n : 0);
-  B.add(6, sizeof(double) * P.ne);
-  B.add(7, sizeof(double) * P.ne);
+  B.add(6, sizeof(double) * P.n_coef);
+  B.add(7, sizeof(double) * P.n_coef);
   B.add(8, sizeof(double) * P.ne);
   B.add(9, sizeof(double) * P.n);
   B.add(10, sizeof(double) * 32);
@@ -833,7 +835,7 @@ krets_status krets_tran(krets_circuit *c, double h, int32_t n_steps, int32_t met
   s = dev_view(x_out, out_bytes, false, c->stream, tx, &dx);
   if (s) return s;
   const DevProg &P = Dtr->view;
-  size_t nd = 8 * (size_t)P.n + 3 * (size_t)P.ne + P.nnz_lu + 64;
+  size_t nd = 8 * (size_t)P.n + 2 * (size_t)P.ne + P.n_coef + P.nnz_lu + 64;
   CU(cudaMalloc(&stbuf.p, nd * sizeof(double)));
   CU(cudaMemsetAsync(stbuf.p, 0, nd * sizeof(double), c->stream));
   double *d = (double *)stbuf.p;
@@ -842,7 +844,7 @@ krets_status krets_tran(krets_circuit *c, double h, int32_t n_steps, int32_t met
   st.prev = d; d += P.n;
   st.guess = d; d += P.n;
   st.b = d; d += P.n;
-  st.ca = d; d += P.ne;
+  st.ca = d; d += P.n_coef;
   st.cb = d; d += P.ne;
   st.icap = d; d += P.ne;
   st.lu = d; d += P.nnz_lu;

@@ -79,7 +79,7 @@ struct DevProg {
   const int *a_rowptr;   // [n+1]
   const int *a_col;      // [nnz_a]
   const int *a_cptr;     // [nnz_a+1]
-  const int *a_contrib;  // packed elem<<2 | unit<<1 | neg
+  const int *a_contrib;  // packed slot<<2 | unit<<1 | neg (slot = coefficient slot)
   const int *b_cptr;     // [n+1]
   const int *b_contrib;  // packed elem<<1 | neg
   const int *piv_ptr;    // [n+1]
@@ -89,6 +89,8 @@ struct DevProg {
   const int4 *el_pos;    // p, m, b, g in position space
   const int *is_cur;     // [n] 1 when the unknown at this position is a branch current
   const krets_element *el;
+  const int *xslot;      // [ne] first extra coefficient slot of the element, or -1
+  int n_coef;            // coefficient slots (ne + extra slots)
   int nonlinear;         // any diode / MOSFET / BJT among the stamped elements
   // step program (warp engine)
   const int *qinv;       // [n] unknown -> position
@@ -168,6 +170,34 @@ __device__ __forceinline__ void diode_lin(const krets_element &E, double is, int
   ieq = cur - g * vd;
 }
 
+// NMOS level 1 (nmosfet.rs:51-103) at the Newton guess: V(gate), V(source), V(drain)
+// default to 0 when the solution map lacks them (stampable.rs:825-833); wp = {vto, kp,
+// lambda, w, l}.  Region tests and products in the reference's order.
+__device__ __forceinline__ void nmos_lin(const krets_element &E, int4 pos, const double *guess, bool empty,
+                                         double &gm, double &gds, double &ieq) {
+  const double vg = (!empty && pos.w >= 0) ? guess[pos.w] : 0.0;
+  const double vs = (!empty && pos.y >= 0) ? guess[pos.y] : 0.0;
+  const double vd = (!empty && pos.x >= 0) ? guess[pos.x] : 0.0;
+  const double vgs = vg - vs, vds = vd - vs;
+  const double vth = E.wp[0], beta = E.wp[1] * (E.wp[3] / E.wp[4]), lambda = E.wp[2];
+  double id;
+  if (vgs <= vth) {
+    gm = 0.0; gds = 0.0; id = 0.0;
+  } else if (vds >= 0.0 && vds <= (vgs - vth)) {  // linear region
+    gm = beta * vds;
+    gds = beta * (vgs - vth - vds);
+    id = beta * ((vgs - vth) * vds - (vds * vds / 2.0));
+  } else if (vds >= (vgs - vth) && vds >= 0.0) {  // saturation
+    const double ov = vgs - vth;
+    gm = beta * ov * (1.0 + lambda * vds);
+    gds = (beta / 2.0) * lambda * (ov * ov);
+    id = (beta / 2.0) * (ov * ov) * (1.0 + lambda * vds);
+  } else {
+    gm = 0.0; gds = 0.0; id = 0.0;
+  }
+  ieq = id - gds * vds - gm * vgs;  // stampable.rs:891
+}
+
 struct PassCtx {
   int mode, method;
   double h, freq;
@@ -181,12 +211,15 @@ struct PassCtx {
 // Per-element coefficients of one stamping pass: ca = matrix coefficient (real part in
 // ca_re, imaginary in ca_im), cb = rhs coefficient.  Expressions and operation order follow
 // stampable.rs so the summed entries match the reference's bit for bit (up to exp/sin).
+// x0 / x1: the values of the element's extra slots (resolved NMOS: g_ds, g_m).
 __device__ __forceinline__ void elem_coefs(const krets_element &E, int e, int4 pos, double val,
                                            const PassCtx &c, double &ca_re, double &ca_im, double &cb,
-                                           int &err) {
+                                           double &x0, double &x1, int &err) {
   ca_re = 0.0;
   ca_im = 0.0;
   cb = 0.0;
+  x0 = 0.0;
+  x1 = 0.0;
   switch (E.kind) {
     case KRETS_ELEM_R:
       ca_re = (E.flags & KRETS_FLAG_G2) ? val : 1.0 / val;
@@ -237,7 +270,16 @@ __device__ __forceinline__ void elem_coefs(const krets_element &E, int e, int4 p
       break;
     }
     case KRETS_ELEM_M:
-      if (c.mode == 1) err |= KS_NOTIMPL;
+      if (c.mode == 1) {
+        err |= KS_NOTIMPL;
+      } else if (E.flags & KRETS_FLAG_NMOS_RESOLVED) {
+        double gm, gds, ieq;
+        nmos_lin(E, pos, c.guess, c.guess_empty, gm, gds, ieq);
+        ca_re = gds + gm;
+        x0 = gds;
+        x1 = gm;
+        cb = ieq;
+      }
       break;
     default:
       err |= KS_NOTIMPL;

@@ -51,11 +51,17 @@ __device__ __forceinline__ void coef_pass(const DevProg &P, const double *vals, 
   for (int e = threadIdx.x; e < P.ne; e += blockDim.x) {
     const krets_element &E = P.el[e];
     double val = vals ? vals[e] : E.value;
-    double ar, ai, b;
-    elem_coefs(E, e, P.el_pos[e], val, c, ar, ai, b, err);
+    double ar, ai, b, x0, x1;
+    elem_coefs(E, e, P.el_pos[e], val, c, ar, ai, b, x0, x1, err);
     ca_re[e] = ar;
     if (ca_im) ca_im[e] = ai;
     cb[e] = b;
+    const int xs = P.xslot[e];
+    if (xs >= 0) {
+      ca_re[xs] = x0;
+      ca_re[xs + 1] = x1;
+      if (ca_im) ca_im[xs] = ca_im[xs + 1] = 0.0;
+    }
   }
   if (err) atomicOr(status, err);
 }

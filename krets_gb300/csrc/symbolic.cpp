@@ -25,9 +25,11 @@ struct BEntry { int r, code; };     // code = packed contribution (pack_b)
 
 // Emit the matrix and rhs stamp entries of element e for the mode, in the reference's
 // order.  Returns false for stamps the reference leaves as todo!().
-bool emit(const krets_element &x, int e, int mode, std::vector<MEntry> &M, std::vector<BEntry> &B) {
+// xs: first extra coefficient slot of the element (-1 = none).
+bool emit(const krets_element &x, int e, int xs, int mode, std::vector<MEntry> &M, std::vector<BEntry> &B) {
   const int ip = x.p, im = x.m, ic = x.b;
   auto A = [&](int r, int c, bool unit, bool neg) { M.push_back({r, c, pack_a(e, unit, neg)}); };
+  auto AS = [&](int r, int c, int slot, bool neg) { M.push_back({r, c, pack_a(slot, false, neg)}); };
   auto R = [&](int r, bool neg) { B.push_back({r, pack_b(e, neg)}); };
   switch (x.kind) {
     case KRETS_ELEM_R:  // stampable.rs:203-246
@@ -99,8 +101,21 @@ bool emit(const krets_element &x, int e, int mode, std::vector<MEntry> &M, std::
       if (im >= 0 && ic >= 0) { A(im, ic, true, true); A(ic, im, true, true); }
       if (ic >= 0) R(ic, false);
       return true;
-    case KRETS_ELEM_M:  // stampable.rs:819-922: index lookups by bare node name never match
-      return mode != MODE_AC;
+    case KRETS_ELEM_M: {  // stampable.rs:819-922
+      if (mode == MODE_AC) return false;                      // todo!() (:914-921)
+      if (!(x.flags & KRETS_FLAG_NMOS_RESOLVED)) return true;  // bare-name lookups never match
+      // slot e = g_ds + g_m, xs = g_ds, xs + 1 = g_m; the reference's entries in its order
+      const int d = x.p, src = x.m, g = x.g;
+      if (d >= 0) AS(d, d, xs, false);
+      if (src >= 0) AS(src, src, e, false);
+      if (d >= 0 && src >= 0) { AS(d, src, e, true); AS(src, d, e, false); }
+      if (src >= 0 && g >= 0) AS(src, g, xs + 1, false);
+      if (d >= 0 && g >= 0) AS(d, g, xs + 1, false);
+      // rhs: (source, i_eq), (drain, -i_eq): per-pass rhs coefficient = i_eq
+      if (src >= 0) R(src, false);
+      if (d >= 0) R(d, true);
+      return true;
+    }
     default:
       return false;
   }
@@ -127,6 +142,10 @@ std::complex<double> rep_coef(const krets_element &x, int mode, int method, doub
         double n = x.wp[0] > 0 ? x.wp[0] : 1.0;
         return (x.value / (n * kVt)) * std::exp(std::min(0.5 / (n * kVt), 700.0));
       }
+    case KRETS_ELEM_M:
+      // NMOS conductances are 0 below threshold, which the first Newton iteration sees
+      // (all guesses 0): pivots do not rely on them, as for diodes
+      return rep_diode_zero ? 0.0 : 1.0;
     default:
       return 1.0;
   }
@@ -413,7 +432,8 @@ static int split_code(int rows, int mx) {
 static void pack_step_program(const krets_element *el, Program &P) {
   const int n = P.n;
   P.sprog.clear();
-  P.sprog_ok = n < 32768 && P.ne < 65535 && P.max_row_lu < 32768;
+  // the step-program engines run linear circuits with one coefficient per element
+  P.sprog_ok = n < 32768 && P.ne < 65535 && P.max_row_lu < 32768 && P.n_coef == P.ne;
   if (!P.sprog_ok) return;
   std::vector<int> &S = P.sprog;
   auto mark = [&](int i) {
@@ -608,15 +628,21 @@ static void pack_transposed_program(Program &P) {
 static int build_with_order(const krets_element *el, int ne, int n, int mode, int method, double h, double f,
                             const std::vector<MEntry> &M, const std::vector<BEntry> &B,
                             const std::vector<int> &q, Program &P, std::string &msg, bool rep_diode_zero,
-                            size_t fill_cap = 0, bool update_list = true, bool dense_tail = false) {
+                            const std::vector<int> &xslot, int n_coef, size_t fill_cap = 0,
+                            bool update_list = true, bool dense_tail = false) {
   P = Program();
   P.mode = mode;
   P.method = method;
   P.n = n;
   P.ne = ne;
+  P.xslot = xslot;
+  P.n_coef = n_coef;
   // ---- representative numeric matrix (CSC, summed), for pivot selection
-  std::vector<std::complex<double>> coef(ne);
-  for (int e = 0; e < ne; ++e) coef[e] = rep_coef(el[e], mode, method, h, f, rep_diode_zero);
+  std::vector<std::complex<double>> coef(n_coef);
+  for (int e = 0; e < ne; ++e) {
+    coef[e] = rep_coef(el[e], mode, method, h, f, rep_diode_zero);
+    if (xslot[e] >= 0) coef[xslot[e]] = coef[xslot[e] + 1] = coef[e];
+  }
   std::vector<std::pair<long long, std::complex<double>>> ent;
   ent.reserve(M.size());
   for (auto &m : M) {
@@ -911,6 +937,14 @@ int build_program(const krets_element *el, int ne, int n, int mode, int method, 
   }
   std::vector<MEntry> M;
   std::vector<BEntry> B;
+  // extra coefficient slots: two per resolved NMOS (g_ds, g_m) after the elements' own
+  std::vector<int> xslot(ne, -1);
+  int n_coef = ne;
+  for (int e = 0; e < ne; ++e)
+    if (el[e].kind == KRETS_ELEM_M && (el[e].flags & KRETS_FLAG_NMOS_RESOLVED)) {
+      xslot[e] = n_coef;
+      n_coef += 2;
+    }
   for (int e = 0; e < ne; ++e) {
     const krets_element &x = el[e];
     if (x.p >= n || x.m >= n || x.b >= n || x.g >= n) {
@@ -918,7 +952,7 @@ int build_program(const krets_element *el, int ne, int n, int mode, int method, 
       return KRETS_ERR_INVALID_ARGUMENT;
     }
     if (mode == MODE_DC && x.kind == KRETS_ELEM_C) continue;  // op.rs:20-24
-    if (!emit(x, e, mode, M, B)) {
+    if (!emit(x, e, xslot[e], mode, M, B)) {
       if (x.kind == KRETS_ELEM_Q || x.kind == KRETS_ELEM_M) {
         msg = x.kind == KRETS_ELEM_Q ? "BJT stamps are not implemented in the reference (todo!())"
                                      : "NMOS AC stamp is not implemented in the reference (todo!())";
@@ -961,11 +995,11 @@ int build_program(const krets_element *el, int ne, int n, int mode, int method, 
     }
     Program P;
     std::string m2;
-    int st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, true, fill_cap, update_list,
-                              dense_tail);
-    if (st == KRETS_ERR_DECOMPOSITION_FAILED)  // only singular without diode conductances
-      st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, false, fill_cap, update_list,
-                            dense_tail);
+    int st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, true, xslot, n_coef, fill_cap,
+                              update_list, dense_tail);
+    if (st == KRETS_ERR_DECOMPOSITION_FAILED)  // only singular without diode / NMOS conductances
+      st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, false, xslot, n_coef, fill_cap,
+                            update_list, dense_tail);
     if (st == kFillCapExceeded) continue;
     if (st != KRETS_OK) {
       if (best_st != KRETS_OK) { best_st = st; best_msg = m2; }

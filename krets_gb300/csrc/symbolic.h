@@ -18,9 +18,11 @@ namespace krets {
 
 enum Mode { MODE_DC = 0, MODE_AC = 1, MODE_TRAN = 2 };
 
-// A matrix stamp contribution, packed as  elem << 2 | unit << 1 | neg:
-//   unit = 1 -> the value is the constant 1 (KCL/KVL incidence), else the element's
-//   per-pass matrix coefficient; neg = 1 -> negated.
+// A matrix stamp contribution, packed as  slot << 2 | unit << 1 | neg:
+//   unit = 1 -> the value is the constant 1 (KCL/KVL incidence), else the per-pass matrix
+//   coefficient in slot `slot`; neg = 1 -> negated.  Slot e is element e's coefficient;
+//   elements with more than one distinct matrix value (a resolved NMOS: g_ds + g_m, g_ds,
+//   g_m) take their further values from slots ne, ne + 1, ... (Program::xslot).
 // A right-hand-side contribution, packed as elem << 1 | neg (value = element's
 // per-pass rhs coefficient).
 inline int pack_a(int e, bool unit, bool neg) { return (e << 2) | (unit ? 2 : 0) | (neg ? 1 : 0); }
@@ -49,6 +51,9 @@ struct Program {
   std::vector<int> lev_ptr, lev_rows, ulev_ptr, ulev_rows;
   // per element: p, m, b, g in POSITION space (-1 = absent)
   std::vector<int> el_pos;
+  // per element: first of its extra coefficient slots (-1 = none); n_coef = slots in all
+  std::vector<int> xslot;
+  int n_coef = 0;
   // --- step program (used by the warp-per-instance engine)
   // level-ordered row descriptors {row, first entry, diag slot, end}: L solve / U solve
   std::vector<int> ldesc, udesc;

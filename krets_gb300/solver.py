@@ -59,10 +59,12 @@ def _round_half_away(x: float) -> int:
 class Solver:
     """Owns the circuit and its compiled device topology (solver.rs:17-25)."""
 
-    def __init__(self, circuit: Circuit, config: SolverConfig | None = None):
+    def __init__(self, circuit: Circuit, config: SolverConfig | None = None, nmos_resolved: bool = False):
+        """nmos_resolved: stamp NMOS devices (the reference's stamp with its node lookups
+        resolved); the default reproduces the reference, whose NMOS stamps nothing."""
         self.circuit = circuit
         self.config = config or SolverConfig()
-        self.table = element_table(circuit)
+        self.table = element_table(circuit, nmos_resolved)
         self.names = circuit.names_by_index()
         self.gpu = _lib.GpuCircuit(self.table, circuit.size, self.config)
 

@@ -20,9 +20,13 @@ ELEM_DTYPE = np.dtype([
 assert ELEM_DTYPE.itemsize == 104
 
 FLAG_G2 = 1
+FLAG_NMOS_RESOLVED = 2
 
 
-def element_table(circuit: Circuit) -> np.ndarray:
+def element_table(circuit: Circuit, nmos_resolved: bool = False) -> np.ndarray:
+    """Flatten the circuit into krets_element records.  nmos_resolved: NMOS devices stamp
+    with their nodes resolved as V(<node>) (the reference looks bare names up and stamps
+    nothing, stampable.rs:842-844)."""
     im = circuit.index_map
     t = np.zeros(len(circuit.elements), dtype=ELEM_DTYPE)
     for k, el in enumerate(circuit.elements):
@@ -45,6 +49,8 @@ def element_table(circuit: Circuit) -> np.ndarray:
             rec["p"] = im.get(f"V({el.nodes[0]})", -1)
             rec["m"] = im.get(f"V({el.nodes[1]})", -1)
         rec["flags"] = FLAG_G2 if el.g2 else 0
+        if el.kind == KIND_M and nmos_resolved:
+            rec["flags"] |= FLAG_NMOS_RESOLVED
         rec["value"] = el.value
         if el.kind == KIND_V:
             rec["ac"] = el.ac

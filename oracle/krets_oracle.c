@@ -47,6 +47,7 @@
 enum { K_R = 1, K_C = 2, K_L = 3, K_V = 4, K_I = 5, K_D = 6, K_M = 7, K_Q = 8 };
 enum { W_NONE = 0, W_PULSE = 1, W_SIN = 2 };
 #define F_G2 1
+#define F_NMOS_RESOLVED 2 /* NMOS nodes looked up as V(<node>) (the reference: bare names) */
 
 /* Same 104-byte layout as the element record of the product's C ABI. */
 typedef struct ko_elem {
@@ -131,6 +132,32 @@ static double ko_diode_ieq(const ko_elem *e, const double *guess) {
   double n = e->wp[0], is = e->value;
   double cur = is * (exp(vdl / (n * KO_VT)) - 1.0);
   return cur - ko_diode_g(e, guess) * ko_diode_vd(e, guess);
+}
+
+/* NMOS level 1, nmosfet.rs:51-103 (g_m :51-66, g_ds :68-84, i_d :86-102) with
+ * beta = kp * (w / l) (models/nmosfet.rs:41-43); wp = {vto, kp, lambda, w, l}.  Terminal
+ * voltages come from the solution map with unwrap_or(0.0) (stampable.rs:825-833). */
+static void ko_nmos(const ko_elem *e, const double *guess, double *gm, double *gds, double *id, double *vgs_out,
+                    double *vds_out) {
+  double vg = (guess && e->g >= 0) ? guess[e->g] : 0.0;
+  double vs = (guess && e->m >= 0) ? guess[e->m] : 0.0;
+  double vd = (guess && e->p >= 0) ? guess[e->p] : 0.0;
+  double vgs = vg - vs, vds = vd - vs;
+  double vth = e->wp[0], beta = e->wp[1] * (e->wp[3] / e->wp[4]), lambda = e->wp[2];
+  *gm = *gds = *id = 0.0;
+  if (vgs <= vth) {
+  } else if (vds >= 0.0 && vds <= (vgs - vth)) {
+    *gm = beta * vds;
+    *gds = beta * (vgs - vth - vds);
+    *id = beta * ((vgs - vth) * vds - (vds * vds / 2.0));
+  } else if (vds >= (vgs - vth) && vds >= 0.0) {
+    double ov = vgs - vth;
+    *gm = beta * ov * (1.0 + lambda * vds);
+    *gds = (beta / 2.0) * lambda * (ov * ov);
+    *id = (beta / 2.0) * (ov * ov) * (1.0 + lambda * vds);
+  }
+  *vgs_out = vgs;
+  *vds_out = vds;
 }
 
 /* ------------------------------------------------------------ triplets */
@@ -279,9 +306,23 @@ static int ko_stamp(const ko_elem *e, int ei, const ko_ctx *x, ko_tlist *G, ko_t
       }
       return 0;
     }
-    case K_M:
+    case K_M: {
       if (x->mode == MODE_AC) return KO_NOTIMPL; /* stampable.rs:914-921 todo!() */
-      return 0; /* bare-name index lookups never match (stampable.rs:842-844) */
+      if (!(e->flags & F_NMOS_RESOLVED)) return 0; /* bare-name lookups never match (:842-844) */
+      /* stampable.rs:846-866 and :870-899 with the lookups resolved */
+      double gm, gds, id, vgs, vds;
+      ko_nmos(e, x->guess, &gm, &gds, &id, &vgs, &vds);
+      int d = e->p, src = e->m, g = e->g;
+      if (d >= 0) PUSH(G, d, d, gds);
+      if (src >= 0) PUSH(G, src, src, gds + gm);
+      if (d >= 0 && src >= 0) { PUSH(G, d, src, -(gds + gm)); PUSH(G, src, d, gds + gm); }
+      if (src >= 0 && g >= 0) PUSH(G, src, g, gm);
+      if (d >= 0 && g >= 0) PUSH(G, d, g, gm);
+      double ieq = id - gds * vds - gm * vgs;
+      if (src >= 0) PUSH(E, src, 0, ieq);
+      if (d >= 0) PUSH(E, d, 0, -ieq);
+      return 0;
+    }
     case K_Q:
       return KO_NOTIMPL; /* stampable.rs:321-357 todo!() */
   }
