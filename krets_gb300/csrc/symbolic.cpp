@@ -867,7 +867,8 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
     for (int e = 0; e < ne; ++e) {
       int k = el[e].kind;
       bool cap = k == KRETS_ELEM_C;
-      bool dyn = cap || k == KRETS_ELEM_L || k == KRETS_ELEM_V || k == KRETS_ELEM_I || k == KRETS_ELEM_D;
+      bool dyn = cap || k == KRETS_ELEM_L || k == KRETS_ELEM_V || k == KRETS_ELEM_I || k == KRETS_ELEM_D ||
+                 (k == KRETS_ELEM_M && (el[e].flags & KRETS_FLAG_NMOS_RESOLVED));
       if (!dyn || (pass == 0) != cap) continue;
       if (mode == MODE_DC && cap) continue;
       dyn_of[e] = (int)P.dyn_e.size();

@@ -122,6 +122,49 @@ def test_default_keeps_the_reference_no_stamp(oracle_lib):
     assert np.all(x[:, c.index_map["V(S)"]] == 0.0)
 
 
+def test_program_wires_the_nmos_coefficient_slots(oracle_lib):
+    """The exported DC program, walked by the CPU emulator with the extended coefficient
+    vector (slot e = g_ds + g_m, then g_ds, g_m after the elements' own slots), performs
+    the same Newton step as the dense restatement from the same guess."""
+    from program_emulator import element_coefs, emulate, export
+    c = _inverter()
+    n = c.size
+    t = element_table(c, nmos_resolved=True)
+    t["value"][next(k for k, el in enumerate(c.elements) if el.identifier == "V1")] = 0.8
+    guess = oracle_lib.op(t, n) + 0.01   # a point where the device conducts
+    ca, cb = element_coefs(t, 0)
+    ne = len(t)
+    ca = np.concatenate([ca, np.zeros(2, dtype=complex)])
+    e = next(k for k, el in enumerate(c.elements) if el.kind == 7)
+    gm, gds, idd, vgs, vds = _nmos_lin(t["wp"][e], guess[t["g"][e]], guess[t["m"][e]], guess[t["p"][e]])
+    assert gm > 0 and gds > 0
+    ca[e], ca[ne], ca[ne + 1] = gds + gm, gds, gm
+    cb[e] = idd - gds * vds - gm * vgs
+    x = emulate(export(t, n, 0), t, n, ca, cb)
+    # dense: one iteration of _dense_dc_sweep's body from `guess`
+    A = np.zeros((n, n))
+    b = np.zeros(n)
+    for k, el in enumerate(t):
+        p, m, br = int(el["p"]), int(el["m"]), int(el["b"])
+        if el["kind"] == 1:
+            for r, cc, sg in ((p, p, 1), (m, m, 1), (p, m, -1), (m, p, -1)):
+                if r >= 0 and cc >= 0:
+                    A[r, cc] += sg / el["value"]
+        elif el["kind"] == 4:
+            for r, cc, sg in ((p, br, 1), (br, p, 1), (m, br, -1), (br, m, -1)):
+                if r >= 0 and cc >= 0:
+                    A[r, cc] += sg
+            b[br] += el["value"]
+    d, src, g = int(t["p"][e]), int(t["m"][e]), int(t["g"][e])
+    for r, cc, val in ((d, d, gds), (src, src, gds + gm), (d, src, -(gds + gm)), (src, d, gds + gm),
+                       (src, g, gm), (d, g, gm)):
+        if r >= 0 and cc >= 0:
+            A[r, cc] += val
+    b[src] += cb[e]
+    b[d] -= cb[e]
+    np.testing.assert_allclose(x.real, np.linalg.solve(A, b), rtol=1e-12, atol=1e-15)
+
+
 def test_flag_only_on_nmos():
     c = parse_circuit_description(COMMON_SOURCE)
     t = element_table(c, nmos_resolved=True)
