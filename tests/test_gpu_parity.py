@@ -243,6 +243,48 @@ def test_errors_are_reported():
         Solver(c).solve(DcAnalysis("V9", 0, 1, 0.5))
 
 
+@pytest.mark.parametrize("precision", [_lib.PREC_FP64, _lib.PREC_MIXED, _lib.PREC_DF])
+def test_batched_failure_stays_with_its_instance(oracle_lib, precision):
+    """A parameter set that makes the matrix non-finite (a 0-ohm resistor) fails alone: its
+    status is set, the call reports the failure, and every other instance still matches
+    the oracle."""
+    import ctypes
+    c = rlc_ladder(30)
+    t = element_table(c)
+    vals = monte_carlo_values(c, 6, seed=9)
+    bad = 3
+    vals[bad, int(np.nonzero(t["kind"] == 1)[0][4])] = 0.0
+    g = _lib.GpuCircuit(t, c.size)
+    n_steps = 200
+    out = _lib.host_buffer((6, n_steps + 1, c.size))
+    st = np.zeros(6, dtype=np.int32)
+    rc = _lib.lib().krets_batch_tran(g.h, 6, _lib.ptr(vals), 1e-12, n_steps, 1, 0, precision, _lib.ptr(out),
+                                     _lib.ptr(st))
+    assert rc != 0 and st[bad] != 0
+    assert not np.delete(st, bad).any()
+    mask = is_current_mask(c)
+    for i in range(6):
+        if i == bad:
+            continue
+        ti = t.copy()
+        ti["value"] = vals[i]
+        ref = oracle_lib.tran(ti, c.size, 1e-12, n_steps, method="tr", lag=False)
+        assert rel_err(out[i], ref, mask) < TOL, i
+
+
+def test_zero_step_transient_is_the_operating_point(oracle_lib):
+    """stop_time < time_step / 2 gives num_steps = 0: the result is the t = 0 operating
+    point alone (transient.rs:14-114)."""
+    c = rlc_ladder(10)
+    t = element_table(c)
+    g = _lib.GpuCircuit(t, c.size)
+    x = g.tran(1e-12, 0, "be")
+    assert x.shape == (1, c.size)
+    np.testing.assert_allclose(x[0], oracle_lib.op(t, c.size), rtol=1e-12, atol=1e-15)
+    xb = g.batch_tran(monte_carlo_values(c, 3, seed=1), 1e-12, 0, "tr", precision=_lib.PREC_DF)
+    assert xb.shape == (3, 1, c.size)
+
+
 def test_batched_transient_host_and_device_outputs_identical():
     """Host output buffers (used in place when the GPU shares the host page tables, else
     through a device copy) give the same bits as a device buffer."""

@@ -27,6 +27,30 @@ def test_library_exports_every_declared_symbol(built_lib):
         assert hasattr(lib, nm), nm
 
 
+def test_circuit_create_checks_arguments_before_the_device(built_lib):
+    """krets_circuit_create validates the element records before it touches CUDA, and
+    without a usable GPU it fails with KRETS_ERR_CUDA (there is no CPU fallback)."""
+    import ctypes
+    from krets_gb300 import _lib
+    L = _lib.lib()
+    c = parse_circuit_description("V1 a 0 1\nR1 a b 1000\nR2 b 0 1000\n")
+    t = element_table(c)
+    h = ctypes.c_void_p()
+    bad = t.copy()
+    bad["kind"][1] = 42
+    assert L.krets_circuit_create(_lib.ptr(bad), len(bad), c.size, None, ctypes.byref(h)) == 3
+    assert b"unknown element kind" in L.krets_last_error_message()
+    bad = t.copy()
+    bad["m"][2] = c.size
+    assert L.krets_circuit_create(_lib.ptr(bad), len(bad), c.size, None, ctypes.byref(h)) == 11
+    assert L.krets_circuit_create(_lib.ptr(t), len(t), 0, None, ctypes.byref(h)) == 11
+    st = L.krets_circuit_create(_lib.ptr(t), len(t), c.size, None, ctypes.byref(h))
+    if st == 0:                       # a GPU is present
+        assert L.krets_circuit_destroy(h) == 0
+    else:
+        assert st == 10 and b"no CPU fallback" in L.krets_last_error_message()
+
+
 @pytest.mark.parametrize("ordering", [-1, 0, 1, 2])
 def test_op_programs_match_oracle(built_lib, oracle_lib, golden, ordering):
     for case in golden["op"]:
