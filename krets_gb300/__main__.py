@@ -3,8 +3,8 @@
 As the reference CLI (crates/krets-cli/src/main.rs:27-138): read the krets.toml analysis
 spec, resolve the circuit path relative to the krets file (else as given, if absolute),
 parse the netlist, solve with the default SolverConfig on the GPU, and write
-result.parquet next to the krets file.  The reference's GUI (krets-gui) is not part of
-this build; --gui is accepted and reported as unavailable.
+result.parquet next to the krets file.  The reference's GUI (krets-gui) has no
+counterpart in this package; --gui is accepted and reported as unavailable.
 """
 from __future__ import annotations
 
@@ -46,7 +46,7 @@ def run(krets_file, solver_factory=None) -> Path:
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(prog="krets", description="SPICE-like circuit simulator (GB300 solve path)")
     ap.add_argument("krets_file")
-    ap.add_argument("-g", "--gui", action="store_true", help="not available in this build")
+    ap.add_argument("-g", "--gui", action="store_true", help="not available (no GUI in this package)")
     ap.add_argument("-l", "--log-level", default="info")
     a = ap.parse_args(argv)
     logging.basicConfig(level=getattr(logging, a.log_level.upper(), logging.INFO), format="%(message)s")
@@ -56,7 +56,7 @@ def main(argv=None) -> int:
         log.info("Error: %s", e)
         return 1
     if a.gui:
-        log.info("The GUI is not part of this build.")
+        log.info("The GUI is not part of this package.")
     return 0
 
 
