@@ -85,6 +85,17 @@ size_t max_smem_optin() {
   return (size_t)v;
 }
 
+size_t max_smem_per_sm() {
+  static int v = -1;
+  if (v < 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess)
+      v = 64 * 1024;
+  }
+  return (size_t)v;
+}
+
 bool is_device_ptr(const void *p) {
   if (!p) return false;
   cudaPointerAttributes a{};
@@ -1575,10 +1586,8 @@ krets_status krets_multi_create(int32_t n_circuits, const krets_element *elems, 
     if (k.items.empty()) continue;
     CU(cudaStreamCreateWithFlags(&k.stream, cudaStreamNonBlocking));
     CU(cudaEventCreate(&k.done));
-    const int per_sm = k.global ? 2 : 1;
-    k.grid = std::max(1, std::min(((int)k.items.size() + k.W - 1) / k.W, per_sm * device_sm_count()));
+    int per_sm = 1;
     if (k.global) {
-      gscratch_bytes = k.region * k.grid * k.W;
       // shared memory of a global-class group (half an SM's, two groups per SM): during the
       // steps a staging tile, x and the rhs coefficients, with the dense-block row slots at
       // the end; during the set-up the same bytes hold the factorisation's row staging
@@ -1598,9 +1607,17 @@ krets_status krets_multi_create(int32_t n_circuits, const krets_element *elems, 
           }
           need = std::max(need, std::max(step, stage));
         }
-      k.x_smem = need <= smax / 2;
+      // three groups per SM (the kernel is built for 80 registers a thread) when their
+      // shared memory fits a third of the SM's, else two: the class is latency bound, so
+      // resident groups set its throughput (4096 uneven netlists: 3.5 s -> 3.0 s); four
+      // would leave x in global memory and the dense-block tiles small, which is slower
+      const long long third = (long long)(max_smem_per_sm() / 3) - 1024;
+      per_sm = need <= third ? 3 : 2;
+      k.x_smem = need <= (per_sm == 3 ? third : smax / 2);
       k.gsm = k.x_smem ? need : kStageBytes;
     }
+    k.grid = std::max(1, std::min(((int)k.items.size() + k.W - 1) / k.W, per_sm * device_sm_count()));
+    if (k.global) gscratch_bytes = k.region * k.grid * k.W;
     all_items.insert(all_items.end(), k.items.begin(), k.items.end());
   }
   CU(cudaMalloc(&m->d_items, sizeof(int) * all_items.size()));

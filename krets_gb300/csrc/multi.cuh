@@ -53,8 +53,9 @@ __host__ __device__ inline MLay multi_lay(int nnz_lu, int n, int ndyn, int ncap,
 // memory.
 constexpr int kStageBytes = 32 * 33 * 8;
 
+// GLOBAL: one 256-thread group per CTA, three CTAs per SM (80 registers a thread).
 template <int G, bool GLOBAL>
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(GLOBAL ? 256 : 512, GLOBAL ? 3 : 1)
     k_multi_tran(const DevProg *__restrict__ progs, const int *__restrict__ items, int n_items,
                  const long long *__restrict__ x_off, long long region_bytes, char *gscratch, int gsm_bytes,
                  int x_smem, double h, int n_steps, int method, int lag, double *x_out, int *circ_status,
