@@ -160,6 +160,24 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
                               double *x_out /* [n_inst][n_steps+1][n] */,
                               int32_t *inst_status /* [n_inst] or NULL */);
 
+/* Transient with local-truncation-error step control (extension: krets steps at a fixed
+ * h, transient.rs:14-114).  From the operating point at t = 0 to t_stop, FP64, per
+ * instance: each attempt solves the companion system at t + h (sources at t + h; Newton
+ * for nonlinear circuits), estimates the LTE by divided differences over the last
+ * accepted points (BE: h^2 DD2, TR: h^3/2 DD3) and accepts it when
+ * max_k |LTE_k| / (lte_tol max(|x_k|, |x_prev,k|) + abstol_k) <= 1 (abstol: the config's
+ * current / voltage tolerance).  h then changes by the largest factor of {2, 1.5, 1, 0.75,
+ * 0.5} (after an accept) or {0.5, 0.25, 0.125} (after a reject; 0.125 when Newton does not
+ * converge) whose predicted ratio stays <= 1/2, within [h_min, h_max]; the first 1 (BE) or
+ * 2 (TR) steps are taken at h0 unchecked.  Accepted points: t_out[n_inst][max_points],
+ * x_out[n_inst][max_points][n] (row 0 = operating point), n_points[n_inst].  A step below
+ * h_min stops the instance (KRETS_ERR_UNEXPECTED); more points than max_points stops it
+ * with KRETS_ERR_INVALID_ARGUMENT.  values may be NULL (one instance, nominal values). */
+krets_status krets_batch_tran_adaptive(krets_circuit *c, int32_t n_inst, const double *values, double h0,
+                                       double t_stop, int32_t method, double lte_tol, double h_min, double h_max,
+                                       int32_t max_points, double *t_out, double *x_out, int32_t *n_points,
+                                       int32_t *inst_status);
+
 /* Batched AC over frequency points of one instance (values NULL) or of several
  * instances: each work item is one (instance, frequency) complex system.
  * precision: FP64 = complex128 factor; MIXED = complex64 factor + complex128 refinement.

@@ -78,6 +78,7 @@ def lib():
             "krets_direct_host_access": [],
             "krets_batch_op": [_P, _I, _P, _P, _P],
             "krets_batch_dc": [_P, _I, _P, _I, _D, _D, _D, _P, _I, _P, _P],
+            "krets_batch_tran_adaptive": [_P, _I, _P, _D, _D, _I, _D, _D, _D, _I, _P, _P, _P, _P],
             "krets_last_timing": [_P, _P, _P],
             "krets_last_refine_stats": [_P, _P, _P],
             "krets_device_alloc": [ctypes.c_size_t, _P],
@@ -296,6 +297,26 @@ class GpuCircuit:
         check(lib().krets_batch_dc(self.h, ni, ptr(v), sweep_index, start, stop, step, ptr(x), npts,
                                    ctypes.byref(got), ptr(st)), "batch_dc")
         return x[:, :got.value], st
+
+    def batch_tran_adaptive(self, values, h0, t_stop, method="tr", lte_tol=1e-3, h_min=None, h_max=None,
+                            max_points=20000, n_inst=None):
+        """Truncation-error step control: per instance (t[points], x[points][n]) and statuses.
+        values None runs one instance with the nominal values."""
+        m = METHOD[method]
+        h_min = h0 * 1e-6 if h_min is None else h_min
+        h_max = t_stop if h_max is None else h_max
+        if values is None:
+            ni = 1 if n_inst is None else n_inst
+        else:
+            values = np.ascontiguousarray(values, dtype=np.float64)
+            ni = values.shape[0]
+        t = host_buffer((ni, max_points))
+        x = host_buffer((ni, max_points, self.n))
+        npts = np.zeros(ni, dtype=np.int32)
+        st = np.zeros(ni, dtype=np.int32)
+        rc = lib().krets_batch_tran_adaptive(self.h, ni, ptr(values), h0, t_stop, m, lte_tol, h_min, h_max,
+                                             max_points, ptr(t), ptr(x), ptr(npts), ptr(st))
+        return [(t[i, :npts[i]], x[i, :npts[i]]) for i in range(ni)], st, rc
 
     def batch_tran(self, values, h, n_steps, method="tr", lag=None, precision=PREC_MIXED, out=None,
                    n_inst=None):

@@ -341,6 +341,22 @@ Lay layout_tran(const DevProg &P, bool mixed) {
   return B.done();
 }
 
+Lay layout_adaptive(const DevProg &P) {
+  LayBuilder B;
+  B.add(0, sizeof(double) * P.ne);
+  B.add(1, sizeof(double) * P.nnz_lu);
+  B.add(2, sizeof(double) * P.n);
+  B.add(3, sizeof(double) * P.n);
+  B.add(4, sizeof(double) * P.n);
+  B.add(5, sizeof(double) * P.n_coef);
+  B.add(6, sizeof(double) * P.ne);
+  B.add(7, sizeof(double) * P.ne);
+  B.add(8, sizeof(double) * 32);
+  B.add(9, sizeof(int) * 4);
+  B.add(10, sizeof(double) * P.n);
+  return B.done();
+}
+
 Lay layout_ac(const DevProg &P, bool mixed) {
   LayBuilder B;
   B.add(0, sizeof(double) * P.ne);
@@ -388,6 +404,8 @@ krets_status map_status(int bits, int mode_for_decomp) {
                 "zero or non-finite pivot during factorisation");
   if (bits & KS_MAXITER) return fail(KRETS_ERR_MAX_ITERATIONS, "maximum Newton iterations exceeded");
   if (bits & KS_STALL) return fail(KRETS_ERR_PIVOT_UNSTABLE, "iterative refinement stalled");
+  if (bits & KS_TSTEP) return fail(KRETS_ERR_UNEXPECTED, "time step fell below h_min");
+  if (bits & KS_FULL) return fail(KRETS_ERR_INVALID_ARGUMENT, "more accepted time points than max_points");
   return KRETS_OK;
 }
 
@@ -747,6 +765,68 @@ krets_status krets_batch_dc(krets_circuit *c, int32_t n_inst, const double *valu
     any |= st[i];
   }
   return map_status(any, 1);
+}
+
+krets_status krets_batch_tran_adaptive(krets_circuit *c, int32_t n_inst, const double *values, double h0,
+                                       double t_stop, int32_t method, double lte_tol, double h_min, double h_max,
+                                       int32_t max_points, double *t_out, double *x_out, int32_t *n_points,
+                                       int32_t *inst_status) {
+  if (!c || !t_out || !x_out || !n_points || n_inst <= 0 || max_points < 2 || !(h0 > 0) || !(t_stop > 0) ||
+      !(lte_tol > 0) || !(h_min > 0) || !(h_min <= h0) || !(h_max >= h0) ||
+      (method != KRETS_METHOD_BE && method != KRETS_METHOD_TR))
+    return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments to krets_batch_tran_adaptive");
+  DevProgram *Ddc, *Dtr;
+  krets_status s = get_program(c, MODE_DC, 0, 0, 0, &Ddc);
+  if (s != KRETS_OK) return s;
+  s = get_program(c, MODE_TRAN, method, h0, 0, &Dtr);  // pivots chosen at h0
+  if (s != KRETS_OK) return s;
+  CU(cudaEventRecord(c->ev[0], c->stream));
+  const size_t stride = (size_t)c->n * max_points;
+  DevBuf tv, tx, tt, tn, ts;
+  void *dv, *dx, *dt, *dn;
+  s = dev_view(values, sizeof(double) * c->ne * (size_t)n_inst, true, c->stream, tv, &dv);
+  if (s) return s;
+  s = dev_view(x_out, sizeof(double) * stride * n_inst, false, c->stream, tx, &dx);
+  if (s) return s;
+  s = dev_view(t_out, sizeof(double) * (size_t)max_points * n_inst, false, c->stream, tt, &dt);
+  if (s) return s;
+  s = dev_view(n_points, sizeof(int) * (size_t)n_inst, false, c->stream, tn, &dn);
+  if (s) return s;
+  CU(cudaMalloc(&ts.p, sizeof(int) * 2 * (size_t)n_inst));
+  int *d_st = (int *)ts.p, *d_opst = d_st + n_inst;
+  CU(cudaMemsetAsync(ts.p, 0, sizeof(int) * 2 * (size_t)n_inst, c->stream));
+  CU(cudaEventRecord(c->ev[2], c->stream));
+  s = run_op(c, Ddc, n_inst, (const double *)dv, (double *)dx, stride, d_opst, nullptr, 128);
+  if (s) return s;
+  const DevProg &P = Dtr->view;
+  Lay L = layout_adaptive(P);
+  int threads = plain_threads(P), grid;
+  size_t smem;
+  char *gws;
+  s = plan_launch(c, k_tran_adaptive, L, threads, n_inst, grid, smem, gws);
+  if (s) return s;
+  k_tran_adaptive<<<grid, threads, smem, c->stream>>>(P, c->cfg, L, gws, (const double *)dv, n_inst, h0, t_stop,
+                                                      method, lte_tol, h_min, h_max, max_points, (double *)dt,
+                                                      (double *)dx, (int *)dn, d_st);
+  g_launches++;
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(c->ev[3], c->stream));
+  if (tx.p) CU(cudaMemcpyAsync(x_out, dx, sizeof(double) * stride * n_inst, cudaMemcpyDeviceToHost, c->stream));
+  if (tt.p) CU(cudaMemcpyAsync(t_out, dt, sizeof(double) * max_points * (size_t)n_inst, cudaMemcpyDeviceToHost, c->stream));
+  if (tn.p) CU(cudaMemcpyAsync(n_points, dn, sizeof(int) * (size_t)n_inst, cudaMemcpyDeviceToHost, c->stream));
+  std::vector<int> st(2 * (size_t)n_inst);
+  CU(cudaMemcpyAsync(st.data(), d_st, sizeof(int) * 2 * (size_t)n_inst, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaEventRecord(c->ev[1], c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  cudaEventElapsedTime(&c->kernel_ms, c->ev[2], c->ev[3]);
+  cudaEventElapsedTime(&c->call_ms, c->ev[0], c->ev[1]);
+  int any = 0;
+  for (int i = 0; i < n_inst; ++i) {
+    const int v = st[i] | st[n_inst + i];
+    if (inst_status) inst_status[i] = v;
+    any |= v;
+  }
+  return map_status(any, 0);
 }
 
 krets_status krets_batch_ac(krets_circuit *c, int32_t n_inst, const double *values, const double *freqs,

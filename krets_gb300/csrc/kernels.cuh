@@ -8,6 +8,8 @@
 //   k_tran_batch   batched transient: persistent CTAs draw instances from a device work
 //                  queue and run the whole step loop with factors and state in shared
 //                  memory; FP64 or FP32-factor + FP64-refinement
+//   k_tran_adaptive batched transient with truncation-error step control (extension),
+//                  FP64, one CTA per instance
 //   k_ac_batch     batched AC: one (instance, frequency) complex system per work item;
 //                  complex128 or complex64-factor + complex128 refinement (ac.rs:39-107)
 #pragma once
@@ -184,6 +186,189 @@ __global__ void k_dc_sweep(DevProg P, KCfg cfg, Lay L, char *gws, int sweep_elem
       if (*status) break;
     }
     if (threadIdx.x == 0) out_status[inst] = *status;
+    __syncthreads();
+  }
+}
+
+// ============================================================== k_tran_adaptive
+// Transient with local-truncation-error step control (an extension: krets steps at a
+// fixed h).  One CTA per instance, FP64 throughout: each attempt stamps and refactors when
+// h changed (or every Newton iteration for nonlinear circuits), solves, and estimates the
+// LTE by divided differences over the attempt and the last accepted points
+//   BE: LTE = h^2 DD2,  TR: LTE = h^3/2 DD3,
+// r = max_k |LTE_k| / (lte_tol max(|x_k|, |x_n,k|) + abstol_k); r <= 1 accepts.  The step
+// factor is the largest of a fixed set with r f^(p+1) <= 1/2 (adapt_factor), so the time
+// grid is exact binary arithmetic.  Accepted points go to t_out / x_out (row 0 = the
+// operating point, written before the launch); the history for the divided differences is
+// read back from those rows.
+#define KS_TSTEP 128  // the step fell below h_min
+#define KS_FULL 256   // more accepted points than max_points
+
+__device__ __forceinline__ double adapt_factor(double r, int order, bool accepted) {
+  if (accepted) {
+    const double fa[5] = {2.0, 1.5, 1.0, 0.75, 0.5};
+    const double p2[5] = {4.0, 2.25, 1.0, 0.5625, 0.25}, p3[5] = {8.0, 3.375, 1.0, 0.421875, 0.125};
+    for (int i = 0; i < 5; ++i)
+      if (r * (order == 1 ? p2[i] : p3[i]) <= 0.5) return fa[i];
+    return 0.5;
+  }
+  const double fr[3] = {0.5, 0.25, 0.125};
+  const double p2[3] = {0.25, 0.0625, 0.015625}, p3[3] = {0.125, 0.015625, 0.001953125};
+  for (int i = 0; i < 3; ++i)
+    if (r * (order == 1 ? p2[i] : p3[i]) <= 0.5) return fr[i];
+  return 0.125;
+}
+
+__global__ void k_tran_adaptive(DevProg P, KCfg cfg, Lay L, char *gws, const double *values, int n_inst, double h0,
+                                double t_stop, int method, double lte_tol, double h_min, double h_max,
+                                int max_points, double *t_out, double *x_out, int *n_points, int *inst_status) {
+  extern __shared__ __align__(16) char smem[];
+  char *base = gws ? gws + (size_t)blockIdx.x * L.bytes : smem;
+  ARR(double, vals, 0);
+  ARR(double, lu, 1);
+  ARR(double, x, 2);
+  ARR(double, guess, 3);
+  ARR(double, b, 4);
+  ARR(double, ca, 5);
+  ARR(double, cb, 6);
+  ARR(double, icap, 7);
+  ARR(double, red, 8);
+  ARR(int, status, 9);
+  ARR(double, xn, 10);
+  const bool trap = method == KRETS_METHOD_TR;
+  const int order = trap ? 2 : 1;
+  for (int inst = blockIdx.x; inst < n_inst; inst += gridDim.x) {
+    double *xo = x_out + (size_t)inst * max_points * P.n;
+    double *to = t_out + (size_t)inst * max_points;
+    for (int e = threadIdx.x; e < P.ne; e += blockDim.x) {
+      vals[e] = values ? values[(size_t)inst * P.ne + e] : P.el[e].value;
+      icap[e] = 0.0;
+    }
+    for (int k = threadIdx.x; k < P.n; k += blockDim.x) xn[k] = xo[P.q[k]];
+    if (threadIdx.x == 0) {
+      *status = 0;
+      to[0] = 0.0;
+    }
+    __syncthreads();
+    double t = 0.0, h = fmin(h0, h_max), h_fact = -1.0;
+    int n_acc = 1;
+    bool fatal = false;
+    while (t < t_stop) {
+      if (t + h >= t_stop || t_stop - (t + h) < h_min) h = t_stop - t;
+      const double t_new = (t + h >= t_stop) ? t_stop : t + h;
+      for (int k = threadIdx.x; k < P.n; k += blockDim.x) guess[k] = xn[k];
+      __syncthreads();
+      PassCtx c{};
+      c.mode = 2;
+      c.method = method;
+      c.h = h;
+      c.prev = xn;
+      c.guess = guess;
+      c.guess_empty = false;
+      c.icap = icap;
+      c.t_src = t_new;
+      double guess_time = t;
+      bool newton_ok = false;
+      for (int it = 0; it < cfg.maxiter; ++it) {
+        coef_pass(P, vals, c, ca, nullptr, cb, status);
+        __syncthreads();
+        if (P.nonlinear || h != h_fact) {
+          stamp_lu<double>(P, lu, ca, nullptr);
+          __syncthreads();
+          factor<double>(P, lu, status);
+          h_fact = h;
+        }
+        if (*status & (KS_SINGULAR | KS_NONFINITE | KS_NOTIMPL)) {
+          fatal = true;
+          break;
+        }
+        for (int k = threadIdx.x; k < P.n; k += blockDim.x) x[k] = sum_rhs(P, k, cb);
+        __syncthreads();
+        lsolve<double, double>(P, lu, x);
+        usolve<double, double>(P, lu, x);
+        if (!P.nonlinear) {
+          newton_ok = true;
+          break;
+        }
+        if (converged(P, cfg, guess, x, true, guess_time, t_new)) {
+          newton_ok = true;
+          break;
+        }
+        for (int k = threadIdx.x; k < P.n; k += blockDim.x) guess[k] = x[k];
+        __syncthreads();
+        guess_time = t_new;
+      }
+      if (fatal) break;
+      int bad = 0;
+      for (int k = threadIdx.x; k < P.n; k += blockDim.x) bad |= !isfinite(x[k]);
+      if (__syncthreads_or(bad)) {
+        if (threadIdx.x == 0) atomicOr(status, KS_NONFINITE);
+        break;
+      }
+      // truncation error of the attempt over the accepted history (rows of x_out)
+      double r = 0.0;
+      const bool checked = newton_ok && n_acc >= order + 1;
+      if (checked) {
+        const double *x1 = xo + (size_t)(n_acc - 2) * P.n;
+        const double *x2 = trap ? xo + (size_t)(n_acc - 3) * P.n : x1;
+        const double t1 = to[n_acc - 2], t2 = trap ? to[n_acc - 3] : 0.0;
+        double rl = 0.0;
+        for (int k = threadIdx.x; k < P.n; k += blockDim.x) {
+          const int o = P.q[k];
+          double lte;
+          if (!trap) {
+            const double d1 = (x[k] - xn[k]) / h, d0 = (xn[k] - x1[o]) / (t - t1);
+            const double dd2 = (d1 - d0) / (t_new - t1);
+            lte = (h * h) * dd2;
+          } else {
+            const double d2 = (x[k] - xn[k]) / h, d1 = (xn[k] - x1[o]) / (t - t1), d0 = (x1[o] - x2[o]) / (t1 - t2);
+            const double e1 = (d2 - d1) / (t_new - t1), e0 = (d1 - d0) / (t - t2);
+            const double dd3 = (e1 - e0) / (t_new - t2);
+            lte = (0.5 * (h * h * h)) * dd3;
+          }
+          const double tol = __dadd_rn(__dmul_rn(lte_tol, fmax(fabs(x[k]), fabs(xn[k]))),
+                                       P.is_cur[k] ? cfg.iabstol : cfg.vabstol);
+          rl = fmax(rl, fabs(lte) / tol);
+        }
+        r = block_max(rl, red);
+      }
+      if (newton_ok && !(r > 1.0)) {
+        if (n_acc >= max_points) {
+          if (threadIdx.x == 0) atomicOr(status, KS_FULL);
+          break;
+        }
+        double *row = xo + (size_t)n_acc * P.n;
+        for (int k = threadIdx.x; k < P.n; k += blockDim.x) row[P.q[k]] = x[k];
+        if (threadIdx.x == 0) to[n_acc] = t_new;
+        if (trap) {
+          for (int e = threadIdx.x; e < P.ne; e += blockDim.x) {
+            if (P.el[e].kind != KRETS_ELEM_C) continue;
+            const int4 ps = P.el_pos[e];
+            const double vn = (ps.x >= 0 ? x[ps.x] : 0.0) - (ps.y >= 0 ? x[ps.y] : 0.0);
+            icap[e] = ca[e] * vn - cb[e];
+          }
+        }
+        __syncthreads();  // the row, the history reads and icap before xn moves on
+        for (int k = threadIdx.x; k < P.n; k += blockDim.x) xn[k] = x[k];
+        __syncthreads();
+        ++n_acc;
+        t = t_new;
+        const double f = checked ? adapt_factor(r, order, true) : 1.0;
+        h = fmin(h * f, h_max);
+        if (h < h_min) h = h_min;
+      } else {
+        h = h * (newton_ok ? adapt_factor(r, order, false) : 0.125);
+        if (h < h_min) {
+          if (threadIdx.x == 0) atomicOr(status, KS_TSTEP);
+          break;
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      n_points[inst] = n_acc;
+      if (inst_status) inst_status[inst] = *status;
+    }
     __syncthreads();
   }
 }

@@ -685,6 +685,164 @@ done:
   return st;
 }
 
+/* ------------------------------------------------ adaptive steps (extension)
+ * Transient with local-truncation-error step control; krets has fixed steps only, so
+ * this is an extension with its own oracle (this function), restating the standard
+ * divided-difference estimate (SPICE2 timestep control, Nagel 1975):
+ *   BE (order 1): LTE ~ h^2/2 x^(2) ~ h^2 DD2     (x^(2) ~ 2! DD2)
+ *   TR (order 2): LTE ~ h^3/12 x^(3) ~ h^3/2 DD3  (x^(3) ~ 3! DD3)
+ * with divided differences over the attempt and the last accepted points.  Error ratio
+ * r = max_k |LTE_k| / (lte_tol * max(|x_k|, |x_n,k|) + abstol_k) (abstol: current or voltage
+ * tolerance of the config).  r <= 1 accepts.  The step factor is the largest of a fixed
+ * set whose predicted ratio r * f^(p+1) stays <= 1/2 ({2, 1.5, 1, 0.75, 0.5} after an
+ * accept, {0.5, 0.25, 0.125} after a reject; 0.125 when Newton does not converge), so the
+ * time grid is exact binary arithmetic shared with the device.  The first p steps (not
+ * enough history) are accepted at h0.  Sources are evaluated at the new time (no lag).
+ * Returns the accepted points (t_out, x_out rows; row 0 = operating point at t = 0). */
+#define KO_TSTEP 8 /* step below h_min */
+#define KO_FULL 9  /* more accepted points than max_points */
+
+static double ko_step_factor(double r, int order, int accepted) {
+  static const double fa[5] = {2.0, 1.5, 1.0, 0.75, 0.5};
+  static const double fa2[5] = {4.0, 2.25, 1.0, 0.5625, 0.25}, fa3[5] = {8.0, 3.375, 1.0, 0.421875, 0.125};
+  static const double fr[3] = {0.5, 0.25, 0.125};
+  static const double fr2[3] = {0.25, 0.0625, 0.015625}, fr3[3] = {0.125, 0.015625, 0.001953125};
+  if (accepted) {
+    const double *pw = order == 1 ? fa2 : fa3;
+    for (int i = 0; i < 5; ++i)
+      if (r * pw[i] <= 0.5) return fa[i];
+    return 0.5;
+  }
+  const double *pw = order == 1 ? fr2 : fr3;
+  for (int i = 0; i < 3; ++i)
+    if (r * pw[i] <= 0.5) return fr[i];
+  return 0.125;
+}
+
+/* LTE ratio of the attempt x (time t_new = tn + h) given the accepted points xn (tn),
+ * x1 (t1), x2 (t2; TR only), in the device's expression order. */
+static double ko_lte_ratio(int n, int trap, const double *x, const double *xn, const double *x1, const double *x2,
+                           double t_new, double tn, double t1, double t2, double h, double lte_tol,
+                           const ko_cfg *cfg, const char *is_cur) {
+  double r = 0.0;
+  for (int k = 0; k < n; ++k) {
+    double lte;
+    if (!trap) {
+      double d1 = (x[k] - xn[k]) / h, d0 = (xn[k] - x1[k]) / (tn - t1);
+      double dd2 = (d1 - d0) / (t_new - t1);
+      lte = (h * h) * dd2;
+    } else {
+      double d2 = (x[k] - xn[k]) / h, d1 = (xn[k] - x1[k]) / (tn - t1), d0 = (x1[k] - x2[k]) / (t1 - t2);
+      double e1 = (d2 - d1) / (t_new - t1), e0 = (d1 - d0) / (tn - t2);
+      double dd3 = (e1 - e0) / (t_new - t2);
+      lte = (0.5 * (h * h * h)) * dd3;
+    }
+    double tol = lte_tol * fmax(fabs(x[k]), fabs(xn[k]));
+    tol = tol + (is_cur[k] ? cfg->iabstol : cfg->vabstol);
+    double q = fabs(lte) / tol;
+    if (!(q <= r)) r = q; /* NaN propagates */
+  }
+  return r;
+}
+
+int ko_tran_adaptive(const ko_elem *el, int ne, int n, const ko_cfg *cfg, double h0, double t_stop, int method,
+                     double lte_tol, double h_min, double h_max, int max_points, double *t_out, double *x_out,
+                     int *n_points) {
+  *n_points = 0;
+  if (max_points < 1) return KO_FULL;
+  int st = ko_op(el, ne, n, cfg, x_out, NULL);
+  if (st) return st;
+  t_out[0] = 0.0;
+  int n_acc = 1;
+  const int trap = method == 1, order = trap ? 2 : 1;
+  int nonlin = ko_nonlinear(el, ne, 0);
+  char *is_cur = ko_is_current(el, ne, n);
+  double *x = (double *)malloc(sizeof(double) * (n + 1));
+  double *guess = (double *)malloc(sizeof(double) * (n + 1));
+  double *icap = (double *)calloc(ne > 0 ? ne : 1, sizeof(double));
+  double complex *b = (double complex *)malloc(sizeof(double complex) * (n + 1));
+  ko_solver S = {0};
+  S.n = n;
+  ko_tlist G = {0}, E = {0};
+  double t = 0.0, h = fmin(h0, h_max), h_fact = -1.0;
+  while (t < t_stop) {
+    if (t + h >= t_stop || t_stop - (t + h) < h_min) h = t_stop - t;
+    const double t_new = (t + h >= t_stop) ? t_stop : t + h;
+    const double *xn = x_out + (size_t)(n_acc - 1) * n;
+    memcpy(guess, xn, sizeof(double) * n);
+    double guess_time = t;
+    int it, newton_ok = 0;
+    for (it = 0; it < cfg->maxiter; ++it) {
+      G.n = E.n = 0;
+      ko_ctx cx = {0};
+      cx.mode = MODE_TRAN;
+      cx.guess = guess;
+      cx.guess_time = guess_time;
+      cx.prev = xn;
+      cx.h = h;
+      cx.trap = trap;
+      cx.ic_prev = icap;
+      cx.lag = 0;
+      cx.t_now = t_new;
+      for (int k = 0; k < ne; ++k) {
+        st = ko_stamp(&el[k], k, &cx, &G, &E);
+        if (st) goto done;
+      }
+      if (nonlin || !S.have || h != h_fact) {
+        st = ko_factor(&S, &G);
+        if (st) goto done;
+        h_fact = h;
+      }
+      ko_rhs(&E, n, b);
+      ko_solve_real(&S, b, x);
+      if (!nonlin) { newton_ok = 1; break; }
+      if (ko_converged(cfg, el, ne, n, guess, 0, x, 1, guess_time, t_new, is_cur)) { newton_ok = 1; break; }
+      memcpy(guess, x, sizeof(double) * n);
+      guess_time = t_new;
+    }
+    for (int k = 0; k < n; ++k)
+      if (!isfinite(x[k])) { st = KO_NONFINITE; goto done; }
+    double r = 0.0;
+    int checked = 0;
+    if (newton_ok && n_acc >= order + 1) {
+      const double *x1 = x_out + (size_t)(n_acc - 2) * n;
+      const double *x2 = trap ? x_out + (size_t)(n_acc - 3) * n : x1;
+      r = ko_lte_ratio(n, trap, x, xn, x1, x2, t_new, t, t_out[n_acc - 2], trap ? t_out[n_acc - 3] : 0.0, h,
+                       lte_tol, cfg, is_cur);
+      checked = 1;
+    }
+    if (newton_ok && !(r > 1.0)) {
+      if (n_acc >= max_points) { st = KO_FULL; goto done; }
+      double *row = x_out + (size_t)n_acc * n;
+      memcpy(row, x, sizeof(double) * n);
+      t_out[n_acc] = t_new;
+      if (trap)
+        for (int k = 0; k < ne; ++k) {
+          if (el[k].kind != K_C) continue;
+          double g = 2.0 * el[k].value / h;
+          double vp = el[k].p >= 0 ? xn[el[k].p] : 0.0, vm = el[k].m >= 0 ? xn[el[k].m] : 0.0;
+          double ihist = g * (vp - vm) + icap[k];
+          double np_ = el[k].p >= 0 ? row[el[k].p] : 0.0, nm_ = el[k].m >= 0 ? row[el[k].m] : 0.0;
+          icap[k] = g * (np_ - nm_) - ihist;
+        }
+      n_acc++;
+      t = t_new;
+      double f = checked ? ko_step_factor(r, order, 1) : 1.0;
+      h = fmin(h * f, h_max);
+      if (h < h_min) h = h_min;
+    } else {
+      double f = newton_ok ? ko_step_factor(r, order, 0) : 0.125;
+      h = h * f;
+      if (h < h_min) { st = KO_TSTEP; goto done; }
+    }
+  }
+done:
+  *n_points = n_acc;
+  free(G.t); free(E.t); free(x); free(guess); free(icap); free(b); free(is_cur);
+  ko_solver_free(&S);
+  return st;
+}
+
 /* Assemble the summed MNA matrix of one mode as dense row-major (tests compare the
  * device's stamped values against this).  mode 0 = DC (caps filtered), 2 = TRAN with
  * prev = guess = x_prev (no lag), 1 = AC (complex interleaved). */

@@ -55,6 +55,7 @@ def lib():
         L.ko_assemble.argtypes = [P, I, I, I, D, I, D, P, P, P]
         L.ko_lu_solve_csc.argtypes = [I, P, P, P, P, P]
         L.ko_adjoint_tran.argtypes = [P, I, I, P, D, I, I, I, P, P]
+        L.ko_tran_adaptive.argtypes = [P, I, I, P, D, D, I, D, D, D, I, P, P, P]
         L.ko_pulse.argtypes = [P, D]
         L.ko_pulse.restype = D
         L.ko_sin.argtypes = [P, D]
@@ -123,6 +124,23 @@ def tran(table, n, h, n_steps, method="be", lag=None, config=None, faithful=Fals
     if st:
         raise OracleError(st, "tran")
     return (x, iters) if return_iters else x
+
+
+def tran_adaptive(table, n, h0, t_stop, method="tr", lte_tol=1e-3, h_min=None, h_max=None, max_points=100000,
+                  config=None):
+    """Adaptive-step transient (truncation-error control): (t[points], x[points][n])."""
+    m = 1 if method == "tr" else 0
+    h_min = h0 * 1e-6 if h_min is None else h_min
+    h_max = t_stop if h_max is None else h_max
+    t = np.zeros(max_points)
+    x = np.zeros((max_points, n))
+    got = ctypes.c_int(0)
+    c = _cfg(config)
+    st = lib().ko_tran_adaptive(_p(table), len(table), n, ctypes.byref(c), h0, t_stop, m, lte_tol, h_min, h_max,
+                                max_points, _p(t), _p(x), ctypes.byref(got))
+    if st:
+        raise OracleError(st, "tran_adaptive")
+    return t[:got.value], x[:got.value]
 
 
 def adjoint_tran(table, n, h, n_steps, out, method="tr", config=None):
