@@ -1,13 +1,16 @@
 """Small cases of the main kernels for profiler captures (one launch each, a few GB on
 the device at most), run as
 
-    python -m krets_gb300.profile_cases tran|multi|adjoint
+    python -m krets_gb300.profile_cases tran|multi|adjoint|kernels
 
   tran     k_tran_dfd: 304 instances of the 200-section RLC ladder, TR 1 ps, 1000 steps
   multi    k_multi_tran (global class): the 152 largest of the first 600 uneven
            netlists, operating point + 100 BE steps at 1 ns
   adjoint  k_adjoint_dfd: 152 instances of the 1000-section RC ladder, TR 1 ns,
            300 steps, checkpoint every 100
+  kernels  every other kernel once or a few times, at small sizes: plain OP / DC sweep /
+           transient (20 steps), batched OP, DC, AC (FP64 and mixed), transient (FP64,
+           mixed, double-float), adaptive transient, 64 small uneven netlists
 """
 from __future__ import annotations
 
@@ -53,7 +56,47 @@ def adjoint():
     return g.timing()
 
 
-CASES = {"tran": tran, "multi": multi, "adjoint": adjoint}
+def kernels():
+    from . import parse_circuit_description
+    from .analyses import AcAnalysis, Decade, generate_frequencies
+    from .generators import config1_circuit, monte_carlo_values, rc_ladder_ac, rlc_ladder, uneven_table
+    from .table import element_table
+    c = config1_circuit()
+    g = _lib.GpuCircuit(element_table(c), c.size)
+    g.op()
+    g.batch_op(monte_carlo_values(c, 64, seed=1))
+    d = parse_circuit_description("V1 in 0 1\nR1 in a 1000\nD1 a 0 DMOD\nR2 a b 2200\nD2 b 0 DMOD\n"
+                                  "R3 b 0 10000\n.model DMOD D (is=1e-12)\n")
+    td = element_table(d)
+    gd = _lib.GpuCircuit(td, d.size)
+    gd.dc(0, -0.5, 3.0, 0.05)
+    gd.batch_dc(monte_carlo_values(d, 16, seed=2), 0, -0.5, 3.0, 0.05)
+    a = rc_ladder_ac(500)
+    ga = _lib.GpuCircuit(element_table(a), a.size)
+    f = np.array(generate_frequencies(AcAnalysis(Decade(455), 1.0, 1e9)))[::16]
+    for prec in (_lib.PREC_FP64, _lib.PREC_MIXED):
+        ga.batch_ac(None, f, precision=prec)
+    r = rlc_ladder(200)
+    tr = element_table(r)
+    gr = _lib.GpuCircuit(tr, r.size)
+    gr.tran(1e-12, 20, "tr")
+    vals = monte_carlo_values(r, 152, seed=3)
+    for prec in (_lib.PREC_FP64, _lib.PREC_MIXED, _lib.PREC_DF):
+        out = _lib.DeviceArray((152, 201, r.size))
+        gr.batch_tran(vals, 1e-12, 200, "tr", lag=False, precision=prec, out=out)
+        del out
+    s = rlc_ladder(20)
+    gs = _lib.GpuCircuit(element_table(s), s.size)
+    gs.batch_tran_adaptive(monte_carlo_values(s, 8, seed=4), 1e-12, 2e-9, "tr", lte_tol=1e-4, h_min=1e-18)
+    tabs = [uneven_table(i) for i in range(64)]
+    m = _lib.MultiCircuit([t for t, _ in tabs], [n for _, n in tabs], method="be", h=1e-9)
+    out = _lib.DeviceArray(m.total(200))
+    m.tran(200, out=out)
+    gr.flush_l2()
+    return m.timing()
+
+
+CASES = {"tran": tran, "multi": multi, "adjoint": adjoint, "kernels": kernels}
 
 if __name__ == "__main__":
     k, c = CASES[sys.argv[1]]()
