@@ -258,6 +258,7 @@ def run_ours(args, rank, world):
     if world > 1:
         dist.barrier()
     launches = _lib.launch_count() - l0
+    engine = g.last_launch()
     total_s = max_over_ranks(sum(call_ms) / 1e3, world)
     ctsteps = N_INST * N_STEPS
     value = job_rate(ctsteps, args.steps, world, total_s)
@@ -355,6 +356,7 @@ def run_ours(args, rank, world):
                    "l2": "flushed between timed steps (512 MB write); outputs 98.6 GB >> L2",
                    "parallelism": "replicas only (instances sharded per GPU)"},
         "max_rel_err_vs_fp64": max(errs),
+        "engine": engine,
         "precision_variants": variants,
         "plain_form": {"value": plain_rate, "unit": UNIT, "what": "1 instance, FP64, per-step kernels (CUDA graph)"},
         "batched_over_plain": value / plain_rate,

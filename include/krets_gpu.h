@@ -244,6 +244,11 @@ const char *krets_last_error_message(void);
 /* Device time (CUDA events on the handle's stream) of the last call's main kernel and of
  * the whole last call (copies included), in milliseconds. */
 krets_status krets_last_timing(const krets_circuit *c, float *kernel_ms, float *call_ms);
+/* The last double-float batched transient launch: info[0] = threads per instance,
+ * info[1] = instances per CTA, info[2] = grid, info[3] = how the group size was chosen
+ * (1 = timed now by the autotuner, 2 = the autotuner's cached choice for this sparsity
+ * signature, 0 = default, too few steps to time; KRETS_GROUP=32|64|128 overrides). */
+krets_status krets_last_launch(const krets_circuit *c, int32_t *info, int32_t cap);
 /* Kernel launches issued by this library since load. */
 int64_t krets_launch_count(void);
 /* Refinement statistics of the last mixed-precision batched call: histogram[k] = number

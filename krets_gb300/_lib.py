@@ -80,6 +80,7 @@ def lib():
             "krets_batch_dc": [_P, _I, _P, _I, _D, _D, _D, _P, _I, _P, _P],
             "krets_batch_tran_adaptive": [_P, _I, _P, _D, _D, _I, _D, _D, _D, _I, _P, _P, _P, _P],
             "krets_last_timing": [_P, _P, _P],
+            "krets_last_launch": [_P, _P, _I],
             "krets_last_refine_stats": [_P, _P, _P],
             "krets_device_alloc": [ctypes.c_size_t, _P],
             "krets_device_free": [_P],
@@ -399,6 +400,15 @@ class GpuCircuit:
         vals = [ctypes.c_int32() for _ in range(5)]
         check(lib().krets_circuit_info(self.h, mode, *[ctypes.byref(v) for v in vals]))
         return dict(zip(["n", "nnz_a", "nnz_lu", "n_levels", "n_ulevels"], [v.value for v in vals]))
+
+    def last_launch(self):
+        """Last double-float batched launch: threads per instance, instances per CTA, grid,
+        and how the group size was chosen ("default" / "autotuner" / "autotuner cache")."""
+        info = np.zeros(4, dtype=np.int32)
+        check(lib().krets_last_launch(self.h, ptr(info), 4), "last_launch")
+        how = {0: "default", 1: "autotuner", 2: "autotuner cache"}.get(int(info[3]), "?")
+        return {"threads_per_instance": int(info[0]), "instances_per_cta": int(info[1]), "grid": int(info[2]),
+                "group_size_from": how}
 
     def flush_l2(self):
         check(lib().krets_flush_l2(self.h))

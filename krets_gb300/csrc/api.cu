@@ -10,6 +10,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -144,6 +145,7 @@ struct krets_circuit {
   long long hist[8] = {};
   int fallbacks = 0;
   int warps_per_cta = 0, grid = 0;
+  int launch_info[4] = {0, 0, 0, 0};  // last batched launch: threads per instance, per CTA, grid, tuned
   void *l2buf = nullptr;
 
   ~krets_circuit() {
@@ -981,6 +983,98 @@ krets_status krets_tran(krets_circuit *c, double h, int32_t n_steps, int32_t met
   return map_status(h2[0], 1);
 }
 
+namespace {
+
+// Double-float direct engine launch for a group size G: instances per CTA (W) from the
+// shared-memory footprint, the kernel instance and its residency.
+using DfdKernel = void (*)(DevProg, KCfg, DfdLay, const double *, int, double, int, int, int, double *, int *, int *,
+                           int, WaveTab);
+struct DfdLaunch {
+  int W = 1, per_sm = 0;
+  size_t smem = 0;
+  DfdKernel kd = nullptr;
+};
+
+krets_status dfd_config(int G, const DfdLay &DL, DfdLaunch &Lc) {
+  Lc.W = (int)std::max<size_t>(1, std::min<size_t>(640 / G, (max_smem_optin() - DL.sprog_bytes) / DL.bytes));
+  Lc.smem = DL.sprog_bytes + (size_t)Lc.W * DL.bytes;
+  Lc.kd = G == 32 ? k_tran_dfd<32> : (G == 64 ? k_tran_dfd<64> : k_tran_dfd<128>);
+  CU(cudaFuncSetAttribute(Lc.kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Lc.smem));
+  CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&Lc.per_sm, Lc.kd, G * Lc.W, Lc.smem));
+  if (Lc.per_sm < 1) return fail(KRETS_ERR_CUDA, "double-float engine does not fit on an SM");
+  return KRETS_OK;
+}
+
+// Autotuner of the double-float engine: the threads per instance (G = 128, 64, 32) are
+// chosen by timing one full wave of instances for up to 128 steps with each, once per
+// sparsity signature (pattern hash, size, LU entries, method); the choice is cached for
+// the process.  how = 1 measured now, 2 from the cache, 0 default (too few steps to time).
+std::mutex g_tune_mu;
+std::map<std::string, int> g_tune;
+
+krets_status dfd_pick_group(krets_circuit *c, const DevProgram *D, const DfdLay &DL, const double *dv,
+                            const double *dx, size_t stride, int n_inst, double h, int n_steps, int method, int lag,
+                            int *queue, int opts, const WaveTab &wt, int &G_out, int &how) {
+  char key[96];
+  snprintf(key, sizeof key, "%016llx/%d/%zu/%d", (unsigned long long)D->host.signature, D->host.n,
+           D->host.lu_col.size(), method);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      G_out = it->second;
+      how = 2;
+      return KRETS_OK;
+    }
+  }
+  G_out = 128;
+  how = 0;
+  const int steps = std::min(n_steps, 128);
+  if (steps < 16) return KRETS_OK;
+  DfdLaunch L0;
+  krets_status s = dfd_config(128, DL, L0);
+  if (s != KRETS_OK) return s;
+  const int n = D->host.n;
+  const int trial = std::max(1, std::min(n_inst, L0.W * L0.per_sm * device_sm_count()));
+  DevBuf tout, tst;
+  const size_t row = sizeof(double) * n * ((size_t)steps + 1);
+  CU(cudaMalloc(&tout.p, row * trial));
+  CU(cudaMalloc(&tst.p, sizeof(int) * trial));
+  // the trial instances start from their operating points (row 0 of each waveform)
+  CU(cudaMemcpy2DAsync(tout.p, row, dx, sizeof(double) * stride, sizeof(double) * n, trial, cudaMemcpyDeviceToDevice,
+                       c->stream));
+  double best = 0.0;
+  for (int G : {128, 64, 32}) {
+    DfdLaunch Lc;
+    if (dfd_config(G, DL, Lc) != KRETS_OK) {
+      cudaGetLastError();
+      continue;
+    }
+    const int grid = std::max(1, std::min((trial + Lc.W - 1) / Lc.W, Lc.per_sm * device_sm_count()));
+    CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
+    CU(cudaEventRecord(c->ev[2], c->stream));
+    Lc.kd<<<grid, G * Lc.W, Lc.smem, c->stream>>>(D->view, c->cfg, DL, dv, trial, h, steps, method, lag,
+                                                  (double *)tout.p, (int *)tst.p, queue, opts, wt);
+    g_launches++;
+    CU(cudaGetLastError());
+    CU(cudaEventRecord(c->ev[3], c->stream));
+    CU(cudaEventSynchronize(c->ev[3]));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+    const double rate = ms > 0.f ? (double)trial * steps / ms : 0.0;
+    if (rate > best) {
+      best = rate;
+      G_out = G;
+    }
+  }
+  how = 1;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = G_out;
+  return KRETS_OK;
+}
+
+}  // namespace
+
 krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *values, double h, int32_t n_steps,
                               int32_t method, int32_t source_lag, int32_t precision, double *x_out,
                               int32_t *inst_status) {
@@ -1054,23 +1148,6 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
     if ((size_t)DL.bytes + DL.sprog_bytes > max_smem_optin()) use_dfd = false;
   }
   if (use_dfd) {
-    const char *genv = getenv("KRETS_GROUP");
-    int G = genv ? atoi(genv) : 128;
-    if (G != 32 && G != 64 && G != 128) G = 128;
-    int W = (int)std::max<size_t>(1, std::min<size_t>(640 / G, (max_smem_optin() - DL.sprog_bytes) / DL.bytes));
-    const size_t smem = DL.sprog_bytes + (size_t)W * DL.bytes;
-    const char *oenv = getenv("KRETS_DFD_OPTS");
-    const int opts = oenv ? atoi(oenv) : 0;
-    void (*kd)(DevProg, KCfg, DfdLay, const double *, int, double, int, int, int, double *, int *, int *, int,
-               WaveTab) =
-        G == 32 ? k_tran_dfd<32> : (G == 64 ? k_tran_dfd<64> : k_tran_dfd<128>);
-    CU(cudaFuncSetAttribute(kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kd, G * W, smem));
-    if (per_sm < 1) return fail(KRETS_ERR_CUDA, "double-float engine does not fit on an SM");
-    int grid = std::max(1, std::min((n_inst + W - 1) / W, per_sm * device_sm_count()));
-    c->warps_per_cta = W * G / 32;
-    c->grid = grid;
     // PULSE / SIN sources tabulated per step (their parameters are not per-instance values)
     const Program &H = Dtr->host;
     std::vector<int> wrow(P.ndyn, -1), wsrc;
@@ -1095,9 +1172,33 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
       wt.tab = (const double *)twave.p;
       wt.row = d_wrow;
     }
+    const char *oenv = getenv("KRETS_DFD_OPTS");
+    const int opts = oenv ? atoi(oenv) : 0;
+    const char *genv = getenv("KRETS_GROUP");
+    int G = 128, how = 0;
+    if (genv) {
+      G = atoi(genv);
+      if (G != 32 && G != 64 && G != 128) G = 128;
+    } else {
+      s = dfd_pick_group(c, Dtr, DL, (const double *)dv, (const double *)dx, stride, n_inst, h, n_steps, method,
+                         source_lag, queue, opts, wt, G, how);
+      if (s != KRETS_OK) return s;
+    }
+    DfdLaunch Lc;
+    s = dfd_config(G, DL, Lc);
+    if (s != KRETS_OK) return s;
+    const int W = Lc.W;
+    int grid = std::max(1, std::min((n_inst + W - 1) / W, Lc.per_sm * device_sm_count()));
+    c->warps_per_cta = W * G / 32;
+    c->grid = grid;
+    c->launch_info[0] = G;
+    c->launch_info[1] = W;
+    c->launch_info[2] = grid;
+    c->launch_info[3] = how;
+    CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
     CU(cudaEventRecord(c->ev[2], c->stream));
-    kd<<<grid, G * W, smem, c->stream>>>(P, c->cfg, DL, (const double *)dv, n_inst, h, n_steps, method, source_lag,
-                                        (double *)dx, d_st, queue, opts, wt);
+    Lc.kd<<<grid, G * W, Lc.smem, c->stream>>>(P, c->cfg, DL, (const double *)dv, n_inst, h, n_steps, method,
+                                               source_lag, (double *)dx, d_st, queue, opts, wt);
   } else if (warp_engine) {
     const char *bud = getenv("KRETS_SMEM_BUDGET");
     size_t budget = bud ? (size_t)atol(bud) : max_smem_optin();
@@ -1363,6 +1464,12 @@ const char *krets_status_string(krets_status s) {
 }
 
 const char *krets_last_error_message(void) { return g_last_error.c_str(); }
+
+krets_status krets_last_launch(const krets_circuit *c, int32_t *info, int32_t cap) {
+  if (!c || !info) return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments to krets_last_launch");
+  for (int i = 0; i < cap && i < 4; ++i) info[i] = c->launch_info[i];
+  return KRETS_OK;
+}
 
 krets_status krets_last_timing(const krets_circuit *c, float *kernel_ms, float *call_ms) {
   if (!c) return fail(KRETS_ERR_INVALID_ARGUMENT, "null circuit");

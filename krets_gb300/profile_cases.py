@@ -10,7 +10,8 @@ the device at most), run as
            300 steps, checkpoint every 100
   kernels  every other kernel once or a few times, at small sizes: plain OP / DC sweep /
            transient (20 steps), batched OP, DC, AC (FP64 and mixed), transient (FP64,
-           mixed, double-float), adaptive transient, 64 small uneven netlists
+           mixed, double-float; nonlinear FP64 and mixed), adaptive transient, 64 small
+           uneven netlists
 """
 from __future__ import annotations
 
@@ -71,6 +72,8 @@ def kernels():
     gd = _lib.GpuCircuit(td, d.size)
     gd.dc(0, -0.5, 3.0, 0.05)
     gd.batch_dc(monte_carlo_values(d, 16, seed=2), 0, -0.5, 3.0, 0.05)
+    for prec in (_lib.PREC_FP64, _lib.PREC_MIXED):   # nonlinear: Newton per step
+        gd.batch_tran(monte_carlo_values(d, 16, seed=5), 1e-9, 50, "be", precision=prec)
     a = rc_ladder_ac(500)
     ga = _lib.GpuCircuit(element_table(a), a.size)
     f = np.array(generate_frequencies(AcAnalysis(Decade(455), 1.0, 1e9)))[::16]

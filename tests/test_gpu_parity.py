@@ -272,6 +272,31 @@ def test_batched_failure_stays_with_its_instance(oracle_lib, precision):
         assert rel_err(out[i], ref, mask) < TOL, i
 
 
+def test_double_float_group_size_autotuner(oracle_lib, monkeypatch):
+    """The first double-float run of a sparsity signature times the group sizes and caches
+    the fastest; later runs reuse it; KRETS_GROUP overrides.  Every choice meets 1e-9."""
+    c = rlc_ladder(37)          # a signature no other test uses
+    t = element_table(c)
+    vals = monte_carlo_values(c, 40, seed=13)
+    g = _lib.GpuCircuit(t, c.size)
+    mask = is_current_mask(c)
+    x = g.batch_tran(vals, 1e-12, 150, "tr", lag=False, precision=_lib.PREC_DF)
+    first = g.last_launch()
+    assert first["group_size_from"] == "autotuner" and first["threads_per_instance"] in (32, 64, 128)
+    g.batch_tran(vals, 1e-12, 150, "tr", lag=False, precision=_lib.PREC_DF)
+    again = g.last_launch()
+    assert again["group_size_from"] == "autotuner cache"
+    assert again["threads_per_instance"] == first["threads_per_instance"]
+    monkeypatch.setenv("KRETS_GROUP", "64")
+    y = g.batch_tran(vals, 1e-12, 150, "tr", lag=False, precision=_lib.PREC_DF)
+    assert g.last_launch()["threads_per_instance"] == 64 and g.last_launch()["group_size_from"] == "default"
+    for i in (0, 39):
+        ti = t.copy()
+        ti["value"] = vals[i]
+        ref = oracle_lib.tran(ti, c.size, 1e-12, 150, method="tr", lag=False)
+        assert rel_err(x[i], ref, mask) < TOL and rel_err(y[i], ref, mask) < TOL
+
+
 def test_zero_step_transient_is_the_operating_point(oracle_lib):
     """stop_time < time_step / 2 gives num_steps = 0: the result is the t = 0 operating
     point alone (transient.rs:14-114)."""
