@@ -188,10 +188,12 @@ krets_status krets_batch_ac(krets_circuit *c, int32_t n_inst, const double *valu
 /* Adjoint sensitivities of a batched linear transient (no counterpart in the reference).
  * Loss per instance: sum over steps n = 1..n_steps of x_out(t_n)^2, out_unknown being the
  * MNA index of the output (e.g. V(out)).  grad_out[n_inst][n_elem] receives dLoss/dvalue for
- * every R, C and L element (0 for the others).  The forward pass keeps a checkpoint every
- * checkpoint_every steps and the backward sweep recomputes each segment from it; transposed
- * solves reuse the forward LU factors.  gradient = 0 runs the forward pass only (loss).
- * The operating point at t = 0 must be zero (KRETS_ERR_NOT_IMPLEMENTED otherwise). */
+ * every R, C and L element; for every V and I source it receives dLoss/dalpha, alpha scaling
+ * the source's transient value (its waveform, or its DC value) at alpha = 1; 0 for the
+ * others.  The forward pass keeps a checkpoint every checkpoint_every steps and the
+ * backward sweep recomputes each segment from it; transposed solves reuse the forward LU
+ * factors.  gradient = 0 runs the forward pass only (loss).  The operating point at t = 0
+ * must be zero (KRETS_ERR_NOT_IMPLEMENTED otherwise). */
 krets_status krets_adjoint_tran(krets_circuit *c, int32_t n_inst, const double *values, double h, int32_t n_steps,
                                 int32_t method, int32_t out_unknown, int32_t checkpoint_every, int32_t gradient,
                                 double *loss_out, double *grad_out);

@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
   int crow[RD];              // backward half: dynamic element's row positions (C: p | m << 16, L: branch)
   int cc0[RK], cc1[RK];      // backward half: up to two C^T terms per row, -1 none, cc1 = -2: use the list
   int erow[RE], ecol[RE];    // recompute half: element's row / column positions (p | m << 16, L: branch)
-  int ekind = 0;             // recompute half: 2 bits per element: 0 none, 1 R, 2 C, 3 L
+  int ekind = 0;             // recompute half: 3 bits per element: 0 none, 1 R, 2 C, 3 L, 4 source
   const int J = (n_steps + K - 1) / K;          // segments
   const size_t ck_words = (size_t)n + P.ncap;  // per checkpoint, in df
   const size_t seg_words = (size_t)(K + 1) * n, hist_words = (size_t)K * n;
@@ -287,12 +287,20 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
         const df *xn = sg + (size_t)(nn - s0) * n, *xp = xn - n;
 #pragma unroll
         for (int i = 0; i < RE; ++i) {
-          const int kind = (ekind >> (2 * i)) & 3;
+          const int kind = (ekind >> (3 * i)) & 7;
           if (!kind) continue;
           const int rp = erow[i] & 0xffff, rm = (int)((unsigned)erow[i] >> 16);
           const int cp = ecol[i] & 0xffff, cm = (int)((unsigned)ecol[i] >> 16);
           df term;
-          if (kind == 3) {
+          if (kind == 4) {
+            // source: rhs of step nn at its row is w_nn (BE) or w_nn + w_{nn-1} (TR form)
+            const int d = ecol[i], e = hl + i * GH;
+            const int wr = wt.tab ? wt.row[d] : -1;
+            const double dc = vals ? vals[e] : P.el[e].value;
+            const double w1 = wr >= 0 ? wt.tab[(size_t)wr * wt.stride + nn] : dc;
+            const double w0 = wr >= 0 ? wt.tab[(size_t)wr * wt.stride + nn - 1] : dc;
+            term = df_mul(ln[rp], df_from_double(tr ? w1 + w0 : w1));
+          } else if (kind == 3) {
             term = df_mul(ln[rp], df_sub(xn[cp], xp[cp]));
           } else {
             const df dl = df_sub(df_pick(ln, rp), df_pick(ln, rm));
@@ -348,8 +356,12 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
               code = 3;
               erow[i] = pack2(a.w, -1);
               ecol[i] = pack2(pos.z, -1);
+            } else if ((kind == KRETS_ELEM_V || kind == KRETS_ELEM_I) && a.w >= 0 && (a.x >> 8) > 0) {
+              code = 4;
+              erow[i] = pack2(a.w, -1);
+              ecol[i] = (a.x >> 8) - 1;  // rhs-element index
             }
-            ekind |= code << (2 * i);
+            ekind |= code << (3 * i);
           }
         }
       }
@@ -435,12 +447,13 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
         for (int i = 0; i < RE; ++i) {
           const int e = hl + i * GH;
           if (e >= P.ne) continue;
-          const int kind = (ekind >> (2 * i)) & 3;
+          const int kind = (ekind >> (3 * i)) & 7;
           const double val = vals ? vals[e] : P.el[e].value;
           const double gsum = df_to_double(gr[i]);
           double r = 0.0;
           if (kind == 1) r = gsum / (val * val);
-          else if (kind >= 2) r = gsum * (tr ? 2.0 / h : 1.0 / h);
+          else if (kind == 2 || kind == 3) r = gsum * (tr ? 2.0 / h : 1.0 / h);
+          else if (kind == 4) r = gsum;
           grad_out[(size_t)inst * P.ne + e] = r;
         }
       }

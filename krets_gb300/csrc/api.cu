@@ -1312,13 +1312,16 @@ krets_status krets_adjoint_tran(krets_circuit *c, int32_t n_inst, const double *
       return fail(KRETS_ERR_NOT_IMPLEMENTED, "adjoint sensitivities need a zero operating point at t = 0 "
                                              "(sources at 0 when the transient starts)");
   // per-element adjoint descriptors and the column map of C^T lambda
-  std::vector<int> adj(4 * (size_t)P.ne, -1), ccp(P.n + 1, 0), cco;
+  std::vector<int> adj(4 * (size_t)P.ne, -1), ccp(P.n + 1, 0), cco, dyn_of(P.ne, -1);
   std::vector<std::vector<int>> cols(P.n);
+  for (size_t d = 0; d < H.dyn_e.size(); ++d) dyn_of[H.dyn_e[d]] = (int)d;
   for (int e = 0; e < P.ne; ++e) {
     const krets_element &E = c->el[e];
     if ((E.kind == KRETS_ELEM_R || E.kind == KRETS_ELEM_C) && (E.flags & KRETS_FLAG_G2))
       return fail(KRETS_ERR_NOT_IMPLEMENTED, "adjoint sensitivities of group-2 resistor/capacitor stamps");
-    adj[4 * e] = E.kind;
+    // kind, and for sources the rhs-element index (their per-step values come from it)
+    const bool src = (E.kind == KRETS_ELEM_V || E.kind == KRETS_ELEM_I) && dyn_of[e] >= 0;
+    adj[4 * e] = E.kind | (src ? (dyn_of[e] + 1) << 8 : 0);
     adj[4 * e + 1] = E.p >= 0 ? H.pinv[E.p] : -1;
     adj[4 * e + 2] = E.m >= 0 ? H.pinv[E.m] : -1;
     adj[4 * e + 3] = E.b >= 0 ? H.pinv[E.b] : -1;

@@ -970,6 +970,13 @@ int ko_adjoint_tran(const ko_elem *el, int ne, int n, const ko_cfg *cfg, double 
         if (e->kind == K_R) grad[k] += dl * (method == 1 ? vp + vn : vn) / (e->value * e->value);
         else if (e->kind == K_C) grad[k] += a * dl * (vp - vn);
         else if (e->kind == K_L && e->b >= 0) grad[k] += a * lam[e->b] * (xs[e->b] - xp[e->b]);
+        else if ((e->kind == K_V || e->kind == K_I) && e->b >= 0) {
+          /* d loss / d alpha for the source's transient value scaled by alpha: the rhs of
+           * step s holds w_s (BE) or w_s + w_{s-1} (TR form of the recurrence) at row b */
+          double ws = e->kind == K_V ? ko_source_at(e, (double)s * h) : e->value;
+          double w0 = e->kind == K_V ? ko_source_at(e, (double)(s - 1) * h) : e->value;
+          grad[k] += lam[e->b] * (method == 1 ? ws + w0 : ws);
+        }
       }
       double *tmp = nxt;
       nxt = lam;

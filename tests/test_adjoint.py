@@ -40,6 +40,29 @@ def _fd_grad(oracle_lib, table, n, vals, h, steps, method, out, rel=1e-5):
     return g
 
 
+def _scaled_source(table, e, alpha):
+    """The table with source e's transient value scaled by alpha (PULSE V1/V2, SIN VO/VA,
+    and the DC value)."""
+    t = table.copy()
+    t["value"][e] *= alpha
+    if t["wave"][e] in (1, 2):
+        t["wp"][e][0] *= alpha
+        t["wp"][e][1] *= alpha
+    return t
+
+
+def _fd_source(oracle_lib, table, n, vals, h, steps, method, out, e, rel=1e-5):
+    t = table.copy()
+    t["value"] = vals
+    lp = _oracle_loss(oracle_lib, _scaled_source(t, e, 1 + rel), n, vals * np.where(np.arange(len(vals)) == e,
+                                                                                      1 + rel, 1), h, steps, method,
+                      out)
+    lm = _oracle_loss(oracle_lib, _scaled_source(t, e, 1 - rel), n, vals * np.where(np.arange(len(vals)) == e,
+                                                                                      1 - rel, 1), h, steps, method,
+                      out)
+    return (lp - lm) / (2 * rel)
+
+
 def _check(oracle_lib, c, vals, h, steps, method, out_name, K):
     t = element_table(c)
     out = c.index_map[out_name]
@@ -51,10 +74,16 @@ def _check(oracle_lib, c, vals, h, steps, method, out_name, K):
         ref = _oracle_loss(oracle_lib, t, c.size, vals[i], h, steps, method, out)
         assert abs(loss[i] - ref) <= LOSS_TOL * abs(ref), (i, loss[i], ref)
         fd = _fd_grad(oracle_lib, t, c.size, vals[i], h, steps, method, out)
+        for e in np.nonzero(np.isin(t["kind"], (4, 5)))[0]:    # sources: waveform scale
+            fd[e] = _fd_source(oracle_lib, t, c.size, vals[i], h, steps, method, out, e)
         err = np.max(np.abs(grad[i] - fd)) / np.max(np.abs(fd))
         assert err < GRAD_TOL, (i, err)
-        # elements that carry no gradient (sources) read exactly zero
-        assert np.all(grad[i][~np.isin(t["kind"], (1, 2, 3))] == 0.0)
+        src = np.isin(t["kind"], (4, 5))
+        if src.any() and np.max(np.abs(fd[src])) > 0:
+            serr = np.max(np.abs(grad[i][src] - fd[src])) / np.max(np.abs(fd[src]))
+            assert serr < GRAD_TOL, (i, serr)
+        # elements that carry no gradient read exactly zero
+        assert np.all(grad[i][~np.isin(t["kind"], (1, 2, 3, 4, 5))] == 0.0)
     return loss, grad
 
 
