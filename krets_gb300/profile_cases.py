@@ -1,7 +1,7 @@
 """Small cases of the main kernels for profiler captures (one launch each, a few GB on
 the device at most), run as
 
-    python -m krets_gb300.profile_cases tran|multi|adjoint|kernels
+    python -m krets_gb300.profile_cases tran|multi|adjoint|kernels|op
 
   tran     k_tran_dfd: 304 instances of the 200-section RLC ladder, TR 1 ps, 1000 steps
   multi    k_multi_tran (global class): the 152 largest of the first 600 uneven
@@ -12,6 +12,7 @@ the device at most), run as
            transient (20 steps), batched OP, DC, AC (FP64 and mixed), transient (FP64,
            mixed, double-float; nonlinear FP64 and mixed), adaptive transient, 64 small
            uneven netlists
+  op       k_op: the plain operating point of the 1001-unknown ladder, three times
 """
 from __future__ import annotations
 
@@ -99,7 +100,17 @@ def kernels():
     return m.timing()
 
 
-CASES = {"tran": tran, "multi": multi, "adjoint": adjoint, "kernels": kernels}
+def op():
+    from .generators import config1_circuit
+    from .table import element_table
+    c = config1_circuit()
+    g = _lib.GpuCircuit(element_table(c), c.size)
+    for _ in range(3):
+        g.op()
+    return g.timing()
+
+
+CASES = {"tran": tran, "multi": multi, "adjoint": adjoint, "kernels": kernels, "op": op}
 
 if __name__ == "__main__":
     k, c = CASES[sys.argv[1]]()
