@@ -127,3 +127,20 @@ def test_adjoint_rejects_nonzero_operating_point_and_nonlinear():
     g = _lib.GpuCircuit(element_table(c), c.size)
     with pytest.raises(KretsError):
         g.adjoint_tran(None, 1e-9, 10, c.index_map["V(a)"], n_inst=1)
+
+
+def test_adjoint_full_size_config5(oracle_lib):
+    """Config 5 at its full size: 1024 instances of the 1000-section RC ladder, 2000 TR
+    steps, checkpoints every 100.  Instances with identical values give bit-identical
+    losses and gradients whatever CTA ran them; instance 0 matches the FP64 oracle adjoint
+    (loss 1e-12, gradient 1e-9 norm-wise)."""
+    c = rc_ladder_step(1000)
+    t = element_table(c)
+    out = c.index_map["V(n20)"]
+    vals = np.tile(t["value"], (1024, 1))
+    g = _lib.GpuCircuit(t, c.size)
+    loss, grad = g.adjoint_tran(vals, 1e-9, 2000, out, method="tr", checkpoint_every=100)
+    assert np.all(loss == loss[0]) and np.all(grad == grad[0])
+    L, gref = oracle_lib.adjoint_tran(t, c.size, 1e-9, 2000, out)
+    assert abs(loss[0] - L) <= 1e-12 * abs(L)
+    assert np.max(np.abs(grad[0] - gref)) <= 1e-9 * np.max(np.abs(gref))
