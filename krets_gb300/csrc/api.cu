@@ -433,6 +433,28 @@ krets_status dev_view(const void *user, size_t bytes, bool in, cudaStream_t s, D
   return KRETS_OK;
 }
 
+// Program arrays a launch of at most one CTA per SM warms into L1 (see warm_l1):
+// factorisation, solves, then stamps.  Empty when CTAs share SMs.
+OpWarm plan_warm(const DevProgram *D, int n_inst) {
+  OpWarm w{};
+  if (n_inst > device_sm_count()) return w;
+  const DevProg &V = D->view;
+  const Program &H = D->host;
+  const struct { const void *p; size_t words; } fs[] = {
+      {V.piv_ptr, H.piv_ptr.size()}, {V.piv, H.piv.size()},         {V.upd, H.upd.size()},
+      {V.lu_diag, H.lu_diag.size()}, {V.lev_rows, H.lev_rows.size()}, {V.lu_rowptr, H.lu_rowptr.size()},
+      {V.lu_col, H.lu_col.size()},   {V.ulev_rows, H.ulev_rows.size()}, {V.lu_src, H.lu_col.size()},
+      {V.a_cptr, H.a_cptr.size()},   {V.a_contrib, H.a_contrib.size()}, {V.b_cptr, H.b_cptr.size()},
+      {V.b_contrib, H.b_contrib.size()}};
+  for (const auto &f : fs) {
+    if (f.words == 0 || w.count == 16) continue;
+    w.ptr[w.count] = static_cast<const char *>(f.p);
+    w.bytes[w.count] = (int)(4 * f.words);
+    ++w.count;
+  }
+  return w;
+}
+
 krets_status run_op(krets_circuit *c, DevProgram *D, int n_inst, const double *d_values, double *d_x,
                     size_t out_stride, int *d_status, int *d_iters, int threads) {
   Lay L = layout_op(D->view);
@@ -442,7 +464,7 @@ krets_status run_op(krets_circuit *c, DevProgram *D, int n_inst, const double *d
   krets_status s = plan_launch(c, k_op, L, threads, n_inst, grid, smem, gws);
   if (s != KRETS_OK) return s;
   k_op<<<grid, threads, smem, c->stream>>>(D->view, c->cfg, L, gws, d_values, d_x, out_stride, d_status, d_iters,
-                                          n_inst);
+                                          n_inst, plan_warm(D, n_inst));
   g_launches++;
   CU(cudaGetLastError());
   return KRETS_OK;
@@ -710,7 +732,7 @@ krets_status run_dc(krets_circuit *c, int32_t sweep_elem, double start, double s
   CU(cudaEventRecord(c->ev[2], c->stream));
   k_dc_sweep<<<grid, threads, smem, c->stream>>>(D->view, c->cfg, L, gws, sweep_elem, start, step, np,
                                                  (const double *)dv, n_inst, (size_t)c->n * np, (double *)dx,
-                                                 d_status);
+                                                 d_status, plan_warm(D, n_inst));
   g_launches++;
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[3], c->stream));
@@ -1615,7 +1637,7 @@ krets_status krets_batch_tran_noalloc(krets_circuit *c, int32_t n_inst, const do
   s = plan_launch(c, k_op, Lop, 128, n_inst, op_grid, op_smem, op_gws);
   if (s) return s;
   k_op<<<op_grid, 128, op_smem, c->stream>>>(Ddc->view, c->cfg, Lop, nullptr, d_values, d_x_out, stride, op_status,
-                                             nullptr, n_inst);
+                                             nullptr, n_inst, OpWarm{});
   g_launches++;
   CU(cudaGetLastError());
   const char *tenv = getenv("KRETS_REFINE_TOL");

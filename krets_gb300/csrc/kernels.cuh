@@ -90,6 +90,24 @@ __global__ void k_gather(double *dst, const double *src, const int *q, int n) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) dst[k] = src[q[k]];
 }
 
+// ============================================================== L1 warm-up
+// A single-CTA solve (plain OP, DC sweep, few batched instances) is bound by dependent
+// loads of its program arrays (pivot entry -> update pairs -> LU slots; slot -> stamp
+// contributions) at L2 latency.  The host lists those arrays (factorisation, solves,
+// stamps) and the CTA first issues one L1 prefetch per 128-byte line of each, so the
+// chains then hit L1.  Only addresses inside the listed arrays are touched.
+struct OpWarm {
+  int count;
+  const char *ptr[16];
+  int bytes[16];
+};
+
+__device__ __forceinline__ void warm_l1(const OpWarm &w) {
+  for (int a = 0; a < w.count; ++a)
+    for (int off = threadIdx.x * 128; off < w.bytes[a]; off += blockDim.x * 128)
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(w.ptr[a] + off));
+}
+
 // ============================================================== k_op
 // Newton OP in FP64.  guess0 (optional, original numbering) warm-starts the iteration
 // as the DC sweep does; step_key >= 0 adds the "step" key to the convergence test.
@@ -131,9 +149,10 @@ __device__ int newton_dc(const DevProg &P, const KCfg &cfg, const double *vals, 
 }
 
 __global__ void k_op(DevProg P, KCfg cfg, Lay L, char *gws, const double *values, double *x_out,
-                     size_t out_stride, int *inst_status, int *iters, int n_inst) {
+                     size_t out_stride, int *inst_status, int *iters, int n_inst, OpWarm warm) {
   extern __shared__ __align__(16) char smem[];
   char *base = gws ? gws + (size_t)blockIdx.x * L.bytes : smem;
+  warm_l1(warm);
   ARR(double, lu, 0);
   ARR(double, b, 1);
   ARR(double, x, 2);
@@ -158,9 +177,10 @@ __global__ void k_op(DevProg P, KCfg cfg, Lay L, char *gws, const double *values
 // and stops at its first failing point, as dc::solve returns on the first error.
 __global__ void k_dc_sweep(DevProg P, KCfg cfg, Lay L, char *gws, int sweep_elem, double start, double step,
                            int n_points, const double *values, int n_inst, size_t inst_stride, double *x_out,
-                           int *out_status) {
+                           int *out_status, OpWarm warm) {
   extern __shared__ __align__(16) char smem[];
   char *base = gws ? gws + (size_t)blockIdx.x * L.bytes : smem;
+  warm_l1(warm);
   ARR(double, lu, 0);
   ARR(double, b, 1);
   ARR(double, x, 2);
