@@ -578,13 +578,23 @@ def workload_uneven(args, world, reference):
     # CPU baseline: the same bounded sample as the reference arm, factor once
     idx = list(range(0, UNEVEN_CIRCUITS, 64))
     cdt = _cpu_pool(lambda i: O.tran(tabs[i][0], tabs[i][1], UNEVEN_H, 200, method="be", lag=True), idx, threads)
-    # end to end with a host output buffer: the first circuits up to 8 GB of waveforms
-    k = 0
-    tot = 0
-    while k < len(tabs) and tot + (UNEVEN_STEPS + 1) * tabs[k][1] * 8 < 8e9:
-        tot += (UNEVEN_STEPS + 1) * tabs[k][1] * 8
-        k += 1
-    m2 = _lib.MultiCircuit([t for t, _ in tabs[:k]], [n for _, n in tabs[:k]], method="be", h=UNEVEN_H)
+    # end to end with a host output buffer: every netlist when the waveforms fit in 45 % of
+    # the available host memory, else the first netlists up to 8 GB of waveforms
+    del out
+    try:
+        with open("/proc/meminfo") as f:
+            avail = int([ln for ln in f if ln.startswith("MemAvailable")][0].split()[1]) * 1024
+    except Exception:
+        avail = 0
+    if m.total(UNEVEN_STEPS) * 8 <= 0.45 * avail:
+        k, m2 = len(tabs), m
+    else:
+        k = 0
+        tot = 0
+        while k < len(tabs) and tot + (UNEVEN_STEPS + 1) * tabs[k][1] * 8 < 8e9:
+            tot += (UNEVEN_STEPS + 1) * tabs[k][1] * 8
+            k += 1
+        m2 = _lib.MultiCircuit([t for t, _ in tabs[:k]], [n for _, n in tabs[:k]], method="be", h=UNEVEN_H)
     host = np.empty(m2.total(UNEVEN_STEPS))
     host.fill(0.0)
     for _ in range(3):
