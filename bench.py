@@ -296,6 +296,25 @@ def run_ours(args, rank, world):
             variants[name]["refinement_histogram"] = [int(v) for v in hist]
             variants[name]["fp64_fallbacks"] = int(fallbacks)
 
+    # probe-only variant: the same double-float run writing only the output node each step
+    out_node = c.index_map["V(n200)"]
+    d_probe_out = _lib.DeviceArray((N_INST, N_STEPS + 1, 1))
+    probe_ms = []
+    for r in range(3):
+        g.flush_l2()
+        g.batch_tran_probe(d_vals, H, N_STEPS, [out_node], "tr", lag=False, out=d_probe_out, n_inst=N_INST)
+        if r > 0:
+            probe_ms.append(g.timing())
+    probe_host = np.empty((N_STEPS + 1,))
+    _lib.check(_lib.lib().krets_memcpy_d2h(probe_host.ctypes.data_as(_lib.ctypes.c_void_p),
+                                           _lib.ctypes.c_void_p(d_probe_out.ptr), probe_host.nbytes))
+    del d_probe_out
+    variants["probe_only_output_node"] = {
+        "value": ctsteps / (statistics.mean(cm for _, cm in probe_ms) / 1e3), "unit": UNIT,
+        "kernel_ms": statistics.mean(k for k, _ in probe_ms), "output": "V(n200) only, 8 B per circuit-step",
+        "max_rel_err_vs_fp64": float(np.abs(probe_host - refs[0][:, out_node]).max()
+                                     / np.abs(refs[0][:, out_node]).max())}
+
     # plain GPU form: one instance, FP64, level-scheduled single-CTA kernels per step
     plain_steps = 2000
     g1 = _lib.GpuCircuit(t, n)

@@ -178,6 +178,15 @@ krets_status krets_batch_tran_adaptive(krets_circuit *c, int32_t n_inst, const d
                                        int32_t max_points, double *t_out, double *x_out, int32_t *n_points,
                                        int32_t *inst_status);
 
+/* Probe-only batched transient: as krets_batch_tran in double-float precision
+ * (KRETS_PREC_DF, linear circuits), but each step writes only the unknowns probe[0..n_probe)
+ * (MNA indices, e.g. the output node): x_out[n_inst][n_steps+1][n_probe], row 0 = their
+ * operating-point values.  The arithmetic is that of krets_batch_tran; only the output
+ * traffic differs. */
+krets_status krets_batch_tran_probe(krets_circuit *c, int32_t n_inst, const double *values, double h,
+                                    int32_t n_steps, int32_t method, int32_t source_lag, int32_t n_probe,
+                                    const int32_t *probe, double *x_out, int32_t *inst_status);
+
 /* Batched AC over frequency points of one instance (values NULL) or of several
  * instances: each work item is one (instance, frequency) complex system.
  * precision: FP64 = complex128 factor; MIXED = complex64 factor + complex128 refinement.

@@ -79,6 +79,7 @@ def lib():
             "krets_batch_op": [_P, _I, _P, _P, _P],
             "krets_batch_dc": [_P, _I, _P, _I, _D, _D, _D, _P, _I, _P, _P],
             "krets_batch_tran_adaptive": [_P, _I, _P, _D, _D, _I, _D, _D, _D, _I, _P, _P, _P, _P],
+            "krets_batch_tran_probe": [_P, _I, _P, _D, _I, _I, _I, _I, _P, _P, _P],
             "krets_last_timing": [_P, _P, _P],
             "krets_last_launch": [_P, _P, _I],
             "krets_last_refine_stats": [_P, _P, _P],
@@ -298,6 +299,25 @@ class GpuCircuit:
         check(lib().krets_batch_dc(self.h, ni, ptr(v), sweep_index, start, stop, step, ptr(x), npts,
                                    ctypes.byref(got), ptr(st)), "batch_dc")
         return x[:, :got.value], st
+
+    def batch_tran_probe(self, values, h, n_steps, probe, method="tr", lag=None, out=None, n_inst=None):
+        """Double-float batched transient writing only the unknowns in `probe` each step:
+        [n_inst][n_steps+1][len(probe)]."""
+        m = METHOD[method]
+        if lag is None:
+            lag = m == 0
+        pr = np.ascontiguousarray(probe, dtype=np.int32)
+        if isinstance(values, DeviceArray):
+            ni = values.shape[0] if n_inst is None else n_inst
+        else:
+            values = np.ascontiguousarray(values, dtype=np.float64)
+            ni = values.shape[0]
+        if out is None:
+            out = host_buffer((ni, n_steps + 1, len(pr)))
+        st = np.zeros(ni, dtype=np.int32)
+        check(lib().krets_batch_tran_probe(self.h, ni, ptr(values), h, n_steps, m, int(bool(lag)), len(pr), ptr(pr),
+                                           ptr(out), ptr(st)), "batch_tran_probe")
+        return out
 
     def batch_tran_adaptive(self, values, h0, t_stop, method="tr", lte_tol=1e-3, h_min=None, h_max=None,
                             max_points=20000, n_inst=None):

@@ -1010,7 +1010,7 @@ namespace {
 // Double-float direct engine launch for a group size G: instances per CTA (W) from the
 // shared-memory footprint, the kernel instance and its residency.
 using DfdKernel = void (*)(DevProg, KCfg, DfdLay, const double *, int, double, int, int, int, double *, int *, int *,
-                           int, WaveTab);
+                           int, WaveTab, Probe);
 struct DfdLaunch {
   int W = 1, per_sm = 0;
   size_t smem = 0;
@@ -1036,7 +1036,7 @@ std::map<std::string, int> g_tune;
 
 krets_status dfd_pick_group(krets_circuit *c, const DevProgram *D, const DfdLay &DL, const double *dv,
                             const double *dx, size_t stride, int n_inst, double h, int n_steps, int method, int lag,
-                            int *queue, int opts, const WaveTab &wt, int &G_out, int &how) {
+                            int *queue, int opts, const WaveTab &wt, const Probe &pr, int &G_out, int &how) {
   char key[96];
   snprintf(key, sizeof key, "%016llx/%d/%zu/%d", (unsigned long long)D->host.signature, D->host.n,
            D->host.lu_col.size(), method);
@@ -1059,12 +1059,14 @@ krets_status dfd_pick_group(krets_circuit *c, const DevProgram *D, const DfdLay 
   const int n = D->host.n;
   const int trial = std::max(1, std::min(n_inst, L0.W * L0.per_sm * device_sm_count()));
   DevBuf tout, tst;
-  const size_t row = sizeof(double) * n * ((size_t)steps + 1);
+  const size_t row = sizeof(double) * (pr.n ? pr.n : n) * ((size_t)steps + 1);
   CU(cudaMalloc(&tout.p, row * trial));
   CU(cudaMalloc(&tst.p, sizeof(int) * trial));
-  // the trial instances start from their operating points (row 0 of each waveform)
-  CU(cudaMemcpy2DAsync(tout.p, row, dx, sizeof(double) * stride, sizeof(double) * n, trial, cudaMemcpyDeviceToDevice,
-                       c->stream));
+  // the trial instances start from their operating points (row 0 of each waveform, or
+  // the probe run's separate operating points)
+  if (!pr.n)
+    CU(cudaMemcpy2DAsync(tout.p, row, dx, sizeof(double) * stride, sizeof(double) * n, trial,
+                         cudaMemcpyDeviceToDevice, c->stream));
   double best = 0.0;
   for (int G : {128, 64, 32}) {
     DfdLaunch Lc;
@@ -1076,7 +1078,7 @@ krets_status dfd_pick_group(krets_circuit *c, const DevProgram *D, const DfdLay 
     CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
     CU(cudaEventRecord(c->ev[2], c->stream));
     Lc.kd<<<grid, G * Lc.W, Lc.smem, c->stream>>>(D->view, c->cfg, DL, dv, trial, h, steps, method, lag,
-                                                  (double *)tout.p, (int *)tst.p, queue, opts, wt);
+                                                  (double *)tout.p, (int *)tst.p, queue, opts, wt, pr);
     g_launches++;
     CU(cudaGetLastError());
     CU(cudaEventRecord(c->ev[3], c->stream));
@@ -1097,9 +1099,11 @@ krets_status dfd_pick_group(krets_circuit *c, const DevProgram *D, const DfdLay 
 
 }  // namespace
 
-krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *values, double h, int32_t n_steps,
-                              int32_t method, int32_t source_lag, int32_t precision, double *x_out,
-                              int32_t *inst_status) {
+// Batched transient; with probes (n_probe > 0) only those unknowns are written each step
+// (double-float engine only): x_out[n_inst][n_steps+1][n_probe].
+static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const double *values, double h,
+                                    int32_t n_steps, int32_t method, int32_t source_lag, int32_t precision,
+                                    double *x_out, int32_t *inst_status, const int32_t *probe, int32_t n_probe) {
   if (!c || !x_out || n_inst <= 0 || n_steps < 0 || !(h > 0)) return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments");
   DevProgram *Ddc, *Dtr;
   krets_status s = get_program(c, MODE_DC, 0, 0, 0, &Ddc);
@@ -1107,8 +1111,9 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
   s = get_program(c, MODE_TRAN, method, h, 0, &Dtr);
   if (s != KRETS_OK) return s;
   CU(cudaEventRecord(c->ev[0], c->stream));
-  size_t stride = (size_t)c->n * ((size_t)n_steps + 1);
-  DevBuf tv, tx, ts, tfb, twave;
+  const int n_out = n_probe > 0 ? n_probe : c->n;
+  size_t stride = (size_t)n_out * ((size_t)n_steps + 1);
+  DevBuf tv, tx, ts, tfb, twave, top, tprobe;
   void *dv, *dx;
   s = dev_view(values, sizeof(double) * c->ne * (size_t)n_inst, true, c->stream, tv, &dv);
   if (s) return s;
@@ -1117,7 +1122,18 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
   CU(cudaMalloc(&ts.p, sizeof(int) * 2 * (size_t)n_inst));
   int *d_st = (int *)ts.p, *d_opst = d_st + n_inst;
   CU(cudaMemsetAsync(ts.p, 0, sizeof(int) * 2 * (size_t)n_inst, c->stream));
-  s = run_op(c, Ddc, n_inst, (const double *)dv, (double *)dx, stride, d_opst, nullptr, 128);
+  Probe pr{nullptr, 0, nullptr};
+  if (n_probe > 0) {
+    // operating points in a separate [n_inst][n] buffer; the probe list on the device
+    CU(cudaMalloc(&top.p, sizeof(double) * c->n * (size_t)n_inst));
+    void *dp;
+    s = dev_view(probe, sizeof(int32_t) * n_probe, true, c->stream, tprobe, &dp);
+    if (s) return s;
+    pr = Probe{(const int *)dp, n_probe, (const double *)top.p};
+    s = run_op(c, Ddc, n_inst, (const double *)dv, (double *)top.p, c->n, d_opst, nullptr, 128);
+  } else {
+    s = run_op(c, Ddc, n_inst, (const double *)dv, (double *)dx, stride, d_opst, nullptr, 128);
+  }
   if (s) return s;
   const bool dfd = precision == KRETS_PREC_DF;
   bool mixed = precision == KRETS_PREC_MIXED;
@@ -1169,6 +1185,9 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
     DL.sprog_bytes = (int)align16((size_t)P.sp_off[5] * sizeof(int));
     if ((size_t)DL.bytes + DL.sprog_bytes > max_smem_optin()) use_dfd = false;
   }
+  if (n_probe > 0 && !use_dfd)
+    return fail(KRETS_ERR_INVALID_ARGUMENT,
+                "probe outputs need the double-float engine (precision 2, a linear circuit that fits)");
   if (use_dfd) {
     // PULSE / SIN sources tabulated per step (their parameters are not per-instance values)
     const Program &H = Dtr->host;
@@ -1203,7 +1222,7 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
       if (G != 32 && G != 64 && G != 128) G = 128;
     } else {
       s = dfd_pick_group(c, Dtr, DL, (const double *)dv, (const double *)dx, stride, n_inst, h, n_steps, method,
-                         source_lag, queue, opts, wt, G, how);
+                         source_lag, queue, opts, wt, pr, G, how);
       if (s != KRETS_OK) return s;
     }
     DfdLaunch Lc;
@@ -1220,7 +1239,7 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
     CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
     CU(cudaEventRecord(c->ev[2], c->stream));
     Lc.kd<<<grid, G * W, Lc.smem, c->stream>>>(P, c->cfg, DL, (const double *)dv, n_inst, h, n_steps, method,
-                                               source_lag, (double *)dx, d_st, queue, opts, wt);
+                                               source_lag, (double *)dx, d_st, queue, opts, wt, pr);
   } else if (warp_engine) {
     const char *bud = getenv("KRETS_SMEM_BUDGET");
     size_t budget = bud ? (size_t)atol(bud) : max_smem_optin();
@@ -1299,6 +1318,23 @@ krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *va
   }
   if (any_op) return map_status(any_op, 0);
   return map_status(any, 1);
+}
+
+krets_status krets_batch_tran(krets_circuit *c, int32_t n_inst, const double *values, double h, int32_t n_steps,
+                              int32_t method, int32_t source_lag, int32_t precision, double *x_out,
+                              int32_t *inst_status) {
+  return batch_tran_impl(c, n_inst, values, h, n_steps, method, source_lag, precision, x_out, inst_status, nullptr, 0);
+}
+
+krets_status krets_batch_tran_probe(krets_circuit *c, int32_t n_inst, const double *values, double h, int32_t n_steps,
+                                    int32_t method, int32_t source_lag, int32_t n_probe, const int32_t *probe,
+                                    double *x_out, int32_t *inst_status) {
+  if (!c || !probe || n_probe <= 0) return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid probe list");
+  if (!is_device_ptr(probe))
+    for (int j = 0; j < n_probe; ++j)
+      if (probe[j] < 0 || probe[j] >= c->n) return fail(KRETS_ERR_INVALID_ARGUMENT, "probe index out of range");
+  return batch_tran_impl(c, n_inst, values, h, n_steps, method, source_lag, KRETS_PREC_DF, x_out, inst_status, probe,
+                         n_probe);
 }
 
 krets_status krets_adjoint_tran(krets_circuit *c, int32_t n_inst, const double *values, double h, int32_t n_steps,

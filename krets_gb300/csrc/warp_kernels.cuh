@@ -1363,11 +1363,22 @@ __global__ void k_wave_table(const krets_element *el, const int *src_elem, int n
   }
 }
 
+// Output selection of the double-float transient: n = 0 writes every unknown each step;
+// otherwise only the unknowns idx[0..n) (original numbering), in that order, and the
+// instance's operating point is read from x0 ([n_inst][P.n]) instead of its output row 0.
+struct Probe {
+  const int *idx;
+  int n;
+  const double *x0;
+};
+
 template <int G, int SG = G>
 __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const df *lu, df *x, const df *cdyn, df *cb,
                                          df *icap, const double *vals, double h, int n_steps, int method, int lag,
                                          double *out, int lnar, int unar, bool int_cvt, int gl, int gid,
-                                         WaveTab wt = WaveTab{nullptr, nullptr, 0}) {
+                                         WaveTab wt = WaveTab{nullptr, nullptr, 0},
+                                         Probe pr = Probe{nullptr, 0, nullptr}) {
+  const int n_out = pr.n ? pr.n : P.n;
   int st = 0;
   for (int s = 1; s <= n_steps; ++s) {
     const double t = (double)s * h;
@@ -1413,12 +1424,12 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
         icap[d] = df_sub(df_mul(cdyn[d], vn), cb[d]);
       }
     }
-    double *row = out + (size_t)s * P.n;
-    for (int k = gl; k < P.n; k += G) {
-      const df xv = x[S.qinv[k]];
+    double *row = out + (size_t)s * n_out;
+    for (int j = gl; j < n_out; j += G) {
+      const df xv = x[S.qinv[pr.n ? pr.idx[j] : j]];
       const double v = int_cvt ? df_to_double_int(xv) : df_to_double(xv);
       if (!isfinite(v)) st |= KS_NONFINITE;
-      __stcs(row + k, v);
+      __stcs(row + j, v);
     }
     // no barrier: the next step's first phase reads x (final since the last solve level)
     // and writes only this thread's cb / reads this thread's icap entries; its barrier
@@ -1432,7 +1443,7 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
 template <int G>
 __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay L, const double *values, int n_inst,
                                                      double h, int n_steps, int method, int lag, double *x_out,
-                                                     int *inst_status, int *queue, int opts, WaveTab wt) {
+                                                     int *inst_status, int *queue, int opts, WaveTab wt, Probe pr) {
   extern __shared__ __align__(16) char smem[];
   const int gl = threadIdx.x % G, gid = threadIdx.x / G;
   {
@@ -1457,7 +1468,7 @@ __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
   df *icap = reinterpret_cast<df *>(base + L.icap);
   int *slot = reinterpret_cast<int *>(base + L.slot);
   double *coef64 = reinterpret_cast<double *>(base + L.coef64);  // set-up only
-  const size_t stride = (size_t)(n_steps + 1) * P.n;
+  const size_t stride = (size_t)(n_steps + 1) * (pr.n ? pr.n : P.n);
   while (true) {
     if (gl == 0) slot[0] = atomicAdd(queue, 1);
     gsync<G>(gid);
@@ -1466,12 +1477,14 @@ __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
     if (inst >= n_inst) break;
     const double *vals = values ? values + (size_t)inst * P.ne : nullptr;
     double *out = x_out + (size_t)inst * stride;
+    const double *op = pr.x0 ? pr.x0 + (size_t)inst * P.n : out;  // operating point
     int st = dfd_setup<G>(P, S, vals, h, method, lu, lu64, coef64, cdyn, gl, gid);
-    for (int k = gl; k < P.n; k += G) x[k] = df_from_double(out[P.q[k]]);
+    for (int k = gl; k < P.n; k += G) x[k] = df_from_double(op[P.q[k]]);
+    for (int j = gl; j < pr.n; j += G) out[j] = op[pr.idx[j]];  // probe row 0
     for (int d = gl; d < P.ncap; d += G) icap[d] = df{0.f, 0.f};
     const bool fatal = gany<G>((st & (KS_SINGULAR | KS_NONFINITE | KS_NOTIMPL)) != 0, gid);
     if (!fatal) st |= dfd_steps<G>(P, S, lu, x, cdyn, cb, icap, vals, h, n_steps, method, lag, out, lnar, unar, int_cvt,
-                                   gl, gid, wt);
+                                   gl, gid, wt, pr);
     if (gl == 0) slot[1] = 0;
     gsync<G>(gid);
     if (st) atomicOr(&slot[1], st);

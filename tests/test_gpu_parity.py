@@ -297,6 +297,23 @@ def test_double_float_group_size_autotuner(oracle_lib, monkeypatch):
         assert rel_err(x[i], ref, mask) < TOL and rel_err(y[i], ref, mask) < TOL
 
 
+def test_probe_only_transient_equals_full_waveform_columns():
+    """The probe-only run writes exactly the probed columns of the full double-float run
+    (same arithmetic, bit for bit), row 0 included; out-of-range probes are rejected."""
+    c = rlc_ladder(40)
+    t = element_table(c)
+    vals = monte_carlo_values(c, 37, seed=17)
+    g = _lib.GpuCircuit(t, c.size)
+    full = g.batch_tran(vals, 1e-12, 400, "tr", lag=False, precision=_lib.PREC_DF)
+    probe = [c.index_map["V(n40)"], c.index_map["V(n1)"], c.index_map["I(V1)"]]
+    got = g.batch_tran_probe(vals, 1e-12, 400, probe, "tr", lag=False)
+    assert got.shape == (37, 401, 3)
+    assert np.array_equal(got, full[:, :, probe])
+    from krets_gb300.errors import KretsError
+    with pytest.raises(KretsError):
+        g.batch_tran_probe(vals, 1e-12, 10, [c.size], "tr")
+
+
 def test_zero_step_transient_is_the_operating_point(oracle_lib):
     """stop_time < time_step / 2 gives num_steps = 0: the result is the t = 0 operating
     point alone (transient.rs:14-114)."""
