@@ -312,8 +312,10 @@ def run_ours(args, rank, world):
     variants["probe_only_output_node"] = {
         "value": ctsteps / (statistics.mean(cm for _, cm in probe_ms) / 1e3), "unit": UNIT,
         "kernel_ms": statistics.mean(k for k, _ in probe_ms), "output": "V(n200) only, 8 B per circuit-step",
+        # the front needs ~20 ns to reach n200 (0.1 ns per section), so within 10 ns V(n200)
+        # stays near 1e-300: the error is scaled by the 1 uV voltage tolerance as well
         "max_rel_err_vs_fp64": float(np.abs(probe_host - refs[0][:, out_node]).max()
-                                     / np.abs(refs[0][:, out_node]).max())}
+                                     / max(np.abs(refs[0][:, out_node]).max(), 1e-6))}
 
     # plain GPU form: one instance, FP64, level-scheduled single-CTA kernels per step
     plain_steps = 2000
