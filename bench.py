@@ -338,6 +338,8 @@ def run_ours(args, rank, world):
     # CPU baseline: optimised oracle (factor once) on the host cores, bounded sample
     threads = os.cpu_count() or 1
     r1, dt1 = cpu_rate(t, vals, n, [0], 500, False, 1)
+    # the reference's cost model (rebuild and refactor every step) on one core, short sample
+    rf1, _ = cpu_rate(t, vals, n, [0], 200, True, 1)
     per_inst_s = N_STEPS / r1
     n_sample = max(threads, min(8 * threads, int(15.0 * threads / max(per_inst_s, 1e-3))))
     cpu_val, cpu_dt = cpu_rate(t, vals, n, list(range(n_sample)), N_STEPS, False, threads)
@@ -401,7 +403,8 @@ def run_ours(args, rank, world):
                      "traffic_note": "ncu DRAM bytes of a 304 x 1000-step capture scaled per circuit-step",
                      "kernel": "k_tran_dfd<128>", "algorithmic_bytes_per_launch": alg_bytes},
         "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{n_sample} instances x {N_STEPS} TR steps, factor once, oracle/ C restatement"},
+                         "sample": f"{n_sample} instances x {N_STEPS} TR steps, factor once, oracle/ C restatement",
+                         "one_core_factor_once": r1, "one_core_refactor_every_step": rf1},
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(host_vals.nbytes),
                 "d2h_bytes_per_step": int(e2e_inst * (N_STEPS + 1) * n * 8), "instances": e2e_inst,
                 "instances_per_wave": wave, "device_resident_same_instances": same_val,
