@@ -396,7 +396,8 @@ def run_ours(args, rank, world):
         "max_rel_err_vs_fp64": max(errs),
         "engine": engine,
         "precision_variants": variants,
-        "plain_form": {"value": plain_rate, "unit": UNIT, "what": "1 instance, FP64, per-step kernels (CUDA graph)"},
+        "plain_form": {"value": plain_rate, "unit": UNIT, "what": "1 instance, FP64, per-step kernels (CUDA graph); linear: factored once and reused, "
+                               "as the batched form"},
         "batched_over_plain": value / plain_rate,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
