@@ -161,7 +161,9 @@ __device__ __forceinline__ void adj_forward_step(const DevProg &P, const SProg &
 // Buffers per CTA (global memory): checkpoints J x (n + ncap), three segment buffers of
 // (K+1) x n states (segment j in buffer j % 3) and two lambda histories of K x n (j & 1).
 //
-// mode 0: forward pass only (loss), mode 1: loss and gradient.
+// mode 0: forward pass only (loss), mode 1: loss and gradient, mode 2: gradient only, the
+// forward pass having run on the double-float engine (k_tran_dfd with AdjFwd: per-instance
+// checkpoints and the loss); the last segment is then recomputed from its checkpoint.
 // adj: per element {kind, row position of p, row position of m, row position of branch}
 // cc_ptr/cc_op: per column position, the rhs contributions of C^T lambda: range
 //       [cc_ptr[j], cc_ptr[j+1]) of (dyn index << 1 | neg) entries.
@@ -221,7 +223,7 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
   const int J = (n_steps + K - 1) / K;          // segments
   const size_t ck_words = (size_t)n + P.ncap;  // per checkpoint, in df
   const size_t seg_words = (size_t)(K + 1) * n, hist_words = (size_t)K * n;
-  df *my_ck = ckpt + (size_t)blockIdx.x * J * ck_words;
+  df *cta_ck = ckpt + (size_t)blockIdx.x * J * ck_words;  // modes 0/1: the CTA's checkpoints
   df *my_seg = seg + (size_t)blockIdx.x * 3 * seg_words;
   df *my_hist = hist + (size_t)blockIdx.x * 2 * hist_words;
   while (true) {
@@ -231,6 +233,8 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
     __syncthreads();
     if (inst >= n_inst) break;
     const double *vals = values ? values + (size_t)inst * P.ne : nullptr;
+    // mode 2: the forward pass ran on the double-float engine, checkpoints per instance
+    df *my_ck = mode == 2 ? ckpt + (size_t)inst * J * ck_words : cta_ck;
     // ---- set-up (as the double-float transient engine)
     int st = g_coef_pass<GF>(P, vals, h, method, coef64, tid);
     gsync<GF>(0);
@@ -263,7 +267,7 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
     // ---- forward pass with checkpoints; the last segment's states go to its buffer
     const int last0 = (J - 1) * K;
     df *last_seg = my_seg + (size_t)((J - 1) % 3) * seg_words;
-    for (int s = 1; s <= n_steps && !fatal; ++s) {
+    for (int s = 1; s <= n_steps && !fatal && mode != 2; ++s) {
       if ((s - 1) % K == 0) {
         df *ck = my_ck + (size_t)((s - 1) / K) * ck_words;
         for (int k = tid; k < n; k += GF) ck[k] = x[k];
@@ -312,7 +316,22 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
         }
       }
     };
-    if (mode == 1 && !fatal) {
+    if (mode == 2 && !fatal) {
+      // the last segment's states, from its checkpoint (the forward pass kept none)
+      const df *ck = my_ck + (size_t)(J - 1) * ck_words;
+      for (int k = tid; k < n; k += GF) {
+        x[k] = ck[k];
+        last_seg[k] = ck[k];
+      }
+      for (int d = tid; d < P.ncap; d += GF) icap[d] = ck[n + d];
+      gsync<GF>(0);
+      for (int s = last0 + 1; s <= n_steps; ++s) {
+        adj_forward_step<GF, GF>(P, S, lu, x, cdyn, cb, icap, vals, method, s, h, wt, tid, 0);
+        for (int k = tid; k < n; k += GF) last_seg[(size_t)(s - last0) * n + k] = x[k];
+      }
+      gsync<GF>(0);
+    }
+    if ((mode == 1 || mode == 2) && !fatal) {
       for (int k = tid; k < n; k += GF) lam[k] = df{0.f, 0.f};
       ekind = 0;
       if (back_half) {
@@ -459,7 +478,7 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
       }
     }
     if (tid == 0) {
-      loss_out[inst] = df_to_double(loss);
+      if (mode != 2) loss_out[inst] = df_to_double(loss);
       slot[1] = 0;
     }
     __syncthreads();

@@ -1010,12 +1010,29 @@ namespace {
 // Double-float direct engine launch for a group size G: instances per CTA (W) from the
 // shared-memory footprint, the kernel instance and its residency.
 using DfdKernel = void (*)(DevProg, KCfg, DfdLay, const double *, int, double, int, int, int, double *, int *, int *,
-                           int, WaveTab, Probe);
+                           int, WaveTab, Probe, AdjFwd);
 struct DfdLaunch {
   int W = 1, per_sm = 0;
   size_t smem = 0;
   DfdKernel kd = nullptr;
 };
+
+// Shared-memory layout of one double-float instance; false when it does not fit a CTA.
+bool dfd_layout(const DevProg &P, DfdLay &DL) {
+  size_t cur = 0;
+  auto put = [&](int &off, size_t bytes) { off = (int)cur; cur = align16(cur + bytes); };
+  put(DL.lu, 8 * (size_t)P.nnz_lu);
+  put(DL.x, 8 * (size_t)P.n);
+  put(DL.cdyn, 8 * (size_t)P.ndyn);
+  put(DL.cb, 8 * (size_t)P.ndyn);
+  put(DL.icap, 8 * (size_t)P.ncap);
+  DL.coef64 = DL.x;  // set-up scratch over x / cdyn / cb / icap (+ padding if needed)
+  if (cur - DL.x < 8 * (size_t)P.ne) cur = DL.x + align16(8 * (size_t)P.ne);
+  put(DL.slot, 16);
+  DL.bytes = (int)align16(cur);
+  DL.sprog_bytes = (int)align16((size_t)P.sp_off[5] * sizeof(int));
+  return (size_t)DL.bytes + DL.sprog_bytes <= max_smem_optin();
+}
 
 krets_status dfd_config(int G, const DfdLay &DL, DfdLaunch &Lc) {
   Lc.W = (int)std::max<size_t>(1, std::min<size_t>(640 / G, (max_smem_optin() - DL.sprog_bytes) / DL.bytes));
@@ -1078,7 +1095,8 @@ krets_status dfd_pick_group(krets_circuit *c, const DevProgram *D, const DfdLay 
     CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
     CU(cudaEventRecord(c->ev[2], c->stream));
     Lc.kd<<<grid, G * Lc.W, Lc.smem, c->stream>>>(D->view, c->cfg, DL, dv, trial, h, steps, method, lag,
-                                                  (double *)tout.p, (int *)tst.p, queue, opts, wt, pr);
+                                                  (double *)tout.p, (int *)tst.p, queue, opts, wt, pr,
+                                                  AdjFwd{nullptr, 1, 0, 0, nullptr});
     g_launches++;
     CU(cudaGetLastError());
     CU(cudaEventRecord(c->ev[3], c->stream));
@@ -1170,21 +1188,7 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
   // engine may not
   DfdLay DL{};
   bool use_dfd = dfd && !P.nonlinear && P.sprog_ok && !(eng && strcmp(eng, "block") == 0);
-  if (use_dfd) {
-    size_t cur = 0;
-    auto put = [&](int &off, size_t bytes) { off = (int)cur; cur = align16(cur + bytes); };
-    put(DL.lu, 8 * (size_t)P.nnz_lu);
-    put(DL.x, 8 * (size_t)P.n);
-    put(DL.cdyn, 8 * (size_t)P.ndyn);
-    put(DL.cb, 8 * (size_t)P.ndyn);
-    put(DL.icap, 8 * (size_t)P.ncap);
-    DL.coef64 = DL.x;  // set-up scratch over x / cdyn / cb / icap (+ padding if needed)
-    if (cur - DL.x < 8 * (size_t)P.ne) cur = DL.x + align16(8 * (size_t)P.ne);
-    put(DL.slot, 16);
-    DL.bytes = (int)align16(cur);
-    DL.sprog_bytes = (int)align16((size_t)P.sp_off[5] * sizeof(int));
-    if ((size_t)DL.bytes + DL.sprog_bytes > max_smem_optin()) use_dfd = false;
-  }
+  if (use_dfd) use_dfd = dfd_layout(P, DL);
   if (n_probe > 0 && !use_dfd)
     return fail(KRETS_ERR_INVALID_ARGUMENT,
                 "probe outputs need the double-float engine (precision 2, a linear circuit that fits)");
@@ -1239,7 +1243,8 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
     CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
     CU(cudaEventRecord(c->ev[2], c->stream));
     Lc.kd<<<grid, G * W, Lc.smem, c->stream>>>(P, c->cfg, DL, (const double *)dv, n_inst, h, n_steps, method,
-                                               source_lag, (double *)dx, d_st, queue, opts, wt, pr);
+                                               source_lag, (double *)dx, d_st, queue, opts, wt, pr,
+                                               AdjFwd{nullptr, 1, 0, 0, nullptr});
   } else if (warp_engine) {
     const char *bud = getenv("KRETS_SMEM_BUDGET");
     size_t budget = bud ? (size_t)atol(bud) : max_smem_optin();
@@ -1437,7 +1442,14 @@ krets_status krets_adjoint_tran(krets_circuit *c, int32_t n_inst, const double *
   const int grid = std::max(1, std::min(n_inst, per_sm * device_sm_count()));
   const int K = std::min(checkpoint_every, n_steps);
   const int J = (n_steps + K - 1) / K;
-  CU(cudaMalloc(&tck.p, sizeof(df) * (size_t)grid * J * ((size_t)P.n + P.ncap)));
+  // The forward pass runs on the double-float transient engine when the instance fits it
+  // (several instances per SM, checkpoints per instance), then the reverse sweep runs here
+  // (mode 2); otherwise both run in this kernel (checkpoints per CTA).
+  // KRETS_ADJ_SINGLE=1 forces the single-kernel form.
+  DfdLay DL{};
+  const char *single = getenv("KRETS_ADJ_SINGLE");
+  const bool split = dfd_layout(P, DL) && !(single && single[0] == '1');
+  CU(cudaMalloc(&tck.p, sizeof(df) * (size_t)(split ? n_inst : grid) * J * ((size_t)P.n + P.ncap)));
   // three segment buffers of K+1 states and two lambda histories of K vectors per CTA
   const size_t seg_bytes = sizeof(df) * (size_t)grid * 3 * ((size_t)K + 1) * P.n;
   const size_t hist_bytes = sizeof(df) * (size_t)grid * 2 * (size_t)K * P.n;
@@ -1480,19 +1492,38 @@ krets_status krets_adjoint_tran(krets_circuit *c, int32_t n_inst, const double *
       wt.row = d_wrow;
     }
   }
+  DevBuf tstf;
+  CU(cudaMalloc(&tstf.p, sizeof(int) * n_inst));
+  CU(cudaMemsetAsync(tstf.p, 0, sizeof(int) * n_inst, c->stream));
   CU(cudaEventRecord(c->ev[2], c->stream));
-  ka<<<grid, kAdjThreads, smem, c->stream>>>(P, AL, (const double *)dv, n_inst, h, n_steps, method, K,
-                                             H.qinv[out_unknown], (const int4 *)d_adj, d_ccp, d_cco, (df *)tck.p,
-                                             (df *)tseg.p, d_hist, (double *)d_loss, (double *)d_grad, (int *)tst.p,
-                                             queue, gradient ? 1 : 0, wt);
-  g_launches++;
-  CU(cudaGetLastError());
+  if (split) {
+    DfdLaunch Lf;
+    s = dfd_config(128, DL, Lf);
+    if (s != KRETS_OK) return s;
+    const int fgrid = std::max(1, std::min((n_inst + Lf.W - 1) / Lf.W, Lf.per_sm * device_sm_count()));
+    const AdjFwd af{(df *)tck.p, K, P.n + P.ncap, H.qinv[out_unknown], (double *)d_loss};
+    Lf.kd<<<fgrid, 128 * Lf.W, Lf.smem, c->stream>>>(P, c->cfg, DL, (const double *)dv, n_inst, h, n_steps, method,
+                                                     0, nullptr, (int *)tstf.p, queue, 0, wt,
+                                                     Probe{nullptr, 0, nullptr}, af);
+    g_launches++;
+    CU(cudaGetLastError());
+    CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
+  }
+  if (!split || gradient) {
+    ka<<<grid, kAdjThreads, smem, c->stream>>>(P, AL, (const double *)dv, n_inst, h, n_steps, method, K,
+                                               H.qinv[out_unknown], (const int4 *)d_adj, d_ccp, d_cco, (df *)tck.p,
+                                               (df *)tseg.p, d_hist, (double *)d_loss, (double *)d_grad,
+                                               (int *)tst.p, queue, split ? 2 : (gradient ? 1 : 0), wt);
+    g_launches++;
+    CU(cudaGetLastError());
+  }
   CU(cudaEventRecord(c->ev[3], c->stream));
   if (dl_loss.p) CU(cudaMemcpyAsync(loss_out, d_loss, sizeof(double) * n_inst, cudaMemcpyDeviceToHost, c->stream));
   if (dl_grad.p)
     CU(cudaMemcpyAsync(grad_out, d_grad, sizeof(double) * (size_t)n_inst * c->ne, cudaMemcpyDeviceToHost, c->stream));
-  std::vector<int> st(n_inst);
+  std::vector<int> st(n_inst), stf(n_inst);
   CU(cudaMemcpyAsync(st.data(), tst.p, sizeof(int) * n_inst, cudaMemcpyDeviceToHost, c->stream));
+  CU(cudaMemcpyAsync(stf.data(), tstf.p, sizeof(int) * n_inst, cudaMemcpyDeviceToHost, c->stream));
   CU(cudaEventRecord(c->ev[1], c->stream));
   CU(cudaStreamSynchronize(c->stream));
   cudaEventElapsedTime(&c->kernel_ms, c->ev[2], c->ev[3]);
@@ -1500,7 +1531,7 @@ krets_status krets_adjoint_tran(krets_circuit *c, int32_t n_inst, const double *
   c->warps_per_cta = kAdjThreads / 32;
   c->grid = grid;
   int any = 0;
-  for (int v : st) any |= v;
+  for (int i = 0; i < n_inst; ++i) any |= st[i] | stf[i];
   return map_status(any, 1);
 }
 

@@ -1372,17 +1372,35 @@ struct Probe {
   const double *x0;
 };
 
+// Forward pass of the adjoint on this engine: from x_0 = 0 (zero operating point), no
+// waveform output; before step s with (s-1) % K == 0 the state (x in position space, the
+// TR capacitor currents) goes to checkpoint (s-1)/K at ck + that * ck_words, and
+// sum_n x_n[out_pos]^2 is accumulated in double-float and written to *loss.  ck and loss
+// point at the instance's own slots (ck == nullptr: not an adjoint forward pass).
+struct AdjFwd {
+  df *ck;
+  int K, ck_words, out_pos;
+  double *loss;
+};
+
 template <int G, int SG = G>
 __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const df *lu, df *x, const df *cdyn, df *cb,
                                          df *icap, const double *vals, double h, int n_steps, int method, int lag,
                                          double *out, int lnar, int unar, bool int_cvt, int gl, int gid,
                                          WaveTab wt = WaveTab{nullptr, nullptr, 0},
-                                         Probe pr = Probe{nullptr, 0, nullptr}) {
+                                         Probe pr = Probe{nullptr, 0, nullptr},
+                                         AdjFwd af = AdjFwd{nullptr, 1, 0, 0, nullptr}) {
   const int n_out = pr.n ? pr.n : P.n;
+  df loss{0.f, 0.f};  // adjoint forward pass: lane 0 of the group accumulates
   int st = 0;
   for (int s = 1; s <= n_steps; ++s) {
     const double t = (double)s * h;
     const double t_src = lag ? (double)(s - 1) * h : t;
+    if (af.ck && (s - 1) % af.K == 0) {  // x and icap are final: the previous step's last level synced
+      df *ck = af.ck + (size_t)((s - 1) / af.K) * af.ck_words;
+      for (int k = gl; k < P.n; k += G) ck[k] = x[k];
+      for (int d = gl; d < P.ncap; d += G) ck[P.n + d] = icap[d];
+    }
     for (int d = gl; d < P.ndyn; d += G) {
       const int4 dd = S.dyn[d];
       const int kind = (int)((unsigned)dd.x >> 24);
@@ -1424,6 +1442,10 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
         icap[d] = df_sub(df_mul(cdyn[d], vn), cb[d]);
       }
     }
+    if (af.ck) {
+      if (gl == 0) loss = df_fma(x[af.out_pos], x[af.out_pos], loss);
+      continue;  // no waveform output in the adjoint forward pass
+    }
     double *row = out + (size_t)s * n_out;
     for (int j = gl; j < n_out; j += G) {
       const df xv = x[S.qinv[pr.n ? pr.idx[j] : j]];
@@ -1436,6 +1458,7 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
     // orders every read of x before the gather overwrites it.  Callers synchronise the
     // group after the last step.
   }
+  if (af.loss && gl == 0) *af.loss = df_to_double(loss);
   return st;
 }
 
@@ -1443,7 +1466,8 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
 template <int G>
 __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay L, const double *values, int n_inst,
                                                      double h, int n_steps, int method, int lag, double *x_out,
-                                                     int *inst_status, int *queue, int opts, WaveTab wt, Probe pr) {
+                                                     int *inst_status, int *queue, int opts, WaveTab wt, Probe pr,
+                                                     AdjFwd af) {
   extern __shared__ __align__(16) char smem[];
   const int gl = threadIdx.x % G, gid = threadIdx.x / G;
   {
@@ -1476,15 +1500,20 @@ __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
     gsync<G>(gid);
     if (inst >= n_inst) break;
     const double *vals = values ? values + (size_t)inst * P.ne : nullptr;
-    double *out = x_out + (size_t)inst * stride;
-    const double *op = pr.x0 ? pr.x0 + (size_t)inst * P.n : out;  // operating point
+    double *out = x_out ? x_out + (size_t)inst * stride : nullptr;
+    const double *op = pr.x0 ? pr.x0 + (size_t)inst * P.n : out;  // operating point (none: x_0 = 0)
     int st = dfd_setup<G>(P, S, vals, h, method, lu, lu64, coef64, cdyn, gl, gid);
-    for (int k = gl; k < P.n; k += G) x[k] = df_from_double(op[P.q[k]]);
+    for (int k = gl; k < P.n; k += G) x[k] = op ? df_from_double(op[P.q[k]]) : df{0.f, 0.f};
     for (int j = gl; j < pr.n; j += G) out[j] = op[pr.idx[j]];  // probe row 0
+    AdjFwd a = af;
+    if (af.ck) {
+      a.ck = af.ck + (size_t)inst * ((n_steps + af.K - 1) / af.K) * af.ck_words;
+      a.loss = af.loss + inst;
+    }
     for (int d = gl; d < P.ncap; d += G) icap[d] = df{0.f, 0.f};
     const bool fatal = gany<G>((st & (KS_SINGULAR | KS_NONFINITE | KS_NOTIMPL)) != 0, gid);
     if (!fatal) st |= dfd_steps<G>(P, S, lu, x, cdyn, cb, icap, vals, h, n_steps, method, lag, out, lnar, unar, int_cvt,
-                                   gl, gid, wt, pr);
+                                   gl, gid, wt, pr, a);
     if (gl == 0) slot[1] = 0;
     gsync<G>(gid);
     if (st) atomicOr(&slot[1], st);
