@@ -727,10 +727,10 @@ def workload_adjoint(args, world, reference):
         "grad_rel_err_vs_central_fd_1e-4": fd4_err,
         "roofline": {"bound": "hbm", "achieved": alg / k_s / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": alg / k_s / 1e9 / peak, "traffic": ADJ_TRAFFIC_PER_INST_STEP * ADJ_INST * ADJ_STEPS,
-                     "traffic_note": "ncu DRAM bytes of a 152 x 300-step capture scaled per instance-step; "
-                                     "beyond the algorithmic bytes: segment states and lambda histories "
-                                     "exchanged between the CTA halves",
-                     "peak_kind": pk, "kernel": "k_adjoint_dfd", "algorithmic_bytes_per_launch": alg},
+                     "traffic_note": "ncu DRAM bytes of a 152 x 300-step capture of the single-kernel form "
+                                     "scaled per instance-step; beyond the algorithmic bytes: segment states "
+                                     "and lambda histories exchanged between the CTA halves",
+                     "peak_kind": pk, "kernel": "k_tran_dfd (forward) + k_adjoint_dfd (reverse)", "algorithmic_bytes_per_launch": alg},
         "cpu_baseline": {"value": n_s / cdt, "unit": "gradients/s", "cores": threads, "kind": "port",
                          "sample": f"{n_s} FP64 adjoint gradients (oracle/)"},
         "e2e": {"value": ADJ_INST / (statistics.mean(cs) / 1e3), "unit": "gradients/s",
