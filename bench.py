@@ -644,10 +644,11 @@ def workload_uneven(args, world, reference):
 
 
 ADJ_INST, ADJ_SECTIONS, ADJ_STEPS, ADJ_H, ADJ_K = 1024, 1000, 2000, 1e-9, 100
-# DRAM bytes per instance-step of k_adjoint_dfd from an ncu capture of 152 instances x 300
-# steps (profiles/k_adjoint_dfd_rc1000_152x300.md: 707 MB read + 746 MB written): the
-# segment states and lambda histories the two halves of a CTA exchange through L2/DRAM
-ADJ_TRAFFIC_PER_INST_STEP = (707e6 + 746e6) / (152 * 300)
+# DRAM bytes per instance-step of the adjoint (forward k_tran_dfd + reverse k_adjoint_dfd)
+# from an ncu capture of 152 instances x 300 steps (profiles/k_adjoint_dfd_rc1000_152x300.md:
+# 0.56 + 704.66 MB read, 734.83 MB written): the segment states and lambda histories the two
+# halves of the reverse kernel's CTAs exchange through L2/DRAM
+ADJ_TRAFFIC_PER_INST_STEP = (0.56e6 + 704.66e6 + 734.83e6) / (152 * 300)
 
 
 def workload_adjoint(args, world, reference):
@@ -727,9 +728,9 @@ def workload_adjoint(args, world, reference):
         "grad_rel_err_vs_central_fd_1e-4": fd4_err,
         "roofline": {"bound": "hbm", "achieved": alg / k_s / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": alg / k_s / 1e9 / peak, "traffic": ADJ_TRAFFIC_PER_INST_STEP * ADJ_INST * ADJ_STEPS,
-                     "traffic_note": "ncu DRAM bytes of a 152 x 300-step capture of the single-kernel form "
-                                     "scaled per instance-step; beyond the algorithmic bytes: segment states "
-                                     "and lambda histories exchanged between the CTA halves",
+                     "traffic_note": "ncu DRAM bytes of a 152 x 300-step capture scaled per instance-step; "
+                                     "beyond the algorithmic bytes: segment states and lambda histories "
+                                     "exchanged between the halves of the reverse kernel's CTAs",
                      "peak_kind": pk, "kernel": "k_tran_dfd (forward) + k_adjoint_dfd (reverse)", "algorithmic_bytes_per_launch": alg},
         "cpu_baseline": {"value": n_s / cdt, "unit": "gradients/s", "cores": threads, "kind": "port",
                          "sample": f"{n_s} FP64 adjoint gradients (oracle/)"},
