@@ -144,3 +144,19 @@ def test_adjoint_full_size_config5(oracle_lib):
     L, gref = oracle_lib.adjoint_tran(t, c.size, 1e-9, 2000, out)
     assert abs(loss[0] - L) <= 1e-12 * abs(L)
     assert np.max(np.abs(grad[0] - gref)) <= 1e-9 * np.max(np.abs(gref))
+
+
+def test_adjoint_single_kernel_form_agrees(monkeypatch):
+    """The forward pass on the double-float engine plus the reverse-only kernel, and the
+    single-kernel form (both passes in the adjoint kernel, used when the circuit does not
+    fit the double-float engine), give the same loss and gradient to double-float rounding."""
+    c = rc_ladder_step(60, seed=11)
+    t = element_table(c)
+    vals = monte_carlo_values(c, 9, seed=4, kinds=(1, 2))
+    g = _lib.GpuCircuit(t, c.size)
+    out = c.index_map["V(n30)"]
+    l_split, g_split = g.adjoint_tran(vals, 1e-9, 400, out, method="tr", checkpoint_every=64)
+    monkeypatch.setenv("KRETS_ADJ_SINGLE", "1")
+    l_one, g_one = g.adjoint_tran(vals, 1e-9, 400, out, method="tr", checkpoint_every=64)
+    assert np.max(np.abs(l_split - l_one) / np.abs(l_one)) < 1e-12
+    assert np.max(np.abs(g_split - g_one)) <= 1e-12 * np.max(np.abs(g_one))
