@@ -1335,9 +1335,12 @@ krets_status krets_batch_tran_probe(krets_circuit *c, int32_t n_inst, const doub
                                     int32_t method, int32_t source_lag, int32_t n_probe, const int32_t *probe,
                                     double *x_out, int32_t *inst_status) {
   if (!c || !probe || n_probe <= 0) return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid probe list");
-  if (!is_device_ptr(probe))
-    for (int j = 0; j < n_probe; ++j)
-      if (probe[j] < 0 || probe[j] >= c->n) return fail(KRETS_ERR_INVALID_ARGUMENT, "probe index out of range");
+  // the kernel indexes shared memory with these: check every index on the host
+  std::vector<int32_t> hp(n_probe);
+  if (is_device_ptr(probe)) CU(cudaMemcpy(hp.data(), probe, sizeof(int32_t) * n_probe, cudaMemcpyDeviceToHost));
+  else memcpy(hp.data(), probe, sizeof(int32_t) * n_probe);
+  for (int32_t v : hp)
+    if (v < 0 || v >= c->n) return fail(KRETS_ERR_INVALID_ARGUMENT, "probe index out of range");
   return batch_tran_impl(c, n_inst, values, h, n_steps, method, source_lag, KRETS_PREC_DF, x_out, inst_status, probe,
                          n_probe);
 }
