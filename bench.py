@@ -213,7 +213,7 @@ def run_reference(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded splitmix64 Monte Carlo values)",
         "config": {"workload": WORKLOAD, "instances": N_INST, "sections": SECTIONS, "h": H, "n_steps": N_STEPS,
-                   "method": "trapezoidal", "parallelism": "host threads"},
+                   "method": "trapezoidal", "seed": shard_seed(0), "parallelism": "host threads"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the Rust reference cannot be built here (no cargo, no crate registry); the C "
@@ -389,7 +389,7 @@ def run_ours(args, rank, world):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64-factor, double-float (2xfp32) solves",
         "data": "synthetic (seeded splitmix64 Monte Carlo values)",
         "config": {"workload": WORKLOAD, "instances": N_INST, "sections": SECTIONS, "unknowns": n, "h": H,
-                   "n_steps": N_STEPS, "method": "trapezoidal",
+                   "n_steps": N_STEPS, "method": "trapezoidal", "seed": shard_seed(rank),
                    "precision": "LU factored in FP64, applied as double-float pairs on FP32 pipes",
                    "l2": "flushed between timed steps (512 MB write); outputs 98.6 GB >> L2",
                    "parallelism": "replicas only (instances sharded per GPU)"},
