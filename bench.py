@@ -160,15 +160,10 @@ def workload(rank=0):
     return c, t, vals
 
 
-def rel_err(x, ref, cur_mask):
-    if not (np.all(np.isfinite(x)) and np.all(np.isfinite(ref))):
-        return float("inf")
-    worst = 0.0
-    for m in (cur_mask, ~cur_mask):
-        r = np.abs(ref[..., m]).max()
-        d = np.abs(x[..., m] - ref[..., m]).max()
-        worst = max(worst, d / r if r > 0 else d)
-    return worst
+def errs_vs_oracle(x, ref, cur_mask):
+    """(norm-wise, element-wise) error against the FP64 oracle (oracle/compare.py)."""
+    from oracle.compare import both
+    return both(x, ref, cur_mask)
 
 
 # ------------------------------------------------------------------ CPU timing (oracle)
@@ -192,7 +187,7 @@ def cpu_rate(t, vals, n, idxs, steps, faithful, threads):
 
 def run_reference(args, rank, world):
     if rank != 0:
-        return
+        return None
     c, t, vals = workload()
     threads = os.cpu_count() or 1
     steps_per_sample = 1000
@@ -219,7 +214,7 @@ def run_reference(args, rank, world):
         "note": "the Rust reference cannot be built here (no cargo, no crate registry); the C "
                 "restatement of its algorithm in oracle/ stands in for it",
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -266,56 +261,66 @@ def run_ours(args, rank, world):
     # accuracy: sampled instances against the FP64 oracle over the full 10000 steps
     from oracle import oracle as O
     mask = is_current_mask(c)
-    sample_idx = [0, N_INST // 2, N_INST - 1]
-    refs = {}
-    for i in sample_idx:
+    sample_idx = sorted(set(np.linspace(0, N_INST - 1, 32).astype(int).tolist()))
+    O.lib()
+
+    def oracle_ref(i):
         ti = t.copy()
         ti["value"] = vals[i]
-        refs[i] = O.tran(ti, n, H, N_STEPS, method="tr", lag=False)
+        return i, O.tran(ti, n, H, N_STEPS, method="tr", lag=False)
+
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        refs = dict(ex.map(oracle_ref, sample_idx))
 
     def sampled_err():
-        worst = 0.0
+        worst = [0.0, 0.0]
         for i in sample_idx:
             host = np.empty((N_STEPS + 1, n))
             off = i * (N_STEPS + 1) * n * 8
             _lib.check(_lib.lib().krets_memcpy_d2h(host.ctypes.data_as(_lib.ctypes.c_void_p),
                                                    _lib.ctypes.c_void_p(d_out.ptr + off), host.nbytes))
-            worst = max(worst, rel_err(host, refs[i], mask))
+            e = errs_vs_oracle(host, refs[i], mask)
+            worst = [max(worst[0], e[0]), max(worst[1], e[1])]
         return worst
 
-    errs = [sampled_err()]
+    errs = sampled_err()
     # the other two precision modes of the same engine, one pass each (not the headline)
     variants = {}
     for name, prec in (("mixed_fp32_lu_df_refinement", _lib.PREC_MIXED), ("fp64", _lib.PREC_FP64)):
         step(prec)
         k, cm = g.timing()
         hist, fallbacks = g.refine_stats()
+        e = sampled_err()
         variants[name] = {"value": ctsteps / (cm / 1e3), "unit": UNIT, "kernel_ms": k,
-                          "max_rel_err_vs_fp64": sampled_err()}
+                          "max_rel_err_vs_fp64": e[0], "max_elementwise_err_vs_fp64": e[1]}
         if prec == _lib.PREC_MIXED:
             variants[name]["refinement_histogram"] = [int(v) for v in hist]
             variants[name]["fp64_fallbacks"] = int(fallbacks)
 
-    # probe-only variant: the same double-float run writing only the output node each step
-    out_node = c.index_map["V(n200)"]
+    # probe-only variant: the same double-float run writing one unknown each step, V(n20),
+    # which the wavefront reaches within the 10 ns window (0.1 ns per section)
+    probe_node = c.index_map["V(n20)"]
     d_probe_out = _lib.DeviceArray((N_INST, N_STEPS + 1, 1))
     probe_ms = []
     for r in range(3):
         g.flush_l2()
-        g.batch_tran_probe(d_vals, H, N_STEPS, [out_node], "tr", lag=False, out=d_probe_out, n_inst=N_INST)
+        g.batch_tran_probe(d_vals, H, N_STEPS, [probe_node], "tr", lag=False, out=d_probe_out, n_inst=N_INST)
         if r > 0:
             probe_ms.append(g.timing())
-    probe_host = np.empty((N_STEPS + 1,))
-    _lib.check(_lib.lib().krets_memcpy_d2h(probe_host.ctypes.data_as(_lib.ctypes.c_void_p),
-                                           _lib.ctypes.c_void_p(d_probe_out.ptr), probe_host.nbytes))
+    probe_err = [0.0, 0.0]
+    for i in sample_idx:
+        probe_host = np.empty((N_STEPS + 1, 1))
+        _lib.check(_lib.lib().krets_memcpy_d2h(probe_host.ctypes.data_as(_lib.ctypes.c_void_p),
+                                               _lib.ctypes.c_void_p(d_probe_out.ptr + i * (N_STEPS + 1) * 8),
+                                               probe_host.nbytes))
+        e = errs_vs_oracle(probe_host, refs[i][:, [probe_node]], np.zeros(1, bool))
+        probe_err = [max(probe_err[0], e[0]), max(probe_err[1], e[1])]
     del d_probe_out
     variants["probe_only_output_node"] = {
         "value": ctsteps / (statistics.mean(cm for _, cm in probe_ms) / 1e3), "unit": UNIT,
-        "kernel_ms": statistics.mean(k for k, _ in probe_ms), "output": "V(n200) only, 8 B per circuit-step",
-        # the front needs ~20 ns to reach n200 (0.1 ns per section), so within 10 ns V(n200)
-        # stays near 1e-300: the error is scaled by the 1 uV voltage tolerance as well
-        "max_rel_err_vs_fp64": float(np.abs(probe_host - refs[0][:, out_node]).max()
-                                     / max(np.abs(refs[0][:, out_node]).max(), 1e-6))}
+        "kernel_ms": statistics.mean(k for k, _ in probe_ms), "output": "V(n20) only, 8 B per circuit-step",
+        "max_rel_err_vs_fp64": probe_err[0], "max_elementwise_err_vs_fp64": probe_err[1],
+        "v_n20_max": float(np.abs(refs[0][:, probe_node]).max())}
 
     # plain GPU form: one instance, FP64, level-scheduled single-CTA kernels per step
     plain_steps = 2000
@@ -329,7 +334,8 @@ def run_ours(args, rank, world):
     # roofline of the dominant kernel (the batched transient)
     alg_bytes = out_bytes - N_INST * n * 8 + vals.nbytes + N_INST * n * 8  # rows 1..N written, inputs read
     # DRAM bytes per circuit-step of k_tran_dfd from an ncu capture of 304 instances x
-    # 1000 steps (profiles/k_tran_dfd_mc_transient_304x1000.md), scaled to this launch
+    # 1000 steps of the same ladder (dram__bytes_read.sum + dram__bytes_write.sum of that
+    # launch divided by its circuit-steps), scaled to this launch
     traffic = TRAFFIC_PER_CIRCUIT_STEP * N_INST * N_STEPS
     k_s = statistics.mean(kern_ms) / 1e3
     peak, peak_kind = measured_peak_hbm()
@@ -382,7 +388,7 @@ def run_ours(args, rank, world):
     del dev_same, dvals
 
     if rank != 0:
-        return
+        return None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": statistics.mean(call_ms), "higher_is_better": True,
@@ -393,7 +399,9 @@ def run_ours(args, rank, world):
                    "precision": "LU factored in FP64, applied as double-float pairs on FP32 pipes",
                    "l2": "flushed between timed steps (512 MB write); outputs 98.6 GB >> L2",
                    "parallelism": "replicas only (instances sharded per GPU)"},
-        "max_rel_err_vs_fp64": max(errs),
+        "max_rel_err_vs_fp64": errs[0],
+        "max_elementwise_err_vs_fp64": errs[1],
+        "accuracy_sample": f"instances {sample_idx} of {N_INST}, all {N_STEPS + 1} rows x {n} unknowns",
         "engine": engine,
         "precision_variants": variants,
         "plain_form": {"value": plain_rate, "unit": UNIT, "what": "1 instance, FP64, per-step kernels (CUDA graph); linear: factored once and reused, "
@@ -413,7 +421,7 @@ def run_ours(args, rank, world):
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # ------------------------------------------------------------------ other workloads
@@ -454,7 +462,7 @@ def _cpu_pool(fn, items, threads):
 def workload_op(args, world, reference):
     from krets_gb300 import _lib
     from krets_gb300.generators import config1_circuit
-    from krets_gb300.table import element_table
+    from krets_gb300.table import element_table, is_current_mask
     from oracle import oracle as O
     c = config1_circuit()
     t = element_table(c)
@@ -480,7 +488,7 @@ def workload_op(args, world, reference):
     launches = _lib.launch_count() - l0
     x, _ = g.op()
     ref = O.op(t, c.size)
-    err = float(np.abs(x - ref).max() / np.abs(ref).max())
+    err = errs_vs_oracle(x, ref, is_current_mask(c))
     reps = 200
     dt = _cpu_pool(lambda _: O.op(t, c.size), range(reps), 1)
     # throughput of independent parameter sets of the same circuit (batched OP, one CTA each)
@@ -492,7 +500,8 @@ def workload_op(args, world, reference):
     k_s = statistics.mean(ks) / 1e3
     peak, pk = measured_peak_hbm()
     return _line(args, world, "OP solves/sec", 1e3 / statistics.mean(ks), "solves/s", wl, {
-        "ms_per_step": statistics.mean(cs), "dtype": "f64", "max_rel_err_vs_fp64": err,
+        "ms_per_step": statistics.mean(cs), "dtype": "f64", "max_rel_err_vs_fp64": err[0],
+        "max_elementwise_err_vs_fp64": err[1],
         "batched_op_1024_parameter_sets": {"value": batched_op, "unit": "solves/s"},
         "roofline": {"bound": "hbm", "achieved": alg / k_s / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": alg / k_s / 1e9 / peak, "traffic": None, "peak_kind": pk, "kernel": "k_op",
@@ -536,17 +545,17 @@ def workload_ac(args, world, reference):
     mask = is_current_mask(c)
     sample = np.arange(0, len(f), 97)
     refz = O.ac(t, c.size, f[sample])
-    err = 0.0
-    for j, i in enumerate(sample):
-        d = np.abs(z[i] - refz[j])
-        r = np.abs(refz[j])
-        err = max(err, d[mask].max() / r[mask].max(), d[~mask].max() / r[~mask].max())
+    err = [0.0, 0.0]
+    for j, i in enumerate(sample):   # per frequency point: each is its own system
+        e = errs_vs_oracle(z[i], refz[j], mask)
+        err = [max(err[0], e[0]), max(err[1], e[1])]
     dt = _cpu_pool(lambda fr: O.ac(t, c.size, fr), [f[:256]], 1)
     alg = len(f) * c.size * 16 + 1000 * 8
     k_s = statistics.mean(ks) / 1e3
     peak, pk = measured_peak_hbm()
     return _line(args, world, "AC points/sec", len(f) / k_s, "points/s", wl, {
-        "ms_per_step": statistics.mean(cs), "dtype": "c64 factor, c128 refinement", "max_rel_err_vs_fp64": err,
+        "ms_per_step": statistics.mean(cs), "dtype": "c64 factor, c128 refinement", "max_rel_err_vs_fp64": err[0],
+        "max_elementwise_err_vs_fp64": err[1], "accuracy_sample": f"every 97th of {len(f)} points",
         "roofline": {"bound": "hbm", "achieved": alg / k_s / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": alg / k_s / 1e9 / peak, "traffic": None, "peak_kind": pk, "kernel": "k_ac_batch<1>",
                      "algorithmic_bytes_per_launch": alg},
@@ -595,21 +604,23 @@ def workload_uneven(args, world, reference):
     info = m.info()
     value = UNEVEN_CIRCUITS * UNEVEN_STEPS / (statistics.mean(ks) / 1e3)
     offs = m.offsets(UNEVEN_STEPS)
-    errs = []
-    for i in (0, 1, 2, 3, 7):
+    # accuracy: small netlists of every size class and the largest ones (n >= 4000, dense
+    # trailing blocks, the global-memory class), every unknown at every step
+    ns = np.array([n for _, n in tabs])
+    acc_idx = [0, 1, 2, 3, 7] + [int(i) for i in np.nonzero(ns >= 4000)[0][:2]] + [int(ns.argmax())]
+
+    def acc_one(i):
         t, n = tabs[i]
         ref = O.tran(t, n, UNEVEN_H, UNEVEN_STEPS, method="be", lag=True)
         x = np.empty((UNEVEN_STEPS + 1) * n)
         _lib.check(_lib.lib().krets_memcpy_d2h(x.ctypes.data_as(_lib.ctypes.c_void_p),
                                                _lib.ctypes.c_void_p(out.ptr + 8 * int(offs[i])), x.nbytes))
-        x = x.reshape(UNEVEN_STEPS + 1, n)
         cur = np.zeros(n, bool)
         cur[t["b"][t["b"] >= 0]] = True
-        e = 0.0
-        for mm in (cur, ~cur):
-            if mm.any():
-                e = max(e, np.abs(x[:, mm] - ref[:, mm]).max() / np.abs(ref[:, mm]).max())
-        errs.append(e)
+        return errs_vs_oracle(x.reshape(UNEVEN_STEPS + 1, n), ref, cur)
+
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        errs = list(ex.map(acc_one, acc_idx))
     # CPU baseline: the same bounded sample as the reference arm, factor once
     idx = list(range(0, UNEVEN_CIRCUITS, 64))
     cdt = _cpu_pool(lambda i: O.tran(tabs[i][0], tabs[i][1], UNEVEN_H, 200, method="be", lag=True), idx, threads)
@@ -634,13 +645,16 @@ def workload_uneven(args, world, reference):
     host.fill(0.0)
     for _ in range(3):
         m2.tran(UNEVEN_STEPS, out=host)
-    e2e = k * UNEVEN_STEPS / (m2.timing()[1] / 1e3)
+    e2e_call_s = m2.timing()[1] / 1e3
+    e2e = k * UNEVEN_STEPS / e2e_call_s
     alg = (int(info[1]) * UNEVEN_STEPS + int(info[1])) * 8
     k_s = statistics.mean(ks) / 1e3
     peak, pk = measured_peak_hbm()
     return _line(args, world, metric, value, "circuit-timesteps/s", wl, {
         "ms_per_step": statistics.mean(cs), "dtype": "f64-factor, double-float (2xfp32) solves",
-        "max_rel_err_vs_fp64": max(errs), "circuits": UNEVEN_CIRCUITS, "sum_unknowns": int(info[1]),
+        "max_rel_err_vs_fp64": max(e[0] for e in errs), "max_elementwise_err_vs_fp64": max(e[1] for e in errs),
+        "accuracy_sample": f"netlists {acc_idx} (n = {[int(ns[i]) for i in acc_idx]}), all steps",
+        "circuits": UNEVEN_CIRCUITS, "sum_unknowns": int(info[1]),
         "sum_lu_entries": int(info[2]), "circuits_per_class": info[4:10].tolist(),
         "class_end_ms": (info[10:16] / 1e3).tolist(), "symbolic_s": create_s,
         "roofline": {"bound": "hbm", "achieved": alg / k_s / 1e9, "peak": peak, "unit": "GB/s",
@@ -649,21 +663,24 @@ def workload_uneven(args, world, reference):
         "cpu_baseline": {"value": len(idx) * 200 / cdt, "unit": "circuit-timesteps/s", "cores": threads,
                          "kind": "port", "sample": f"{len(idx)} netlists (every 64th) x 200 BE steps, factor once"},
         "e2e": {"value": e2e, "unit": "circuit-timesteps/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": int(host.nbytes), "circuits": k},
+                "d2h_bytes_per_step": int(host.nbytes), "circuits": k,
+                "with_symbolic_pass": k * UNEVEN_STEPS / (e2e_call_s + create_s * k / UNEVEN_CIRCUITS),
+                "note": "with_symbolic_pass adds the host symbolic pass and upload (krets_multi_create) "
+                        "of these netlists to the call time"},
         "gpu_launches": int(launches), "clocks": clk.summary()})
 
 
 ADJ_INST, ADJ_SECTIONS, ADJ_STEPS, ADJ_H, ADJ_K = 1024, 1000, 2000, 1e-9, 100
 # DRAM bytes per instance-step of the adjoint (forward k_tran_dfd + reverse k_adjoint_dfd)
-# from an ncu capture of 152 instances x 300 steps (profiles/k_adjoint_dfd_rc1000_152x300.md:
-# 0.56 + 704.66 MB read, 734.83 MB written): the segment states and lambda histories the two
+# from an ncu capture of 152 instances x 300 steps of the same ladder (0.56 + 704.66 MB
+# read, 734.83 MB written): the segment states and lambda histories the two
 # halves of the reverse kernel's CTAs exchange through L2/DRAM
 ADJ_TRAFFIC_PER_INST_STEP = (0.56e6 + 704.66e6 + 734.83e6) / (152 * 300)
 
 
 def workload_adjoint(args, world, reference):
     from krets_gb300 import _lib
-    from krets_gb300.generators import rc_ladder_step
+    from krets_gb300.generators import rc_ladder_step, rc_ladder_step_values
     from krets_gb300.table import element_table
     from oracle import oracle as O
     c = rc_ladder_step(ADJ_SECTIONS)
@@ -672,16 +689,23 @@ def workload_adjoint(args, world, reference):
     wl = f"adjoint_rc_ladder_{ADJ_INST}x{ADJ_SECTIONS}sec_tr_1ns_{ADJ_STEPS}steps_K{ADJ_K}_loss_sum_Vn20_sq"
     threads = os.cpu_count() or 1
     metric = "gradients/sec (loss + d loss / d every R and C)"
+    # seeded values per instance (R log-uniform 100 Ohm-10 kOhm, C log-uniform 1-100 pF)
+    vals = rc_ladder_step_values(c, ADJ_INST, seed=5)
+
+    def table_of(i):
+        ti = t.copy()
+        ti["value"] = vals[i]
+        return ti
+
     if reference:
         O.lib()
         n_s = 2 * threads
-        dt = _cpu_pool(lambda _: O.adjoint_tran(t, c.size, ADJ_H, ADJ_STEPS, out), range(n_s), threads)
+        dt = _cpu_pool(lambda i: O.adjoint_tran(table_of(i), c.size, ADJ_H, ADJ_STEPS, out), range(n_s), threads)
         v = n_s / dt
         return _line(args, world, metric, v, "gradients/s", wl,
                      {"impl": "reference", "dtype": "f64", "cpu_baseline": {"value": v, "unit": "gradients/s",
                       "cores": threads, "kind": "port", "sample": f"{n_s} FP64 adjoint gradients (oracle/)"},
                       "e2e": {"value": v, "unit": "gradients/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
-    vals = np.tile(t["value"], (ADJ_INST, 1))
     g = _lib.GpuCircuit(t, c.size)
     l0 = _lib.launch_count()
     res = {}
@@ -691,49 +715,62 @@ def workload_adjoint(args, world, reference):
                         g.flush_l2, g.timing)
     launches = _lib.launch_count() - l0
     loss, grad = res["r"]
+    # the two forward passes a gradient is compared with: the loss-only forward that the
+    # gradient itself runs (checkpoints, no waveforms), and the transient writing every
+    # waveform (16 GB)
+    lks, _ = _timed(args, lambda: g.adjoint_tran(vals, ADJ_H, ADJ_STEPS, out, checkpoint_every=ADJ_K,
+                                                 gradient=False), g.flush_l2, g.timing)
     fwd = _lib.DeviceArray((ADJ_INST, ADJ_STEPS + 1, c.size))
     fks, _ = _timed(args, lambda: g.batch_tran(vals, ADJ_H, ADJ_STEPS, "tr", lag=False, precision=_lib.PREC_DF,
                                                  out=fwd), g.flush_l2, g.timing)
     del fwd
-    L, gref = O.adjoint_tran(t, c.size, ADJ_H, ADJ_STEPS, out)
-    gerr = float(np.max(np.abs(grad[0] - gref)) / np.max(np.abs(gref)))
-    # central differences (h = 1e-6 relative) of the FP64 oracle loss on the 8 largest R/C
-    # gradients (a source's entry is the derivative with respect to its waveform scale)
-    rc = np.isin(t["kind"], (1, 2, 3))
-    top = np.argsort(-np.where(rc, np.abs(gref), -1.0))[:8]
-    fd = []
-    for e in top:
-        d = 1e-6 * t["value"][e]
-        tp, tm = t.copy(), t.copy()
-        tp["value"][e] += d
-        tm["value"][e] -= d
-        fd.append((np.sum(O.tran(tp, c.size, ADJ_H, ADJ_STEPS, method="tr", lag=False)[1:, out] ** 2)
-                   - np.sum(O.tran(tm, c.size, ADJ_H, ADJ_STEPS, method="tr", lag=False)[1:, out] ** 2)) / (2 * d))
-    fd = np.array(fd)
+    # accuracy: loss and gradient of sampled instances against the FP64 CPU adjoint
+    samp = [0, ADJ_INST // 2, ADJ_INST - 1]
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        refs = list(ex.map(lambda i: O.adjoint_tran(table_of(i), c.size, ADJ_H, ADJ_STEPS, out), samp))
+    gerr = max(float(np.max(np.abs(grad[i] - gr)) / np.max(np.abs(gr))) for i, (_, gr) in zip(samp, refs))
+    lerr = max(abs(loss[i] - L) / L for i, (L, _) in zip(samp, refs))
+    gref = refs[0][1]
+    t0v = table_of(0)
+
+    # central differences of the FP64 oracle loss on instance 0's 8 largest R/C gradients
+    def fd_at(rel):
+        rc = np.isin(t["kind"], (1, 2, 3))
+        top = np.argsort(-np.where(rc, np.abs(gref), -1.0))[:8]
+
+        def one(e):
+            d = rel * t0v["value"][e]
+            tp, tm = t0v.copy(), t0v.copy()
+            tp["value"][e] += d
+            tm["value"][e] -= d
+            return (np.sum(O.tran(tp, c.size, ADJ_H, ADJ_STEPS, method="tr", lag=False)[1:, out] ** 2)
+                    - np.sum(O.tran(tm, c.size, ADJ_H, ADJ_STEPS, method="tr", lag=False)[1:, out] ** 2)) / (2 * d)
+
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            fd = np.array(list(ex.map(one, top)))
+        return top, fd
+
+    top, fd = fd_at(1e-6)
     fd_err = float(np.max(np.abs(grad[0][top] - fd) / np.abs(fd)))
     fd_floor = float(np.max(np.abs(gref[top] - fd) / np.abs(fd)))  # FP64 adjoint vs the same differences
     # at h = 1e-6 the FP64 loss differences are rounding limited (~1e-6 relative); at
     # h = 1e-4 they are accurate to ~1e-9, so the gradient's own error shows
-    fd4 = []
-    for e in top:
-        d = 1e-4 * t["value"][e]
-        tp, tm = t.copy(), t.copy()
-        tp["value"][e] += d
-        tm["value"][e] -= d
-        fd4.append((np.sum(O.tran(tp, c.size, ADJ_H, ADJ_STEPS, method="tr", lag=False)[1:, out] ** 2)
-                    - np.sum(O.tran(tm, c.size, ADJ_H, ADJ_STEPS, method="tr", lag=False)[1:, out] ** 2)) / (2 * d))
-    fd4 = np.array(fd4)
-    fd4_err = float(np.max(np.abs(grad[0][top] - fd4) / np.abs(fd4)))
+    top4, fd4 = fd_at(1e-4)
+    fd4_err = float(np.max(np.abs(grad[0][top4] - fd4) / np.abs(fd4)))
     n_s = 2 * threads
-    cdt = _cpu_pool(lambda _: O.adjoint_tran(t, c.size, ADJ_H, ADJ_STEPS, out), range(n_s), threads)
+    cdt = _cpu_pool(lambda i: O.adjoint_tran(table_of(i), c.size, ADJ_H, ADJ_STEPS, out), range(n_s), threads)
     k_s = statistics.mean(ks) / 1e3
     J = (ADJ_STEPS + ADJ_K - 1) // ADJ_K
     alg = ADJ_INST * (2 * c.elements.__len__() * 8 + 2 * J * c.size * 8)
     peak, pk = measured_peak_hbm()
     return _line(args, world, metric, ADJ_INST / k_s, "gradients/s", wl, {
         "ms_per_step": statistics.mean(cs), "dtype": "f64-factor, double-float (2xfp32) solves",
-        "forward_ms": statistics.mean(fks), "gradient_over_forward": statistics.mean(ks) / statistics.mean(fks),
-        "loss_rel_err_vs_fp64_adjoint": abs(loss[0] - L) / L, "grad_rel_err_vs_fp64_adjoint": gerr,
+        "config_values": "seeded per instance (R log-U 100 Ohm-10 kOhm, C log-U 1-100 pF)",
+        "loss_only_forward_ms": statistics.mean(lks), "waveform_forward_ms": statistics.mean(fks),
+        "gradient_over_loss_only_forward": statistics.mean(ks) / statistics.mean(lks),
+        "gradient_over_waveform_forward": statistics.mean(ks) / statistics.mean(fks),
+        "loss_rel_err_vs_fp64_adjoint": lerr, "grad_rel_err_vs_fp64_adjoint": gerr,
+        "accuracy_sample": f"instances {samp} against the FP64 CPU adjoint",
         "grad_rel_err_vs_central_fd_1e-6": fd_err, "fp64_adjoint_rel_err_vs_central_fd_1e-6": fd_floor,
         "grad_rel_err_vs_central_fd_1e-4": fd4_err,
         "roofline": {"bound": "hbm", "achieved": alg / k_s / 1e9, "peak": peak, "unit": "GB/s",
@@ -750,6 +787,43 @@ def workload_adjoint(args, world, reference):
 
 
 WORKLOADS = {"op": workload_op, "ac": workload_ac, "uneven": workload_uneven, "adjoint": workload_adjoint}
+CONFIG_NAMES = {"op": "config 1: plain OP", "ac": "config 2: batched AC sweep", "uneven": "config 4: uneven batch",
+                "adjoint": "config 5: adjoint sensitivity"}
+
+
+def compact(line):
+    """The fields of another configuration's line that the headline line carries."""
+    keep = ("metric", "value", "unit", "impl", "ms_per_step", "max_rel_err_vs_fp64", "max_elementwise_err_vs_fp64",
+            "accuracy_sample", "gradient_over_loss_only_forward", "gradient_over_waveform_forward",
+            "loss_only_forward_ms", "waveform_forward_ms", "grad_rel_err_vs_fp64_adjoint",
+            "grad_rel_err_vs_central_fd_1e-6", "grad_rel_err_vs_central_fd_1e-4", "symbolic_s", "class_end_ms",
+            "batched_op_1024_parameter_sets", "gpu_launches", "clocks")
+    c = {k: line[k] for k in keep if k in line}
+    c["workload"] = line["config"]["workload"]
+    if "roofline" in line:
+        r = line["roofline"]
+        c["roofline"] = {k: r.get(k) for k in ("kernel", "achieved", "peak", "frac", "traffic")}
+    for k in ("e2e", "cpu_baseline"):
+        if k in line:
+            c[k] = line[k]
+    return c
+
+
+def other_configs(args, world, reference):
+    """Configurations 1, 2, 4 and 5 at --steps 2 each (same timing rules), compacted."""
+    a = argparse.Namespace(**vars(args))
+    a.steps = 2
+    out = {}
+    for name, fn in WORKLOADS.items():
+        t0 = time.perf_counter()
+        try:
+            c = compact(fn(a, world, reference))
+        except Exception as e:  # a failing configuration is reported, not hidden
+            c = {"error": f"{type(e).__name__}: {e}"}
+        c["what"] = CONFIG_NAMES[name]
+        c["wall_s"] = time.perf_counter() - t0
+        out[name] = c
+    return out
 
 
 def main():
@@ -759,6 +833,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="mc_transient", choices=["mc_transient"] + sorted(WORKLOADS))
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the other configurations' compact lines (other_configs)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if world > 1:
@@ -773,9 +849,14 @@ def main():
             print(json.dumps(line), flush=True)
         return
     if args.impl == "reference":
-        run_reference(args, rank, world)
+        line = run_reference(args, rank, world)
     else:
-        run_ours(args, rank, world)
+        line = run_ours(args, rank, world)
+    if rank == 0 and line is not None:
+        # the other configurations of the solve path, on one GPU (single-GPU runs only)
+        if world == 1 and not args.headline_only:
+            line["other_configs"] = other_configs(args, world, args.impl == "reference")
+        print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

@@ -290,13 +290,26 @@ krets_status krets_device_synchronize(void);
  *
  *  - values (may be NULL: nominal values), x_out and inst_status must be device pointers
  *    (same shapes as krets_batch_tran).
+ *  - precision is KRETS_PREC_FP64, KRETS_PREC_MIXED or KRETS_PREC_DF (anything else is
+ *    KRETS_ERR_INVALID_ARGUMENT).  For each, the call picks the same engine, kernels,
+ *    refinement tolerance and launch shape as krets_batch_tran, so with the same inputs
+ *    the two return identical results.  For KRETS_PREC_DF it uses the group size that the
+ *    autotuner of an earlier krets_batch_tran call cached for this circuit (else 128); it
+ *    never runs the autotuner itself.
  *  - The circuit must already hold the compiled programs for (method, h): call
  *    krets_batch_tran once with the same time step and method during set-up.  Otherwise
  *    the call fails with KRETS_ERR_INVALID_ARGUMENT.
+ *  - Only circuits that run entirely in shared memory are accepted: the operating-point
+ *    workspace must fit in one CTA's shared memory, and so must the transient engine's
+ *    (the double-float engine's layout for KRETS_PREC_DF, else the warp engine's).
+ *    krets_batch_tran runs larger circuits with global-memory workspaces that it
+ *    allocates; here they are rejected with KRETS_ERR_INVALID_ARGUMENT.
  *  - Its scratch is a fixed 16 MiB device array inside the library, present on every GPU
  *    that loads the library until the process exits.  Requests that do not fit (too many
- *    instances, or one instance's FP64 fallback factors too large) are rejected with
- *    KRETS_ERR_INVALID_ARGUMENT; a smaller array only limits the number of concurrent CTAs.
+ *    instances, a KRETS_PREC_DF waveform table of n_steps + 1 values per PULSE / SIN
+ *    source that is too long, or one CTA's FP64 fallback factors too large) are rejected
+ *    with KRETS_ERR_INVALID_ARGUMENT; otherwise a smaller array only limits the number of
+ *    concurrent CTAs.
  *  - The first call on a device looks up that array's device address (once per device);
  *    make that first call before any stream capture.
  *  - Every call shares the array and clears what must start at zero on entry; calls that

@@ -488,21 +488,23 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[KRETS_NOALLOC_S
 
 namespace {
 
-// Device address of g_noalloc_scratch per device, looked up once per device (the host-side
-// name of the array is only a stand-in, never a device address).
+// Device address of g_noalloc_scratch per device, looked up once per device with that
+// device current (the host-side name of the array is only a stand-in, never a device
+// address).  Atomic slots: two host threads making their first call on one device at the
+// same time may both look it up, and both store the same address.
 constexpr int kMaxDevices = 64;
-void *g_noalloc_addr[kMaxDevices] = {};
+std::atomic<void *> g_noalloc_addr[kMaxDevices];
 
 krets_status noalloc_scratch_address(void **out) {
   int dev = 0;
   CU(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(KRETS_ERR_CUDA, "device index out of range");
-  if (!g_noalloc_addr[dev]) {
-    void *p = nullptr;
+  void *p = g_noalloc_addr[dev].load(std::memory_order_acquire);
+  if (!p) {
     CU(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_noalloc_addr[dev] = p;
+    g_noalloc_addr[dev].store(p, std::memory_order_release);
   }
-  *out = g_noalloc_addr[dev];
+  *out = p;
   return KRETS_OK;
 }
 
@@ -516,15 +518,18 @@ DevProgram *find_program(krets_circuit *c, int mode, int method, double h, doubl
 }
 
 // OR of the operating-point and transient statuses, folded into the caller's per-instance
-// status array, plus one summary word.
-__global__ void k_status_fold(const int *op_status, int *inst_status, int n, int *any) {
-  int acc = 0;
+// status array, plus one summary word for each (the operating point's failures map to
+// the operating-point error codes, as in krets_batch_tran).
+__global__ void k_status_fold(const int *op_status, int *inst_status, int n, int *any_op, int *any_tran) {
+  int acc_op = 0, acc_tr = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int v = op_status[i] | inst_status[i];
-    inst_status[i] = v;
-    acc |= v;
+    const int o = op_status[i], t = inst_status[i];
+    inst_status[i] = o | t;
+    acc_op |= o;
+    acc_tr |= t;
   }
-  if (acc) atomicOr(any, acc);
+  if (acc_op) atomicOr(any_op, acc_op);
+  if (acc_tr) atomicOr(any_tran, acc_tr);
 }
 
 }  // namespace
@@ -1115,6 +1120,70 @@ krets_status dfd_pick_group(krets_circuit *c, const DevProgram *D, const DfdLay 
   return KRETS_OK;
 }
 
+// Group size of the double-float engine without a trial run: KRETS_GROUP, else the
+// autotuner's cached choice for this sparsity signature, else the default 128.
+int dfd_cached_group(const DevProgram *D, int method, int &how) {
+  const char *genv = getenv("KRETS_GROUP");
+  how = 0;
+  if (genv) {
+    const int G = atoi(genv);
+    return (G == 32 || G == 64 || G == 128) ? G : 128;
+  }
+  char key[96];
+  snprintf(key, sizeof key, "%016llx/%d/%zu/%d", (unsigned long long)D->host.signature, D->host.n,
+           D->host.lu_col.size(), method);
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(key);
+  if (it == g_tune.end()) return 128;
+  how = 2;
+  return it->second;
+}
+
+// Shared-memory layout of one warp of the warp engine (k_tran_warp, k_tran_warp_df);
+// returns the bytes per warp.
+size_t warp_layout(const DevProg &P, bool mixed, WarpLay &WL) {
+  size_t cur = 0;
+  auto put = [&](int &off, size_t bytes) { off = (int)cur; cur = align16(cur + bytes); };
+  put(WL.lu, (mixed ? 4 : 8) * (size_t)P.nnz_lu);
+  put(WL.coef, 8 * (size_t)P.ne);
+  put(WL.x, 8 * (size_t)P.n);
+  put(WL.b, 8 * (size_t)P.n);
+  put(WL.w, mixed ? 4 * (size_t)P.n : 16);
+  put(WL.cb, 8 * (size_t)P.ndyn);
+  put(WL.icap, 8 * (size_t)P.ncap);
+  put(WL.prev, P.nonlinear ? 8 * (size_t)P.n : 0);
+  put(WL.guess, P.nonlinear ? 8 * (size_t)P.n : 0);
+  WL.bytes = (int)align16(cur);
+  WL.sprog_bytes = (int)align16((size_t)P.sp_off[11] * sizeof(int));
+  return (size_t)WL.bytes;
+}
+
+// Warps per CTA of the warp engine (KRETS_SMEM_BUDGET and KRETS_WARPS_PER_CTA override).
+int warp_engine_width(const WarpLay &WL, size_t per_warp) {
+  const char *bud = getenv("KRETS_SMEM_BUDGET");
+  size_t budget = bud ? (size_t)atol(bud) : max_smem_optin();
+  budget = std::min(budget, max_smem_optin());
+  int W = (int)std::max<size_t>(1, std::min<size_t>(8, (budget - WL.sprog_bytes) / per_warp));
+  const char *wenv = getenv("KRETS_WARPS_PER_CTA");
+  if (wenv) W = std::max(1, std::min(8, atoi(wenv)));
+  while (W > 1 && WL.sprog_bytes + (size_t)W * per_warp > max_smem_optin()) --W;
+  return W;
+}
+
+// PULSE / SIN sources of a transient program that the double-float engine tabulates per
+// step: wrow[d] = table row of rhs element d (or -1), wsrc = their element indices.
+void wave_sources(const krets_circuit *c, const Program &H, int ndyn, std::vector<int> &wrow, std::vector<int> &wsrc) {
+  wrow.assign(ndyn, -1);
+  wsrc.clear();
+  for (int d = 0; d < ndyn; ++d) {
+    const krets_element &E = c->el[H.dyn_e[d]];
+    if (E.kind == KRETS_ELEM_V && E.wave != KRETS_WAVE_NONE) {
+      wrow[d] = (int)wsrc.size();
+      wsrc.push_back(H.dyn_e[d]);
+    }
+  }
+}
+
 }  // namespace
 
 // Batched transient; with probes (n_probe > 0) only those unknowns are written each step
@@ -1166,20 +1235,7 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
   WarpLay WL{};
   size_t per_warp = 0;
   if (warp_engine) {
-    size_t cur = 0;
-    auto put = [&](int &off, size_t bytes) { off = (int)cur; cur = align16(cur + bytes); };
-    put(WL.lu, (mixed ? 4 : 8) * (size_t)P.nnz_lu);
-    put(WL.coef, 8 * (size_t)P.ne);
-    put(WL.x, 8 * (size_t)P.n);
-    put(WL.b, 8 * (size_t)P.n);
-    put(WL.w, mixed ? 4 * (size_t)P.n : 16);  // double-float direct: the group's 4 status words
-    put(WL.cb, 8 * (size_t)P.ndyn);
-    put(WL.icap, 8 * (size_t)P.ncap);
-    put(WL.prev, P.nonlinear ? 8 * (size_t)P.n : 0);
-    put(WL.guess, P.nonlinear ? 8 * (size_t)P.n : 0);
-    WL.bytes = (int)align16(cur);
-    WL.sprog_bytes = (int)align16((size_t)P.sp_off[11] * sizeof(int));
-    per_warp = WL.bytes;
+    per_warp = warp_layout(P, mixed, WL);
     if (!P.sprog_ok || per_warp + WL.sprog_bytes > max_smem_optin()) warp_engine = false;
   }
   double *fb = nullptr;
@@ -1194,15 +1250,8 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
                 "probe outputs need the double-float engine (precision 2, a linear circuit that fits)");
   if (use_dfd) {
     // PULSE / SIN sources tabulated per step (their parameters are not per-instance values)
-    const Program &H = Dtr->host;
-    std::vector<int> wrow(P.ndyn, -1), wsrc;
-    for (int d = 0; d < P.ndyn; ++d) {
-      const krets_element &E = c->el[H.dyn_e[d]];
-      if (E.kind == KRETS_ELEM_V && E.wave != KRETS_WAVE_NONE) {
-        wrow[d] = (int)wsrc.size();
-        wsrc.push_back(H.dyn_e[d]);
-      }
-    }
+    std::vector<int> wrow, wsrc;
+    wave_sources(c, Dtr->host, P.ndyn, wrow, wsrc);
     WaveTab wt{nullptr, nullptr, n_steps + 1};
     if (!wsrc.empty()) {
       const size_t tab_bytes = sizeof(double) * wsrc.size() * (size_t)(n_steps + 1);
@@ -1246,13 +1295,7 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
                                                source_lag, (double *)dx, d_st, queue, opts, wt, pr,
                                                AdjFwd{nullptr, 1, 0, 0, nullptr});
   } else if (warp_engine) {
-    const char *bud = getenv("KRETS_SMEM_BUDGET");
-    size_t budget = bud ? (size_t)atol(bud) : max_smem_optin();
-    budget = std::min(budget, max_smem_optin());
-    int W = (int)std::max<size_t>(1, std::min<size_t>(8, (budget - WL.sprog_bytes) / per_warp));
-    const char *wenv = getenv("KRETS_WARPS_PER_CTA");
-    if (wenv) W = std::max(1, std::min(8, atoi(wenv)));
-    while (W > 1 && WL.sprog_bytes + (size_t)W * per_warp > max_smem_optin()) --W;
+    const int W = warp_engine_width(WL, per_warp);
     size_t smem = WL.sprog_bytes + (size_t)W * per_warp;
     auto kern = mixed ? k_tran_warp<1> : k_tran_warp<0>;
     // linear circuits in mixed precision take the double-float variant (FP32 pipes)
@@ -1624,13 +1667,18 @@ krets_status krets_device_synchronize(void) {
 }
 
 // Batched transient for callers that must not allocate device memory (see krets_gpu.h).
-// Same kernels and results as krets_batch_tran with device-resident buffers; the scratch
-// that call would allocate comes from g_noalloc_scratch.
+// For each precision it makes the same engine choice, with the same kernels, group size,
+// tolerances and launch parameters, as krets_batch_tran with device-resident buffers, so
+// the results are identical; what that call would allocate (status words, the work-queue
+// counter, the source-waveform table, FP64 fallback factors) comes from g_noalloc_scratch.
+// Circuits that krets_batch_tran runs with global-memory workspaces are rejected.
 krets_status krets_batch_tran_noalloc(krets_circuit *c, int32_t n_inst, const double *d_values, double h,
                                       int32_t n_steps, int32_t method, int32_t source_lag, int32_t precision,
                                       double *d_x_out, int32_t *d_inst_status) {
   if (!c || n_inst <= 0 || n_steps < 0 || !(h > 0) || !d_x_out || !d_inst_status)
     return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments to krets_batch_tran_noalloc");
+  if (precision != KRETS_PREC_FP64 && precision != KRETS_PREC_MIXED && precision != KRETS_PREC_DF)
+    return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc: unknown precision");
   if ((d_values && !is_device_ptr(d_values)) || !is_device_ptr(d_x_out) || !is_device_ptr(d_inst_status))
     return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc needs device pointers for values, "
                                             "x_out and inst_status");
@@ -1640,95 +1688,143 @@ krets_status krets_batch_tran_noalloc(krets_circuit *c, int32_t n_inst, const do
     return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc: the circuit has no compiled program for this "
                                             "time step and method; run krets_batch_tran once with them first");
   const DevProg &P = Dtr->view;
-  const bool mixed = precision == KRETS_PREC_MIXED;
   // operating point: its per-CTA workspace must fit in shared memory (no global workspace)
-  Lay Lop = layout_op(Ddc->view);
-  if (Lop.bytes > max_smem_optin())
+  if (layout_op(Ddc->view).bytes > max_smem_optin())
     return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc: circuit too large for the shared-memory "
                                             "operating-point kernel");
-  // warp engine layout (identical to krets_batch_tran's)
+  // engine choice, as in batch_tran_impl
+  const bool dfd = precision == KRETS_PREC_DF;
+  bool mixed = precision == KRETS_PREC_MIXED;
+  if (dfd && P.nonlinear) mixed = true;
+  const char *eng = getenv("KRETS_ENGINE");
+  const bool block_forced = eng && strcmp(eng, "block") == 0;
+  DfdLay DL{};
+  const bool use_dfd = dfd && !P.nonlinear && P.sprog_ok && !block_forced && dfd_layout(P, DL);
   WarpLay WL{};
-  size_t cur = 0;
-  auto put = [&](int &off, size_t bytes) { off = (int)cur; cur = align16(cur + bytes); };
-  put(WL.lu, (mixed ? 4 : 8) * (size_t)P.nnz_lu);
-  put(WL.coef, 8 * (size_t)P.ne);
-  put(WL.x, 8 * (size_t)P.n);
-  put(WL.b, 8 * (size_t)P.n);
-  put(WL.w, mixed ? 4 * (size_t)P.n : 0);
-  put(WL.cb, 8 * (size_t)P.ndyn);
-  put(WL.icap, 8 * (size_t)P.ncap);
-  put(WL.prev, P.nonlinear ? 8 * (size_t)P.n : 0);
-  put(WL.guess, P.nonlinear ? 8 * (size_t)P.n : 0);
-  WL.bytes = (int)align16(cur);
-  WL.sprog_bytes = (int)align16((size_t)P.sp_off[11] * sizeof(int));
-  const size_t per_warp = WL.bytes;
-  if (!P.sprog_ok || per_warp + WL.sprog_bytes > max_smem_optin())
-    return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc: circuit too large for the warp engine");
-  int W = (int)std::max<size_t>(1, std::min<size_t>(8, (max_smem_optin() - WL.sprog_bytes) / per_warp));
-  const size_t smem = WL.sprog_bytes + (size_t)W * per_warp;
-  auto kern = mixed ? k_tran_warp<1> : k_tran_warp<0>;
-  CU(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 0;
-  CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * W, smem));
-  if (per_sm < 1) return fail(KRETS_ERR_CUDA, "warp engine does not fit on an SM");
-  int grid = std::max(1, std::min((n_inst + W - 1) / W, per_sm * device_sm_count()));
-  // scratch layout: [0,64) counters, [64,128) histogram, [256, 256+4n) OP status, then the
-  // FP64 fallback factors of every warp slot (mixed precision)
+  const size_t per_warp = warp_layout(P, mixed, WL);
+  const bool warp_engine = !use_dfd && !block_forced && P.sprog_ok && per_warp + WL.sprog_bytes <= max_smem_optin();
+  if (!use_dfd && !warp_engine)
+    return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc: circuit too large for the shared-memory "
+                                            "transient engines");
+  const char *dfenv = getenv("KRETS_DF");
+  const bool use_df = warp_engine && mixed && !P.nonlinear && !(dfenv && dfenv[0] == '0');
+  const bool need_fb = warp_engine && mixed && !use_df;  // k_tran_warp<1>: FP64 fallback factors
+  // scratch layout: [0,64) counters and summary words, [64,128) refinement histogram,
+  // [256, ..) operating-point status per instance, then the waveform table (double-float
+  // engine with PULSE / SIN sources), then the FP64 fallback factors of every warp slot
+  std::vector<int> wrow, wsrc;
+  if (use_dfd) wave_sources(c, Dtr->host, P.ndyn, wrow, wsrc);
   const size_t op_off = 256;
-  const size_t lu_off = align16(op_off + sizeof(int) * (size_t)n_inst);
-  const size_t lu_slot = sizeof(double) * (size_t)P.nnz_lu;
+  const size_t tab_off = align16(op_off + sizeof(int) * (size_t)n_inst);
+  const size_t tab_bytes = wsrc.empty() ? 0 : sizeof(double) * wsrc.size() * ((size_t)n_steps + 1);
+  const size_t wrow_off = tab_off + tab_bytes;
+  const size_t wsrc_off = wrow_off + sizeof(int) * wrow.size();
+  const size_t lu_off = align16(wsrc.empty() ? tab_off : wsrc_off + sizeof(int) * wsrc.size());
   if (lu_off > KRETS_NOALLOC_SCRATCH_BYTES)
-    return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc: too many instances for the 16 MiB scratch");
-  if (mixed) {
-    const size_t slots = (KRETS_NOALLOC_SCRATCH_BYTES - lu_off) / lu_slot;
-    if (slots < (size_t)W)
-      return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc: instance size exceeds the 16 MiB scratch");
-    grid = std::min(grid, (int)(slots / W));
-  }
+    return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc: instances x steps exceed the 16 MiB scratch");
   void *scr = nullptr;
   krets_status s = noalloc_scratch_address(&scr);
   if (s) return s;
   char *base = (char *)scr;
   int *queue = (int *)(base + 0);
   int *fallbacks = (int *)(base + 4);
-  int *any = (int *)(base + 8);
+  int *any_op = (int *)(base + 8);
+  int *any_tran = (int *)(base + 12);
   unsigned long long *hist = (unsigned long long *)(base + 64);
   int *op_status = (int *)(base + op_off);
-  double *fb = mixed ? (double *)(base + lu_off) : nullptr;
   CU(cudaEventRecord(c->ev[0], c->stream));
-  // everything that must start at zero: counters, histogram, statuses
+  // everything that must start at zero: counters, summary words, histogram, statuses
   CU(cudaMemsetAsync(base, 0, 256, c->stream));
   CU(cudaMemsetAsync(op_status, 0, sizeof(int) * (size_t)n_inst, c->stream));
   CU(cudaMemsetAsync(d_inst_status, 0, sizeof(int) * (size_t)n_inst, c->stream));
   const size_t stride = (size_t)c->n * ((size_t)n_steps + 1);
-  int op_grid;
-  size_t op_smem;
-  char *op_gws;
-  s = plan_launch(c, k_op, Lop, 128, n_inst, op_grid, op_smem, op_gws);
+  // the operating-point workspace fits in shared memory, so run_op allocates nothing
+  s = run_op(c, Ddc, n_inst, d_values, d_x_out, stride, op_status, nullptr, 128);
   if (s) return s;
-  k_op<<<op_grid, 128, op_smem, c->stream>>>(Ddc->view, c->cfg, Lop, nullptr, d_values, d_x_out, stride, op_status,
-                                             nullptr, n_inst, OpWarm{});
-  g_launches++;
-  CU(cudaGetLastError());
-  const char *tenv = getenv("KRETS_REFINE_TOL");
-  const double tol = tenv ? atof(tenv) : 1e-10;
-  CU(cudaEventRecord(c->ev[2], c->stream));
-  kern<<<grid, 32 * W, smem, c->stream>>>(P, c->cfg, WL, d_values, n_inst, h, n_steps, method, source_lag, d_x_out,
-                                         d_inst_status, queue, hist, fallbacks, fb, tol);
+  if (use_dfd) {
+    WaveTab wt{nullptr, nullptr, n_steps + 1};
+    if (!wsrc.empty()) {
+      int *d_wrow = (int *)(base + wrow_off), *d_wsrc = (int *)(base + wsrc_off);
+      CU(cudaMemcpyAsync(d_wrow, wrow.data(), sizeof(int) * wrow.size(), cudaMemcpyHostToDevice, c->stream));
+      CU(cudaMemcpyAsync(d_wsrc, wsrc.data(), sizeof(int) * wsrc.size(), cudaMemcpyHostToDevice, c->stream));
+      k_wave_table<<<256, 256, 0, c->stream>>>(c->d_el, d_wsrc, (int)wsrc.size(), h, n_steps, source_lag,
+                                              (double *)(base + tab_off));
+      g_launches++;
+      CU(cudaGetLastError());
+      wt.tab = (const double *)(base + tab_off);
+      wt.row = d_wrow;
+    }
+    const char *oenv = getenv("KRETS_DFD_OPTS");
+    const int opts = oenv ? atoi(oenv) : 0;
+    int how = 0;
+    const int G = dfd_cached_group(Dtr, method, how);  // never a trial run: it would allocate
+    DfdLaunch Lc;
+    s = dfd_config(G, DL, Lc);
+    if (s != KRETS_OK) return s;
+    const int grid = std::max(1, std::min((n_inst + Lc.W - 1) / Lc.W, Lc.per_sm * device_sm_count()));
+    c->warps_per_cta = Lc.W * G / 32;
+    c->grid = grid;
+    c->launch_info[0] = G;
+    c->launch_info[1] = Lc.W;
+    c->launch_info[2] = grid;
+    c->launch_info[3] = how;
+    CU(cudaEventRecord(c->ev[2], c->stream));
+    Lc.kd<<<grid, G * Lc.W, Lc.smem, c->stream>>>(P, c->cfg, DL, d_values, n_inst, h, n_steps, method, source_lag,
+                                                  d_x_out, d_inst_status, queue, opts, wt, Probe{nullptr, 0, nullptr},
+                                                  AdjFwd{nullptr, 1, 0, 0, nullptr});
+  } else {
+    const int W = warp_engine_width(WL, per_warp);
+    const size_t smem = WL.sprog_bytes + (size_t)W * per_warp;
+    auto kern = mixed ? k_tran_warp<1> : k_tran_warp<0>;
+    int per_sm = 0;
+    if (use_df) {
+      CU(cudaFuncSetAttribute(k_tran_warp_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tran_warp_df, 32 * W, smem));
+    } else {
+      CU(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * W, smem));
+    }
+    if (per_sm < 1) return fail(KRETS_ERR_CUDA, "warp engine does not fit on an SM");
+    int grid = std::max(1, std::min((n_inst + W - 1) / W, per_sm * device_sm_count()));
+    double *fb = nullptr;
+    if (need_fb) {
+      // one factor slot per warp of the grid; fewer slots only mean fewer resident CTAs
+      // (each instance's arithmetic does not depend on the grid)
+      const size_t lu_slot = sizeof(double) * (size_t)P.nnz_lu;
+      const size_t slots = lu_off < KRETS_NOALLOC_SCRATCH_BYTES ? (KRETS_NOALLOC_SCRATCH_BYTES - lu_off) / lu_slot : 0;
+      if (slots < (size_t)W)
+        return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc: one CTA's FP64 fallback factors exceed "
+                                                "the 16 MiB scratch");
+      grid = std::min(grid, (int)(slots / W));
+      fb = (double *)(base + lu_off);
+    }
+    const char *tenv = getenv("KRETS_REFINE_TOL");
+    const double tol = tenv ? atof(tenv) : 1e-8;
+    c->warps_per_cta = W;
+    c->grid = grid;
+    CU(cudaEventRecord(c->ev[2], c->stream));
+    if (use_df)
+      k_tran_warp_df<<<grid, 32 * W, smem, c->stream>>>(P, c->cfg, WL, d_values, n_inst, h, n_steps, method,
+                                                       source_lag, d_x_out, d_inst_status, queue, hist, (float)tol);
+    else
+      kern<<<grid, 32 * W, smem, c->stream>>>(P, c->cfg, WL, d_values, n_inst, h, n_steps, method, source_lag, d_x_out,
+                                             d_inst_status, queue, hist, fallbacks, fb, tol);
+  }
   g_launches++;
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[3], c->stream));
   k_status_fold<<<std::max(1, std::min(1024, (n_inst + 255) / 256)), 256, 0, c->stream>>>(op_status, d_inst_status,
-                                                                                         n_inst, any);
+                                                                                         n_inst, any_op, any_tran);
   g_launches++;
   CU(cudaGetLastError());
-  int any_h = 0;
-  CU(cudaMemcpyAsync(&any_h, any, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  int any_h[2] = {0, 0};
+  CU(cudaMemcpyAsync(any_h, any_op, sizeof any_h, cudaMemcpyDeviceToHost, c->stream));
   CU(cudaEventRecord(c->ev[1], c->stream));
   CU(cudaStreamSynchronize(c->stream));
   cudaEventElapsedTime(&c->kernel_ms, c->ev[2], c->ev[3]);
   cudaEventElapsedTime(&c->call_ms, c->ev[0], c->ev[1]);
-  return map_status(any_h, 1);
+  if (any_h[0]) return map_status(any_h[0], 0);
+  return map_status(any_h[1], 1);
 }
 
 // ------------------------------------------------------------------ multi-circuit

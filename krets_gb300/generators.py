@@ -129,6 +129,21 @@ def rc_ladder_step(sections: int = 1000, seed: int = 5) -> Circuit:
     return parse_circuit_description("\n".join(lines) + "\n")
 
 
+def rc_ladder_step_values(circuit: Circuit, n_inst: int, seed: int = 5) -> np.ndarray:
+    """[n_inst][n_elem] values of the adjoint workload's RC ladder, drawn per instance: R
+    log-uniform 100 Ohm-10 kOhm, C log-uniform 1 pF-100 pF (instance i from seed
+    seed + 7919 i, so instance 0 has the values of rc_ladder_step(seed=seed))."""
+    t = element_table(circuit)
+    r_pos = np.nonzero(t["kind"] == 1)[0]
+    c_pos = np.nonzero(t["kind"] == 2)[0]
+    vals = np.tile(t["value"].astype(np.float64), (n_inst, 1))
+    for i in range(n_inst):
+        s = seed + 7919 * i
+        vals[i, r_pos] = log_uniform(s, len(r_pos), 100.0, 1e4)
+        vals[i, c_pos] = log_uniform(s + 1000003, len(c_pos), 1e-12, 1e-10)
+    return vals
+
+
 # ---------------------------------------------------------------- uneven batch
 UNEVEN_NODES = (10, 5000)
 

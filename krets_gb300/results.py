@@ -1,5 +1,6 @@
 """Parquet result files with the reference's column layout
-(crates/krets-result/src/lib.rs:20-208), written with pyarrow.
+(crates/krets-result/src/lib.rs:20-208), written by krets_gb300.parquet (no third-party
+library needed).
 
 * OP: one row, a column per key.  (The reference takes the order of its HashMap; here
   the keys are sorted so files are reproducible.)
@@ -22,11 +23,9 @@ def _parquet_name(filename) -> str:
 
 
 def _write(columns: Dict[str, list], filename) -> str:
-    import pyarrow as pa
-    import pyarrow.parquet as pq
+    from .parquet import write_parquet
     name = _parquet_name(filename)
-    table = pa.table({k: pa.array(v, type=pa.float64()) for k, v in columns.items()})
-    pq.write_table(table, name)
+    write_parquet(columns, name)
     return name
 
 

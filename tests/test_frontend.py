@@ -2,6 +2,7 @@
 import numpy as np
 import pytest
 
+from conftest import ROOT
 from krets_gb300 import AnalysisSpec, generate_frequencies, parse_circuit_description
 from krets_gb300.analyses import AcAnalysis, Decade, Linear, Octave, TransientAnalysis
 from krets_gb300.errors import ParseError
@@ -112,26 +113,89 @@ def _write_case(tmp_path, case):
 def test_cli_ac_parquet_matches_reference_file(tmp_path, golden, oracle_lib):
     """The CLI path (krets.toml -> netlist -> solve -> result.parquet, main.rs:27-138) with
     the parquet layout of krets-result (lib.rs:127-208) reproduces the reference's own
-    circuits/low_pass_filter/ac/result.parquet: column names, order and values."""
-    pq = pytest.importorskip("pyarrow.parquet")
+    circuits/low_pass_filter/ac/result.parquet: column names, order and values (solved
+    here by the oracle; the GPU form of this test is below)."""
     from oracle_solver import OracleSolver
     from krets_gb300.__main__ import run
+    from krets_gb300.parquet import read_parquet
     case = golden["parquet"]["low_pass_ac"]
     out = run(_write_case(tmp_path, case), solver_factory=OracleSolver)
-    t = pq.read_table(out)
+    got = read_parquet(out)
     ref = case["columns"]
-    assert t.column_names == list(ref)
+    assert list(got) == list(ref)
     for k, v in ref.items():
-        np.testing.assert_allclose(t.column(k).to_numpy(), v, rtol=1e-12, atol=1e-15)
+        np.testing.assert_allclose(got[k], v, rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["low_pass_ac", "inverter_dc"])
+def test_cli_on_the_gpu_matches_reference_files(tmp_path, golden, name):
+    """The command line end to end on the GPU: krets.toml and the netlist in a folder,
+    `python -m krets_gb300 krets.toml` (a child process, the reference CLI's behaviour:
+    main.rs:27-138) solves with the default GPU Solver and writes result.parquet, whose
+    columns equal the reference's own result.parquet (AC: magnitude and phase of every
+    unknown at 10 frequencies; DC: the inverter's 101-point sweep)."""
+    import subprocess
+    import sys
+    from krets_gb300.parquet import read_parquet
+    case = golden["parquet"][name]
+    toml = _write_case(tmp_path, case)
+    r = subprocess.run([sys.executable, "-m", "krets_gb300", str(toml)], cwd=str(ROOT), capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    got = read_parquet(tmp_path / "result.parquet")
+    ref = case["columns"]
+    assert sorted(got) == sorted(ref)
+    for k, v in ref.items():
+        np.testing.assert_allclose(got[k], v, rtol=1e-12, atol=1e-15, err_msg=k)
+
+
+@pytest.mark.gpu
+def test_run_with_the_gpu_solver_writes_reference_columns(tmp_path, golden):
+    """run() in-process with the default (GPU) solver on the low-pass AC fixture."""
+    from krets_gb300.__main__ import run
+    from krets_gb300.parquet import read_parquet
+    case = golden["parquet"]["low_pass_ac"]
+    got = read_parquet(run(_write_case(tmp_path, case)))
+    ref = case["columns"]
+    assert list(got) == list(ref)
+    for k, v in ref.items():
+        np.testing.assert_allclose(got[k], v, rtol=1e-12, atol=1e-15, err_msg=k)
+
+
+def test_parquet_writer_reader_round_trip_and_arrow(tmp_path):
+    """The package's own parquet writer: nullable double columns read back by its reader,
+    and by pyarrow (an independent implementation) where it is installed; files pyarrow
+    writes uncompressed with PLAIN pages read back by the package's reader."""
+    from krets_gb300.parquet import read_parquet, write_parquet
+    cols = {"time": [0.0, 1e-3, None] + [float(i) for i in range(30)],
+            "V(a)": [None, 1.5, -2.0] + [None] * 10 + [3.25] * 20,
+            "I(V1)": [np.pi] * 33}
+    f = tmp_path / "a.parquet"
+    write_parquet(cols, f)
+    assert read_parquet(f) == cols
+    write_parquet({"only": [2.5]}, f)
+    assert read_parquet(f) == {"only": [2.5]}
+    pa = pytest.importorskip("pyarrow")
+    pq = pytest.importorskip("pyarrow.parquet")
+    write_parquet(cols, f)
+    t = pq.read_table(f)
+    assert t.column_names == list(cols)
+    for k, v in cols.items():
+        assert t.column(k).to_pylist() == v
+    g = tmp_path / "b.parquet"
+    pq.write_table(pa.table({k: pa.array(v, type=pa.float64()) for k, v in cols.items()}), g,
+                   compression="none", use_dictionary=False, data_page_version="1.0")
+    assert read_parquet(g) == cols
 
 
 def test_transient_and_dc_writers_put_keys_in_order(tmp_path):
-    pq = pytest.importorskip("pyarrow.parquet")
+    from krets_gb300.parquet import read_parquet
     from krets_gb300.results import write_dc_results_to_parquet, write_tran_results_to_parquet
     rows = [{"V(b)": 1.0, "time": 0.0, "I(V1)": 2.0}, {"V(b)": 3.0, "time": 1e-3}]
     name = write_tran_results_to_parquet(rows, tmp_path / "tran")
-    t = pq.read_table(name)
-    assert name.endswith(".parquet") and t.column_names == ["time", "I(V1)", "V(b)"]
-    assert t.column("I(V1)").to_pylist() == [2.0, None]
-    t = pq.read_table(write_dc_results_to_parquet([{"step": 0.0, "V(a)": 1.5}], tmp_path / "dc.parquet"))
-    assert t.column_names == ["V(a)", "step"]
+    t = read_parquet(name)
+    assert name.endswith(".parquet") and list(t) == ["time", "I(V1)", "V(b)"]
+    assert t["I(V1)"] == [2.0, None]
+    t = read_parquet(write_dc_results_to_parquet([{"step": 0.0, "V(a)": 1.5}], tmp_path / "dc.parquet"))
+    assert list(t) == ["V(a)", "step"]

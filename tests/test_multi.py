@@ -1,6 +1,6 @@
 """Multi-circuit engine: many distinct netlists (uneven sizes) in one launch set, each
 checked against the oracle's operating point + backward-Euler transient (reference source
-timing, transient.rs:14-114)."""
+timing, transient.rs:14-114), norm-wise and element-wise (oracle/compare.py) at 1e-9."""
 import numpy as np
 import pytest
 
@@ -8,6 +8,7 @@ from krets_gb300 import _lib
 from krets_gb300.generators import uneven_netlist, uneven_table
 from krets_gb300.netlist import parse_circuit_description
 from krets_gb300.table import element_table
+from oracle.compare import elementwise_err, normwise_err
 
 TOL = 1e-9
 
@@ -20,13 +21,8 @@ def _cur_mask(t, n):
 
 
 def _rel_err(x, ref, mask):
-    worst = 0.0
-    for m in (mask, ~mask):
-        if m.any():
-            r = np.abs(ref[..., m]).max()
-            d = np.abs(x[..., m] - ref[..., m]).max()
-            worst = max(worst, d / r if r > 0 else d)
-    return worst
+    """The larger of the norm-wise and the element-wise error (both must be below 1e-9)."""
+    return max(normwise_err(x, ref, mask), elementwise_err(x, ref, mask))
 
 
 @pytest.mark.parametrize("index", [0, 1, 7, 12])
@@ -72,3 +68,21 @@ def test_multi_circuit_output_offsets_and_device_buffers():
     assert np.array_equal(dev.download(), host)
     host2, _ = m.tran(steps)
     assert np.array_equal(host, host2)                                   # deterministic
+
+
+@pytest.mark.gpu
+def test_multi_circuit_largest_netlists_full_length(oracle_lib):
+    """The largest netlists of the 4096-netlist uneven batch (seed 4) at its full length:
+    the first five with n >= 4000 unknowns and the largest of all (n = 5747), which run in
+    the global-memory class with dense trailing blocks, for 2000 BE steps at 1 ns against
+    the oracle, every unknown at every step."""
+    idx = [23, 32, 35, 40, 54, 2077]
+    tabs = [uneven_table(i) for i in idx]
+    assert min(n for _, n in tabs) >= 4000 and max(n for _, n in tabs) == 5747
+    m = _lib.MultiCircuit([t for t, _ in tabs], [n for _, n in tabs], method="be", h=1e-9)
+    steps = 2000
+    flat, st = m.tran(steps)
+    assert np.all(st == 0)
+    for (t, n), x in zip(tabs, m.split(flat, steps)):
+        ref = oracle_lib.tran(t, n, 1e-9, steps, method="be", lag=True)
+        assert _rel_err(x, ref, _cur_mask(t, n)) < TOL, n
