@@ -569,6 +569,21 @@ def workload_ac(args, world, reference):
 UNEVEN_CIRCUITS, UNEVEN_STEPS, UNEVEN_H = 4096, 2000, 1e-9
 
 
+def fp64_spread(t, n, ref, cur):
+    """Element-wise disagreement of two FP64 solvers over a BE trajectory: SciPy's SuperLU
+    re-solving each step's right-hand side A x_ref[s] (the oracle's own solution) against
+    x_ref[s].  On ill-conditioned netlists it bounds what per-value agreement any FP64
+    solver can show."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as sla
+    from oracle import oracle as O
+    from oracle.compare import elementwise_err
+    A, _ = O.assemble(t, n, mode="tran", h=UNEVEN_H, method="be", sol=ref[0])
+    As = sp.csc_matrix(A)
+    xs = sla.splu(As).solve(np.ascontiguousarray((As @ ref[1:].T)))
+    return elementwise_err(xs.T, ref[1:], cur)
+
+
 def workload_uneven(args, world, reference):
     from krets_gb300 import _lib
     from krets_gb300.generators import uneven_table
@@ -617,7 +632,8 @@ def workload_uneven(args, world, reference):
                                                _lib.ctypes.c_void_p(out.ptr + 8 * int(offs[i])), x.nbytes))
         cur = np.zeros(n, bool)
         cur[t["b"][t["b"] >= 0]] = True
-        return errs_vs_oracle(x.reshape(UNEVEN_STEPS + 1, n), ref, cur)
+        e = errs_vs_oracle(x.reshape(UNEVEN_STEPS + 1, n), ref, cur)
+        return e[0], e[1], fp64_spread(t, n, ref, cur)
 
     with ThreadPoolExecutor(max_workers=threads) as ex:
         errs = list(ex.map(acc_one, acc_idx))
@@ -653,6 +669,9 @@ def workload_uneven(args, world, reference):
     return _line(args, world, metric, value, "circuit-timesteps/s", wl, {
         "ms_per_step": statistics.mean(cs), "dtype": "f64-factor, double-float (2xfp32) solves",
         "max_rel_err_vs_fp64": max(e[0] for e in errs), "max_elementwise_err_vs_fp64": max(e[1] for e in errs),
+        "fp64_solvers_elementwise_spread": max(e[2] for e in errs),
+        "per_netlist_errors": [{"netlist": i, "normwise": e[0], "elementwise": e[1], "fp64_spread": e[2]}
+                               for i, e in zip(acc_idx, errs)],
         "accuracy_sample": f"netlists {acc_idx} (n = {[int(ns[i]) for i in acc_idx]}), all steps",
         "circuits": UNEVEN_CIRCUITS, "sum_unknowns": int(info[1]),
         "sum_lu_entries": int(info[2]), "circuits_per_class": info[4:10].tolist(),

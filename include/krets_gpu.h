@@ -274,6 +274,12 @@ krets_status krets_device_alloc(size_t bytes, void **ptr);
 krets_status krets_device_free(void *ptr);
 krets_status krets_memcpy_h2d(void *dst, const void *src, size_t bytes);
 krets_status krets_memcpy_d2h(void *dst, const void *src, size_t bytes);
+/* Page-lock (pin) a caller's host buffer for the lifetime of a run, and release it.  No
+ * counterpart in the reference.  Results of krets_batch_tran with precision
+ * KRETS_PREC_DF are copied into host x_out buffers by the copy engines while the next
+ * span of steps runs; into pinned memory those copies run at the host link's rate. */
+krets_status krets_host_register(void *ptr, size_t bytes);
+krets_status krets_host_unregister(void *ptr);
 /* Write a scratch buffer larger than L2 (on the given circuit's stream). */
 krets_status krets_flush_l2(krets_circuit *c);
 krets_status krets_device_synchronize(void);

@@ -88,6 +88,8 @@ def lib():
             "krets_memcpy_h2d": [_P, _P, ctypes.c_size_t],
             "krets_memcpy_d2h": [_P, _P, ctypes.c_size_t],
             "krets_flush_l2": [_P],
+            "krets_host_register": [_P, ctypes.c_size_t],
+            "krets_host_unregister": [_P],
             "krets_device_synchronize": [],
             "krets_symbolic_export": [_P, _I, _I, _I, _I, _D, _D, _I, _I, _P, ctypes.c_int64, _P],
         }
@@ -121,6 +123,28 @@ def host_buffer(shape, dtype=np.float64) -> np.ndarray:
     a = np.empty(shape, dtype)
     a.fill(0)
     return a
+
+
+class PinnedBuffer:
+    """A host array page-locked through the library (krets_host_register) until close():
+    the double-float batched transient copies its results into pinned memory at the
+    host link's rate.  `.array` is the numpy view; its pages are touched first."""
+
+    def __init__(self, shape, dtype=np.float64):
+        self.array = host_buffer(shape, dtype)
+        self._ptr = self.array.ctypes.data
+        check(lib().krets_host_register(ctypes.c_void_p(self._ptr), self.array.nbytes), "host_register")
+
+    def close(self):
+        if self._ptr:
+            lib().krets_host_unregister(ctypes.c_void_p(self._ptr))
+            self._ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def ptr(a) -> ctypes.c_void_p:

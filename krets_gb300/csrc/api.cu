@@ -147,8 +147,17 @@ struct krets_circuit {
   int warps_per_cta = 0, grid = 0;
   int launch_info[4] = {0, 0, 0, 0};  // last batched launch: threads per instance, per CTA, grid, tuned
   void *l2buf = nullptr;
+  // staged host output of the double-float engine: two staging buffers, a copy stream
+  void *stage = nullptr;
+  size_t stage_bytes = 0;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t sev[5] = {};  // kernel done x2, copy done x2, operating point done
 
   ~krets_circuit() {
+    if (stage) cudaFree(stage);
+    for (auto &e : sev)
+      if (e) cudaEventDestroy(e);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
     if (d_el) cudaFree(d_el);
     if (scratch) cudaFree(scratch);
     if (d_small) cudaFree(d_small);
@@ -157,6 +166,20 @@ struct krets_circuit {
     for (auto &e : ev)
       if (e) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
+  }
+
+  krets_status ensure_stage(size_t bytes) {
+    if (!copy_stream) {
+      CU(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+      for (auto &e : sev) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    if (bytes <= stage_bytes) return KRETS_OK;
+    if (stage) cudaFree(stage);
+    stage = nullptr;
+    stage_bytes = 0;
+    CU(cudaMalloc(&stage, bytes));
+    stage_bytes = bytes;
+    return KRETS_OK;
   }
 
   krets_status ensure_scratch(size_t bytes) {
@@ -1015,7 +1038,8 @@ namespace {
 // Double-float direct engine launch for a group size G: instances per CTA (W) from the
 // shared-memory footprint, the kernel instance and its residency.
 using DfdKernel = void (*)(DevProg, KCfg, DfdLay, const double *, int, double, int, int, int, double *, int *, int *,
-                           int, WaveTab, Probe, AdjFwd);
+                           int, WaveTab, Probe, AdjFwd, Span);
+constexpr Span kWholeRun{1, 0, 0, nullptr};
 struct DfdLaunch {
   int W = 1, per_sm = 0;
   size_t smem = 0;
@@ -1041,6 +1065,8 @@ bool dfd_layout(const DevProg &P, DfdLay &DL) {
 
 krets_status dfd_config(int G, const DfdLay &DL, DfdLaunch &Lc) {
   Lc.W = (int)std::max<size_t>(1, std::min<size_t>(640 / G, (max_smem_optin() - DL.sprog_bytes) / DL.bytes));
+  const char *wenv = getenv("KRETS_DFD_W");  // at most this many instances per CTA (tuning)
+  if (wenv && atoi(wenv) > 0) Lc.W = std::min(Lc.W, atoi(wenv));
   Lc.smem = DL.sprog_bytes + (size_t)Lc.W * DL.bytes;
   Lc.kd = G == 32 ? k_tran_dfd<32> : (G == 64 ? k_tran_dfd<64> : k_tran_dfd<128>);
   CU(cudaFuncSetAttribute(Lc.kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Lc.smem));
@@ -1086,7 +1112,7 @@ krets_status dfd_pick_group(krets_circuit *c, const DevProgram *D, const DfdLay 
   CU(cudaMalloc(&tst.p, sizeof(int) * trial));
   // the trial instances start from their operating points (row 0 of each waveform, or
   // the probe run's separate operating points)
-  if (!pr.n)
+  if (!pr.n && !pr.x0)
     CU(cudaMemcpy2DAsync(tout.p, row, dx, sizeof(double) * stride, sizeof(double) * n, trial,
                          cudaMemcpyDeviceToDevice, c->stream));
   double best = 0.0;
@@ -1101,7 +1127,7 @@ krets_status dfd_pick_group(krets_circuit *c, const DevProgram *D, const DfdLay 
     CU(cudaEventRecord(c->ev[2], c->stream));
     Lc.kd<<<grid, G * Lc.W, Lc.smem, c->stream>>>(D->view, c->cfg, DL, dv, trial, h, steps, method, lag,
                                                   (double *)tout.p, (int *)tst.p, queue, opts, wt, pr,
-                                                  AdjFwd{nullptr, 1, 0, 0, nullptr});
+                                                  AdjFwd{nullptr, 1, 0, 0, nullptr}, kWholeRun);
     g_launches++;
     CU(cudaGetLastError());
     CU(cudaEventRecord(c->ev[3], c->stream));
@@ -1197,20 +1223,49 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
   if (s != KRETS_OK) return s;
   s = get_program(c, MODE_TRAN, method, h, 0, &Dtr);
   if (s != KRETS_OK) return s;
+  const DevProg &P = Dtr->view;
+  const char *eng = getenv("KRETS_ENGINE");
+  const bool block_forced = eng && strcmp(eng, "block") == 0;
+  // double-float direct: one instance per group of G threads (default 128); it stages only
+  // the step-program words before the residual operators, so it fits where the warp
+  // engine may not
+  DfdLay DL{};
+  const bool use_dfd = precision == KRETS_PREC_DF && !P.nonlinear && P.sprog_ok && !block_forced && dfd_layout(P, DL);
+  // Host output of the double-float engine is staged: the transient runs as spans of
+  // steps, each written to a device staging buffer and copied into the caller's rows by
+  // one strided copy on a second stream while the next span runs (KRETS_HOST_OUT=inplace
+  // keeps the kernel writing host memory directly where the GPU can).
+  const char *hout = getenv("KRETS_HOST_OUT");
+  const bool staged = use_dfd && n_probe <= 0 && n_steps >= 2 && !is_device_ptr(x_out) &&
+                      !(hout && strcmp(hout, "inplace") == 0) &&
+                      sizeof(double) * (size_t)c->n * ((size_t)n_steps + 1) < ((size_t)1 << 31);  // copy pitch
   CU(cudaEventRecord(c->ev[0], c->stream));
   const int n_out = n_probe > 0 ? n_probe : c->n;
   size_t stride = (size_t)n_out * ((size_t)n_steps + 1);
-  DevBuf tv, tx, ts, tfb, twave, top, tprobe;
-  void *dv, *dx;
-  s = dev_view(values, sizeof(double) * c->ne * (size_t)n_inst, true, c->stream, tv, &dv);
-  if (s) return s;
-  s = dev_view(x_out, sizeof(double) * stride * n_inst, false, c->stream, tx, &dx);
-  if (s) return s;
+  DevBuf tv, tx, ts, tfb, twave, top, tprobe, tstate;
+  void *dv, *dx = nullptr;
+  if (staged && values && !is_device_ptr(values)) {  // read once per span: keep a device copy
+    CU(cudaMalloc(&tv.p, sizeof(double) * c->ne * (size_t)n_inst));
+    CU(cudaMemcpyAsync(tv.p, values, sizeof(double) * c->ne * (size_t)n_inst, cudaMemcpyHostToDevice, c->stream));
+    dv = tv.p;
+  } else {
+    s = dev_view(values, sizeof(double) * c->ne * (size_t)n_inst, true, c->stream, tv, &dv);
+    if (s) return s;
+  }
+  if (!staged) {
+    s = dev_view(x_out, sizeof(double) * stride * n_inst, false, c->stream, tx, &dx);
+    if (s) return s;
+  }
   CU(cudaMalloc(&ts.p, sizeof(int) * 2 * (size_t)n_inst));
   int *d_st = (int *)ts.p, *d_opst = d_st + n_inst;
   CU(cudaMemsetAsync(ts.p, 0, sizeof(int) * 2 * (size_t)n_inst, c->stream));
   Probe pr{nullptr, 0, nullptr};
-  if (n_probe > 0) {
+  if (staged) {
+    // operating points in a separate [n_inst][n] buffer (copied to row 0 of each instance)
+    CU(cudaMalloc(&top.p, sizeof(double) * c->n * (size_t)n_inst));
+    pr = Probe{nullptr, 0, (const double *)top.p};
+    s = run_op(c, Ddc, n_inst, (const double *)dv, (double *)top.p, c->n, d_opst, nullptr, 128);
+  } else if (n_probe > 0) {
     // operating points in a separate [n_inst][n] buffer; the probe list on the device
     CU(cudaMalloc(&top.p, sizeof(double) * c->n * (size_t)n_inst));
     void *dp;
@@ -1224,14 +1279,12 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
   if (s) return s;
   const bool dfd = precision == KRETS_PREC_DF;
   bool mixed = precision == KRETS_PREC_MIXED;
-  const DevProg &P = Dtr->view;
   if (dfd && P.nonlinear) mixed = true;  // nonlinear circuits: refactor per Newton iteration (FP32 + refinement)
   int *queue = c->d_small + 8;
   int *d_fallbacks = c->d_small + 12;
   CU(cudaMemsetAsync(c->d_small + 8, 0, 8 * sizeof(int), c->stream));
   CU(cudaMemsetAsync(c->d_hist, 0, 8 * sizeof(unsigned long long), c->stream));
-  const char *eng = getenv("KRETS_ENGINE");
-  bool warp_engine = !(eng && strcmp(eng, "block") == 0);
+  bool warp_engine = !block_forced;
   WarpLay WL{};
   size_t per_warp = 0;
   if (warp_engine) {
@@ -1239,12 +1292,6 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
     if (!P.sprog_ok || per_warp + WL.sprog_bytes > max_smem_optin()) warp_engine = false;
   }
   double *fb = nullptr;
-  // double-float direct: one instance per group of G threads (default 128); it stages only
-  // the step-program words before the residual operators, so it fits where the warp
-  // engine may not
-  DfdLay DL{};
-  bool use_dfd = dfd && !P.nonlinear && P.sprog_ok && !(eng && strcmp(eng, "block") == 0);
-  if (use_dfd) use_dfd = dfd_layout(P, DL);
   if (n_probe > 0 && !use_dfd)
     return fail(KRETS_ERR_INVALID_ARGUMENT,
                 "probe outputs need the double-float engine (precision 2, a linear circuit that fits)");
@@ -1289,11 +1336,69 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
     c->launch_info[1] = W;
     c->launch_info[2] = grid;
     c->launch_info[3] = how;
-    CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
-    CU(cudaEventRecord(c->ev[2], c->stream));
-    Lc.kd<<<grid, G * W, Lc.smem, c->stream>>>(P, c->cfg, DL, (const double *)dv, n_inst, h, n_steps, method,
-                                               source_lag, (double *)dx, d_st, queue, opts, wt, pr,
-                                               AdjFwd{nullptr, 1, 0, 0, nullptr});
+    if (!staged) {
+      CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
+      CU(cudaEventRecord(c->ev[2], c->stream));
+      Lc.kd<<<grid, G * W, Lc.smem, c->stream>>>(P, c->cfg, DL, (const double *)dv, n_inst, h, n_steps, method,
+                                                 source_lag, (double *)dx, d_st, queue, opts, wt, pr,
+                                                 AdjFwd{nullptr, 1, 0, 0, nullptr}, kWholeRun);
+    } else {
+      // spans of R steps; two staging buffers of n_inst x R rows (KRETS_STAGE_MB each,
+      // default 2048), at least 8 spans
+      const size_t row_bytes = sizeof(double) * c->n * (size_t)n_inst;
+      const char *smb = getenv("KRETS_STAGE_MB");
+      const size_t budget = (smb ? (size_t)std::max(1, atoi(smb)) : 2048) << 20;
+      const int R = (int)std::max<size_t>(1, std::min<size_t>((n_steps + 7) / 8, budget / row_bytes));
+      const int nspan = (n_steps + R - 1) / R;
+      s = c->ensure_stage(2 * (size_t)R * row_bytes);
+      if (s != KRETS_OK) return s;
+      double *stage[2] = {(double *)c->stage, (double *)c->stage + (size_t)R * c->n * n_inst};
+      CU(cudaMalloc(&tstate.p, sizeof(df) * ((size_t)P.n + P.ncap) * n_inst));
+      cudaEvent_t *kdone = c->sev, *copied = c->sev + 2, op_done = c->sev[4];
+      const size_t pitch = sizeof(double) * stride;
+      auto launch = [&](int j) -> krets_status {
+        const int s0 = j * R + 1, s1 = std::min(n_steps, (j + 1) * R);
+        if (j >= 2) CU(cudaStreamWaitEvent(c->stream, copied[j & 1], 0));  // its buffer has been copied out
+        CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
+        Lc.kd<<<grid, G * W, Lc.smem, c->stream>>>(P, c->cfg, DL, (const double *)dv, n_inst, h, s1, method,
+                                                   source_lag, stage[j & 1], d_st, queue, opts, wt, pr,
+                                                   AdjFwd{nullptr, 1, 0, 0, nullptr},
+                                                   Span{s0, s0, (long long)R * c->n, (df *)tstate.p});
+        g_launches++;
+        CU(cudaGetLastError());
+        CU(cudaEventRecord(kdone[j & 1], c->stream));
+        return KRETS_OK;
+      };
+      auto copy_out = [&](int j) -> krets_status {
+        const int s0 = j * R + 1, s1 = std::min(n_steps, (j + 1) * R);
+        CU(cudaStreamWaitEvent(c->copy_stream, kdone[j & 1], 0));
+        CU(cudaMemcpy2DAsync(x_out + (size_t)s0 * c->n, pitch, stage[j & 1], sizeof(double) * R * c->n,
+                             sizeof(double) * (size_t)(s1 - s0 + 1) * c->n, n_inst, cudaMemcpyDeviceToHost,
+                             c->copy_stream));
+        CU(cudaEventRecord(copied[j & 1], c->copy_stream));
+        return KRETS_OK;
+      };
+      CU(cudaEventRecord(c->ev[2], c->stream));
+      // each span's copy is issued after the next span's launch, so the copies overlap
+      // the kernels even where a copy into pageable memory returns only when it is done
+      s = launch(0);
+      if (s != KRETS_OK) return s;
+      CU(cudaEventRecord(op_done, c->stream));
+      CU(cudaStreamWaitEvent(c->copy_stream, op_done, 0));
+      CU(cudaMemcpy2DAsync(x_out, pitch, top.p, sizeof(double) * c->n, sizeof(double) * c->n, n_inst,
+                           cudaMemcpyDeviceToHost, c->copy_stream));  // row 0: the operating points
+      for (int j = 0; j < nspan; ++j) {
+        if (j + 1 < nspan) {
+          s = launch(j + 1);
+          if (s != KRETS_OK) return s;
+        }
+        s = copy_out(j);
+        if (s != KRETS_OK) return s;
+      }
+      CU(cudaEventRecord(c->ev[3], c->stream));
+      CU(cudaEventRecord(op_done, c->copy_stream));
+      CU(cudaStreamWaitEvent(c->stream, op_done, 0));  // every copy is done before the call returns
+    }
   } else if (warp_engine) {
     const int W = warp_engine_width(WL, per_warp);
     size_t smem = WL.sprog_bytes + (size_t)W * per_warp;
@@ -1341,9 +1446,11 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
     kern<<<grid, threads, smem, c->stream>>>(P, c->cfg, L, gws, (const double *)dv, n_inst, h, n_steps, method,
                                              source_lag, (double *)dx, d_st, queue, c->d_hist, d_fallbacks, fb);
   }
-  g_launches++;
-  CU(cudaGetLastError());
-  CU(cudaEventRecord(c->ev[3], c->stream));
+  if (!staged) {
+    g_launches++;
+    CU(cudaGetLastError());
+    CU(cudaEventRecord(c->ev[3], c->stream));
+  }
   if (tx.p) CU(cudaMemcpyAsync(x_out, dx, sizeof(double) * stride * n_inst, cudaMemcpyDeviceToHost, c->stream));
   std::vector<int> st(2 * (size_t)n_inst);
   CU(cudaMemcpyAsync(st.data(), ts.p, sizeof(int) * 2 * (size_t)n_inst, cudaMemcpyDeviceToHost, c->stream));
@@ -1550,7 +1657,7 @@ krets_status krets_adjoint_tran(krets_circuit *c, int32_t n_inst, const double *
     const AdjFwd af{(df *)tck.p, K, P.n + P.ncap, H.qinv[out_unknown], (double *)d_loss};
     Lf.kd<<<fgrid, 128 * Lf.W, Lf.smem, c->stream>>>(P, c->cfg, DL, (const double *)dv, n_inst, h, n_steps, method,
                                                      0, nullptr, (int *)tstf.p, queue, 0, wt,
-                                                     Probe{nullptr, 0, nullptr}, af);
+                                                     Probe{nullptr, 0, nullptr}, af, kWholeRun);
     g_launches++;
     CU(cudaGetLastError());
     CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
@@ -1648,6 +1755,18 @@ krets_status krets_memcpy_h2d(void *dst, const void *src, size_t bytes) {
 
 krets_status krets_memcpy_d2h(void *dst, const void *src, size_t bytes) {
   CU(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+  return KRETS_OK;
+}
+
+krets_status krets_host_register(void *ptr, size_t bytes) {
+  if (!ptr || !bytes) return fail(KRETS_ERR_INVALID_ARGUMENT, "null or empty host buffer");
+  CU(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+  return KRETS_OK;
+}
+
+krets_status krets_host_unregister(void *ptr) {
+  if (!ptr) return fail(KRETS_ERR_INVALID_ARGUMENT, "null host buffer");
+  CU(cudaHostUnregister(ptr));
   return KRETS_OK;
 }
 
@@ -1771,7 +1890,7 @@ krets_status krets_batch_tran_noalloc(krets_circuit *c, int32_t n_inst, const do
     CU(cudaEventRecord(c->ev[2], c->stream));
     Lc.kd<<<grid, G * Lc.W, Lc.smem, c->stream>>>(P, c->cfg, DL, d_values, n_inst, h, n_steps, method, source_lag,
                                                   d_x_out, d_inst_status, queue, opts, wt, Probe{nullptr, 0, nullptr},
-                                                  AdjFwd{nullptr, 1, 0, 0, nullptr});
+                                                  AdjFwd{nullptr, 1, 0, 0, nullptr}, kWholeRun);
   } else {
     const int W = warp_engine_width(WL, per_warp);
     const size_t smem = WL.sprog_bytes + (size_t)W * per_warp;

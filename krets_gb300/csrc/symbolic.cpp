@@ -273,6 +273,13 @@ std::vector<int> order_min_degree(int n, const std::vector<std::vector<int>> &ad
     size_t bd = 0;
     for (int v = 0; v < n; ++v)
       if (!gone[v] && (best < 0 || adj[v].size() < bd)) { best = v; bd = adj[v].size(); }
+    if (bd + 1 == (size_t)(n - step)) {
+      // every remaining vertex is adjacent to all others: a clique, whose vertices the
+      // selection above would take in increasing index order (equal degrees throughout)
+      for (int v = 0; v < n; ++v)
+        if (!gone[v]) order.push_back(v);
+      break;
+    }
     gone[best] = 1;
     order.push_back(best);
     const std::vector<int> nb = adj[best];
@@ -289,7 +296,8 @@ std::vector<int> order_min_degree(int n, const std::vector<std::vector<int>> &ad
   return order;
 }
 
-std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<int>> &adj) {
+std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<int>> &adj, int *top_sep) {
+  if (top_sep) *top_sep = 0;
   std::vector<int> order;
   order.reserve(n);
   std::vector<int> in_set(n, -1), level(n, -1);
@@ -378,6 +386,7 @@ std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<in
       for (int l = 0; l < best; ++l) A.insert(A.end(), levels[l].begin(), levels[l].end());
       for (int l = best + 1; l < L; ++l) B.insert(B.end(), levels[l].begin(), levels[l].end());
       std::vector<int> S = levels[best];
+      if (top_sep && *top_sep == 0) *top_sep = (int)S.size();  // the first separator found
       nd(A);
       nd(B);
       std::sort(S.begin(), S.end());
@@ -714,14 +723,39 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
       return KRETS_ERR_UNEXPECTED;
     }
   }
+  // ---- dense trailing block: the largest m whose trailing m x m block is fully dense
+  // (row k holds every column from cstart[k] to n-1; a trailing block is dense when each
+  // of its rows starts its run at or before the block start, and density of a block
+  // implies density of every smaller trailing block)
+  if (dense_tail && n > 0) {
+    int t0 = n, runmax = 0;
+    for (int k = n - 1; k >= 0; --k) {
+      int expect = n - 1, s = P.lu_rowptr[k + 1] - 1;
+      while (s >= P.lu_rowptr[k] && P.lu_col[s] == expect) { --s; --expect; }
+      runmax = std::max(runmax, expect + 1);
+      if (runmax > k) break;
+      t0 = k;
+    }
+    if (n - t0 >= kMinDenseTail) {
+      P.tail0 = t0;
+      P.tail_m = n - t0;
+    }
+  }
   // ---- factorisation program (IKJ)
   P.piv_ptr.assign(n + 1, 0);
   if (!update_list) {
     // no explicit update list (the device merges each U row into the pattern of row k):
-    // count the work and check that every update lands inside the static pattern
+    // count the work and check that every update lands inside the static pattern (rows
+    // k and j both in the dense trailing block need no check: U row j's columns all lie
+    // in the block, where row k holds every column)
+    const int t0 = P.tail_m ? P.tail0 : n;
     for (int k = 0; k < n; ++k) {
       for (int s = P.lu_rowptr[k]; s < P.lu_diag[k]; ++s) {
         const int j = P.lu_col[s];
+        if (k >= t0 && j >= t0) {
+          P.factor_flops += 2 * (P.lu_rowptr[j + 1] - P.lu_diag[j] - 1) + 1;
+          continue;
+        }
         int p = s + 1;
         for (int t = P.lu_diag[j] + 1; t < P.lu_rowptr[j + 1]; ++t) {
           const int c = P.lu_col[t];
@@ -755,24 +789,6 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
       P.factor_flops += 1;
     }
     P.piv_ptr[k + 1] = (int)P.piv.size() / 4;
-  }
-  // ---- dense trailing block: the largest m whose trailing m x m block is fully dense
-  // (row k holds every column from cstart[k] to n-1; a trailing block is dense when each
-  // of its rows starts its run at or before the block start, and density of a block
-  // implies density of every smaller trailing block)
-  if (dense_tail && n > 0) {
-    int t0 = n, runmax = 0;
-    for (int k = n - 1; k >= 0; --k) {
-      int expect = n - 1, s = P.lu_rowptr[k + 1] - 1;
-      while (s >= P.lu_rowptr[k] && P.lu_col[s] == expect) { --s; --expect; }
-      runmax = std::max(runmax, expect + 1);
-      if (runmax > k) break;
-      t0 = k;
-    }
-    if (n - t0 >= kMinDenseTail) {
-      P.tail0 = t0;
-      P.tail_m = n - t0;
-    }
   }
   const int tail0 = P.tail_m ? P.tail0 : n;
   // ---- level schedules (rows of the dense block: one last L level of their sparse
@@ -889,7 +905,9 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
     P.bd_ptr[r + 1] = (int)P.bd_op.size();
   }
   pack_step_program(el, P);
-  if (mode == MODE_TRAN && !P.tail_m) pack_transposed_program(P);
+  // the transposed program serves the adjoint, which runs single-circuit programs (with
+  // an update list); multi-circuit programs never need it
+  if (mode == MODE_TRAN && !P.tail_m && update_list) pack_transposed_program(P);
   uint64_t sig = 1469598103934665603ull;
   sig = fnv1a(sig, (uint64_t)mode);
   sig = fnv1a(sig, (uint64_t)n);
@@ -992,7 +1010,12 @@ int build_program(const krets_element *el, int ne, int n, int mode, int method, 
       if (n > 20000) continue;
       q = order_min_degree(n, adj);
     } else {
-      q = order_nested_dissection(n, adj);
+      int top_sep = 0;
+      q = order_nested_dissection(n, adj, &top_sep);
+      // bisection by BFS levels suits chains, ladders and meshes (separators of a few
+      // vertices, or ~sqrt(n)); on irregular graphs its first separator is already large and
+      // its fill beyond the minimum-degree one, so it is not factored once that is known
+      if (fill_cap && top_sep > std::max(16, (int)(2.0 * std::sqrt((double)n)))) continue;
     }
     Program P;
     std::string m2;

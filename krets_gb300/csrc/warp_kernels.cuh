@@ -1383,17 +1383,42 @@ struct AdjFwd {
   double *loss;
 };
 
-template <int G, int SG = G>
+// Steps s_begin .. n_steps; the row of step s is out + (s - row_base) * n_out.
+// CBREC (trapezoidal rule, not with an adjoint forward pass): a capacitor's rhs value is
+// carried from step to step as its companion current source itself, cb_n = 2 (2C/h) v_{n-1}
+// - cb_{n-1} (the same recurrence as cb_n = (2C/h) v_{n-1} + i_{n-1} with
+// i_{n-1} = (2C/h) v_{n-1} - cb_{n-1}), so the per-step pass that forms the capacitor
+// currents after the solve is not needed; icap holds the currents again on return.
+template <int G, int SG = G, bool CBREC = false>
 __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const df *lu, df *x, const df *cdyn, df *cb,
                                          df *icap, const double *vals, double h, int n_steps, int method, int lag,
                                          double *out, int lnar, int unar, bool int_cvt, int gl, int gid,
                                          WaveTab wt = WaveTab{nullptr, nullptr, 0},
                                          Probe pr = Probe{nullptr, 0, nullptr},
-                                         AdjFwd af = AdjFwd{nullptr, 1, 0, 0, nullptr}) {
+                                         AdjFwd af = AdjFwd{nullptr, 1, 0, 0, nullptr}, int s_begin = 1,
+                                         int row_base = 0) {
   const int n_out = pr.n ? pr.n : P.n;
   df loss{0.f, 0.f};  // adjoint forward pass: lane 0 of the group accumulates
   int st = 0;
-  for (int s = 1; s <= n_steps; ++s) {
+  // The first tabulated source among this thread's rhs elements has its next value loaded
+  // one step ahead, off the step's critical path (others read the table in the step).
+  int pf_d = -1;
+  size_t pf_base = 0;
+  double pf_val = 0.0;
+  if (wt.tab && s_begin <= n_steps)
+    for (int d = gl; d < P.ndyn; d += G)
+      if ((int)((unsigned)S.dyn[d].x >> 24) == KRETS_ELEM_V && wt.row[d] >= 0) {
+        pf_d = d;
+        pf_base = (size_t)wt.row[d] * wt.stride;
+        pf_val = wt.tab[pf_base + s_begin];
+        break;
+      }
+  if (CBREC)  // companion currents of the step before s_begin (x and icap are final: the caller synced)
+    for (int d = gl; d < P.ncap; d += G) {
+      const int4 dd = S.dyn[d];
+      cb[d] = df_sub(df_mul(cdyn[d], df_sub(df_at(x, dd.y), df_at(x, dd.z))), icap[d]);
+    }
+  for (int s = s_begin; s <= n_steps; ++s) {
     const double t = (double)s * h;
     const double t_src = lag ? (double)(s - 1) * h : t;
     if (af.ck && (s - 1) % af.K == 0) {  // x and icap are final: the previous step's last level synced
@@ -1407,17 +1432,27 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
       df v{0.f, 0.f};
       if (kind == KRETS_ELEM_C) {
         const df vprev = df_sub(df_at(x, dd.y), df_at(x, dd.z));
-        v = method == KRETS_METHOD_TR ? df_fma(cdyn[d], vprev, icap[d]) : df_mul(cdyn[d], vprev);
+        if (CBREC) {
+          const df c2{2.f * cdyn[d].hi, 2.f * cdyn[d].lo};  // exact doubling
+          v = df_fma(c2, vprev, df_neg(cb[d]));
+        } else {
+          v = method == KRETS_METHOD_TR ? df_fma(cdyn[d], vprev, icap[d]) : df_mul(cdyn[d], vprev);
+        }
       } else if (kind == KRETS_ELEM_L) {
         const df li = df_neg(df_mul(cdyn[d], x[dd.w]));
         v = method == KRETS_METHOD_TR ? df_sub(li, df_sub(df_at(x, dd.y), df_at(x, dd.z))) : li;
       } else if (kind == KRETS_ELEM_V) {
-        const int e = dd.x & 0xffffff;
-        const krets_element &E = P.el[e];
-        const int wr = wt.tab ? wt.row[d] : -1;
-        if (wr >= 0) v = df_from_double(wt.tab[(size_t)wr * wt.stride + s]);
-        else if (E.wave == KRETS_WAVE_NONE) v = cdyn[d];  // the DC value, split at set-up
-        else v = df_from_double(wave_value(E, vals ? vals[e] : E.value, t_src));
+        if (d == pf_d) {
+          v = df_from_double(pf_val);
+          if (s < n_steps) pf_val = wt.tab[pf_base + s + 1];
+        } else {
+          const int e = dd.x & 0xffffff;
+          const krets_element &E = P.el[e];
+          const int wr = wt.tab ? wt.row[d] : -1;
+          if (wr >= 0) v = df_from_double(wt.tab[(size_t)wr * wt.stride + s]);
+          else if (E.wave == KRETS_WAVE_NONE) v = cdyn[d];  // the DC value, split at set-up
+          else v = df_from_double(wave_value(E, vals ? vals[e] : E.value, t_src));
+        }
       } else if (kind == KRETS_ELEM_I) {
         v = cdyn[d];
       }
@@ -1435,7 +1470,7 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
     gsync<G>(gid);
     df_solve<G, false, SG>(S, lu, x, gl, gid, lnar);
     df_solve<G, true, SG>(S, lu, x, gl, gid, unar);
-    if (method == KRETS_METHOD_TR) {
+    if (!CBREC && method == KRETS_METHOD_TR) {
       for (int d = gl; d < P.ncap; d += G) {
         const int4 dd = S.dyn[d];
         const df vn = df_sub(df_at(x, dd.y), df_at(x, dd.z));
@@ -1446,7 +1481,7 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
       if (gl == 0) loss = df_fma(x[af.out_pos], x[af.out_pos], loss);
       continue;  // no waveform output in the adjoint forward pass
     }
-    double *row = out + (size_t)s * n_out;
+    double *row = out + (size_t)(s - row_base) * n_out;
     for (int j = gl; j < n_out; j += G) {
       const df xv = x[S.qinv[pr.n ? pr.idx[j] : j]];
       const double v = int_cvt ? df_to_double_int(xv) : df_to_double(xv);
@@ -1458,16 +1493,37 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
     // orders every read of x before the gather overwrites it.  Callers synchronise the
     // group after the last step.
   }
+  if (CBREC) {  // the capacitor currents of the last step, for a caller that keeps the state
+    gsync<G>(gid);
+    for (int d = gl; d < P.ncap; d += G) {
+      const int4 dd = S.dyn[d];
+      icap[d] = df_sub(df_mul(cdyn[d], df_sub(df_at(x, dd.y), df_at(x, dd.z))), cb[d]);
+    }
+  }
   if (af.loss && gl == 0) *af.loss = df_to_double(loss);
   return st;
 }
 
-// opts bit 0: run narrow levels on one warp; bit 1: integer-only FP64 output conversion
+// A span of the time steps for one launch, so that a long transient can run as several
+// launches (each writing its rows to a staging buffer that is copied out while the next
+// launch runs).  Steps s_begin .. n_steps are computed; step s goes to output row
+// s - row_base of the instance, whose rows are `stride` values apart (0: (n_steps + 1)
+// rows of the output width).  With `state` ([n_inst][n + ncap] double-float: x in
+// position space, then the TR capacitor currents) a span with s_begin > 1 resumes from
+// the state the previous span saved, and every span saves its final state there.
+struct Span {
+  int s_begin, row_base;
+  long long stride;
+  df *state;
+};
+
+// opts bit 0: run narrow levels on one warp; bit 1: integer-only FP64 output conversion;
+// bit 2: trapezoidal capacitor history as companion currents (dfd_steps CBREC)
 template <int G>
 __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay L, const double *values, int n_inst,
                                                      double h, int n_steps, int method, int lag, double *x_out,
                                                      int *inst_status, int *queue, int opts, WaveTab wt, Probe pr,
-                                                     AdjFwd af) {
+                                                     AdjFwd af, Span sp) {
   extern __shared__ __align__(16) char smem[];
   const int gl = threadIdx.x % G, gid = threadIdx.x / G;
   {
@@ -1483,6 +1539,8 @@ __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
   while (unar < S.nulev && S.ulev_ptr[unar + 1] - S.ulev_ptr[unar] <= 64) ++unar;
   if (!(opts & 1)) lnar = unar = -1;
   const bool int_cvt = (opts & 2) != 0;
+  // bit 2: trapezoidal capacitor history carried as the companion current (no adjoint pass)
+  const bool cbrec = (opts & 4) != 0 && method == KRETS_METHOD_TR && !af.ck;
   char *base = smem + L.sprog_bytes + (size_t)gid * L.bytes;
   df *lu = reinterpret_cast<df *>(base + L.lu);
   double *lu64 = reinterpret_cast<double *>(base + L.lu);  // same bytes, set-up only
@@ -1492,7 +1550,8 @@ __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
   df *icap = reinterpret_cast<df *>(base + L.icap);
   int *slot = reinterpret_cast<int *>(base + L.slot);
   double *coef64 = reinterpret_cast<double *>(base + L.coef64);  // set-up only
-  const size_t stride = (size_t)(n_steps + 1) * (pr.n ? pr.n : P.n);
+  const size_t stride = sp.stride ? (size_t)sp.stride : (size_t)(n_steps + 1) * (pr.n ? pr.n : P.n);
+  const int ns = P.n + P.ncap;  // state words of an instance
   while (true) {
     if (gl == 0) slot[0] = atomicAdd(queue, 1);
     gsync<G>(gid);
@@ -1503,22 +1562,40 @@ __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
     double *out = x_out ? x_out + (size_t)inst * stride : nullptr;
     const double *op = pr.x0 ? pr.x0 + (size_t)inst * P.n : out;  // operating point (none: x_0 = 0)
     int st = dfd_setup<G>(P, S, vals, h, method, lu, lu64, coef64, cdyn, gl, gid);
-    for (int k = gl; k < P.n; k += G) x[k] = op ? df_from_double(op[P.q[k]]) : df{0.f, 0.f};
-    for (int j = gl; j < pr.n; j += G) out[j] = op[pr.idx[j]];  // probe row 0
+    df *state = sp.state ? sp.state + (size_t)inst * ns : nullptr;
+    if (state && sp.s_begin > 1) {  // resume: x and the TR currents where the previous span stopped
+      for (int k = gl; k < P.n; k += G) x[k] = state[k];
+      for (int d = gl; d < P.ncap; d += G) icap[d] = state[P.n + d];
+    } else {
+      for (int k = gl; k < P.n; k += G) x[k] = op ? df_from_double(op[P.q[k]]) : df{0.f, 0.f};
+      for (int j = gl; j < pr.n; j += G) out[j] = op[pr.idx[j]];  // probe row 0
+      for (int d = gl; d < P.ncap; d += G) icap[d] = df{0.f, 0.f};
+    }
     AdjFwd a = af;
     if (af.ck) {
       a.ck = af.ck + (size_t)inst * ((n_steps + af.K - 1) / af.K) * af.ck_words;
       a.loss = af.loss + inst;
     }
-    for (int d = gl; d < P.ncap; d += G) icap[d] = df{0.f, 0.f};
     const bool fatal = gany<G>((st & (KS_SINGULAR | KS_NONFINITE | KS_NOTIMPL)) != 0, gid);
-    if (!fatal) st |= dfd_steps<G>(P, S, lu, x, cdyn, cb, icap, vals, h, n_steps, method, lag, out, lnar, unar, int_cvt,
-                                   gl, gid, wt, pr, a);
+    if (!fatal) {
+      if (cbrec)
+        st |= dfd_steps<G, G, true>(P, S, lu, x, cdyn, cb, icap, vals, h, n_steps, method, lag, out, lnar, unar,
+                                    int_cvt, gl, gid, wt, pr, a, sp.s_begin, sp.row_base);
+      else
+        st |= dfd_steps<G>(P, S, lu, x, cdyn, cb, icap, vals, h, n_steps, method, lag, out, lnar, unar, int_cvt, gl,
+                           gid, wt, pr, a, sp.s_begin, sp.row_base);
+    }
+    if (state) {  // the last step's solution level and TR currents are final once the group syncs
+      gsync<G>(gid);
+      for (int k = gl; k < P.n; k += G) state[k] = x[k];
+      for (int d = gl; d < P.ncap; d += G) state[P.n + d] = icap[d];
+    }
     if (gl == 0) slot[1] = 0;
     gsync<G>(gid);
     if (st) atomicOr(&slot[1], st);
     gsync<G>(gid);
-    if (gl == 0 && inst_status) inst_status[inst] = slot[1];
+    // statuses accumulate over the spans of one transient (the caller zeroes them first)
+    if (gl == 0 && inst_status) inst_status[inst] |= slot[1];
   }
 }
 
