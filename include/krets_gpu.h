@@ -258,7 +258,9 @@ krets_status krets_last_timing(const krets_circuit *c, float *kernel_ms, float *
 /* The last double-float batched transient launch: info[0] = threads per instance,
  * info[1] = instances per CTA, info[2] = grid, info[3] = how the group size was chosen
  * (1 = timed now by the autotuner, 2 = the autotuner's cached choice for this sparsity
- * signature, 0 = default, too few steps to time; KRETS_GROUP=32|64|128 overrides). */
+ * signature, 0 = default, too few steps to time; KRETS_GROUP=32|64|128 overrides),
+ * info[4] = 1 when the factors were kept in global memory (more instances per SM) instead
+ * of shared memory (the autotuner chooses; KRETS_DFD_LU=smem|global overrides). */
 krets_status krets_last_launch(const krets_circuit *c, int32_t *info, int32_t cap);
 /* Kernel launches issued by this library since load. */
 int64_t krets_launch_count(void);

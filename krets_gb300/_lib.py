@@ -447,12 +447,13 @@ class GpuCircuit:
 
     def last_launch(self):
         """Last double-float batched launch: threads per instance, instances per CTA, grid,
-        and how the group size was chosen ("default" / "autotuner" / "autotuner cache")."""
-        info = np.zeros(4, dtype=np.int32)
-        check(lib().krets_last_launch(self.h, ptr(info), 4), "last_launch")
+        how the group size was chosen ("default" / "autotuner" / "autotuner cache"), and
+        where the factors were kept."""
+        info = np.zeros(5, dtype=np.int32)
+        check(lib().krets_last_launch(self.h, ptr(info), 5), "last_launch")
         how = {0: "default", 1: "autotuner", 2: "autotuner cache"}.get(int(info[3]), "?")
         return {"threads_per_instance": int(info[0]), "instances_per_cta": int(info[1]), "grid": int(info[2]),
-                "group_size_from": how}
+                "group_size_from": how, "factors": "global memory" if info[4] else "shared memory"}
 
     def flush_l2(self):
         check(lib().krets_flush_l2(self.h))

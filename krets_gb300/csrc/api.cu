@@ -107,6 +107,20 @@ bool is_device_ptr(const void *p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Host memory that is page-locked (cudaHostAlloc or cudaHostRegister) over [p, p + bytes).
+bool is_pinned_host(const void *p, size_t bytes) {
+  if (!p || !bytes) return false;
+  for (const char *q : {(const char *)p, (const char *)p + bytes - 1}) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    if (a.type != cudaMemoryTypeHost) return false;
+  }
+  return true;
+}
+
 // Kernels may read and write pageable host memory directly on systems whose GPU shares the
 // host's page tables (Grace: NVLink-C2C with address translation); then host buffers are
 // used in place instead of through a device copy.  KRETS_NO_DIRECT_HOST=1 turns it off.
@@ -145,8 +159,11 @@ struct krets_circuit {
   long long hist[8] = {};
   int fallbacks = 0;
   int warps_per_cta = 0, grid = 0;
-  int launch_info[4] = {0, 0, 0, 0};  // last batched launch: threads per instance, per CTA, grid, tuned
+  int launch_info[5] = {0, 0, 0, 0, 0};  // last batched launch: threads per instance, per CTA, grid, tuned, lug
   void *l2buf = nullptr;
+  // global-memory factors of the double-float engine's groups (k_tran_dfd<G, true>)
+  void *lug = nullptr;
+  size_t lug_bytes = 0;
   // staged host output of the double-float engine: two staging buffers, a copy stream
   void *stage = nullptr;
   size_t stage_bytes = 0;
@@ -154,6 +171,7 @@ struct krets_circuit {
   cudaEvent_t sev[5] = {};  // kernel done x2, copy done x2, operating point done
 
   ~krets_circuit() {
+    if (lug) cudaFree(lug);
     if (stage) cudaFree(stage);
     for (auto &e : sev)
       if (e) cudaEventDestroy(e);
@@ -166,6 +184,16 @@ struct krets_circuit {
     for (auto &e : ev)
       if (e) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
+  }
+
+  krets_status ensure_lug(size_t bytes) {
+    if (bytes <= lug_bytes) return KRETS_OK;
+    if (lug) cudaFree(lug);
+    lug = nullptr;
+    lug_bytes = 0;
+    CU(cudaMalloc(&lug, bytes));
+    lug_bytes = bytes;
+    return KRETS_OK;
   }
 
   krets_status ensure_stage(size_t bytes) {
@@ -1038,19 +1066,26 @@ namespace {
 // Double-float direct engine launch for a group size G: instances per CTA (W) from the
 // shared-memory footprint, the kernel instance and its residency.
 using DfdKernel = void (*)(DevProg, KCfg, DfdLay, const double *, int, double, int, int, int, double *, int *, int *,
-                           int, WaveTab, Probe, AdjFwd, Span);
+                           int, WaveTab, Probe, AdjFwd, Span, df *);
 constexpr Span kWholeRun{1, 0, 0, nullptr};
+// default options of the double-float engine (KRETS_DFD_OPTS overrides): trapezoidal
+// capacitor history as companion currents (bit 2), measured 4 % faster on the RLC ladder
+constexpr int kDfdDefaultOpts = 4;
 struct DfdLaunch {
-  int W = 1, per_sm = 0;
+  int G = 128, W = 1, per_sm = 0;
+  bool lug = false;  // factors in global memory (k_tran_dfd<G, true>)
   size_t smem = 0;
   DfdKernel kd = nullptr;
+  int slots() const { return W * per_sm * device_sm_count(); }
 };
 
-// Shared-memory layout of one double-float instance; false when it does not fit a CTA.
-bool dfd_layout(const DevProg &P, DfdLay &DL) {
+// Shared-memory layout of one double-float instance (without the factors when lug: they
+// are then in global memory); false when it does not fit a CTA.
+bool dfd_layout(const DevProg &P, DfdLay &DL, bool lug = false) {
   size_t cur = 0;
   auto put = [&](int &off, size_t bytes) { off = (int)cur; cur = align16(cur + bytes); };
-  put(DL.lu, 8 * (size_t)P.nnz_lu);
+  if (lug) DL.lu = 0;
+  else put(DL.lu, 8 * (size_t)P.nnz_lu);
   put(DL.x, 8 * (size_t)P.n);
   put(DL.cdyn, 8 * (size_t)P.ndyn);
   put(DL.cb, 8 * (size_t)P.ndyn);
@@ -1063,91 +1098,134 @@ bool dfd_layout(const DevProg &P, DfdLay &DL) {
   return (size_t)DL.bytes + DL.sprog_bytes <= max_smem_optin();
 }
 
-krets_status dfd_config(int G, const DfdLay &DL, DfdLaunch &Lc) {
-  Lc.W = (int)std::max<size_t>(1, std::min<size_t>(640 / G, (max_smem_optin() - DL.sprog_bytes) / DL.bytes));
+// Instances per CTA (W) from the shared-memory footprint, at most 896 threads per CTA (the
+// kernel's launch bound) and 15 groups (named barriers 1..15) for G >= 64.
+krets_status dfd_config(int G, bool lug, const DfdLay &DL, DfdLaunch &Lc) {
+  Lc.G = G;
+  Lc.lug = lug;
+  const size_t cap = std::min<size_t>(896 / G, G >= 64 ? 15 : 28);
+  Lc.W = (int)std::max<size_t>(1, std::min<size_t>(cap, (max_smem_optin() - DL.sprog_bytes) / DL.bytes));
   const char *wenv = getenv("KRETS_DFD_W");  // at most this many instances per CTA (tuning)
   if (wenv && atoi(wenv) > 0) Lc.W = std::min(Lc.W, atoi(wenv));
   Lc.smem = DL.sprog_bytes + (size_t)Lc.W * DL.bytes;
-  Lc.kd = G == 32 ? k_tran_dfd<32> : (G == 64 ? k_tran_dfd<64> : k_tran_dfd<128>);
+  if (lug) Lc.kd = G == 32 ? k_tran_dfd<32, true> : (G == 64 ? k_tran_dfd<64, true> : k_tran_dfd<128, true>);
+  else Lc.kd = G == 32 ? k_tran_dfd<32> : (G == 64 ? k_tran_dfd<64> : k_tran_dfd<128>);
   CU(cudaFuncSetAttribute(Lc.kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Lc.smem));
   CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&Lc.per_sm, Lc.kd, G * Lc.W, Lc.smem));
   if (Lc.per_sm < 1) return fail(KRETS_ERR_CUDA, "double-float engine does not fit on an SM");
   return KRETS_OK;
 }
 
-// Autotuner of the double-float engine: the threads per instance (G = 128, 64, 32) are
-// chosen by timing one full wave of instances for up to 128 steps with each, once per
+// Global-memory factors of every group of a launch (cached in the handle).
+krets_status dfd_lu_buffer(krets_circuit *c, const DfdLaunch &Lc, int grid, const DevProg &P, df **out) {
+  *out = nullptr;
+  if (!Lc.lug) return KRETS_OK;
+  const size_t bytes = sizeof(df) * (size_t)P.nnz_lu * grid * Lc.W;
+  krets_status s = c->ensure_lug(bytes);
+  if (s != KRETS_OK) return s;
+  *out = (df *)c->lug;
+  return KRETS_OK;
+}
+
+// Autotuner of the double-float engine: the threads per instance (G = 128, 64, 32) and the
+// place of the factors (shared memory, or global memory with more instances per SM) are
+// chosen by timing one full wave of instances for up to 128 steps with each candidate, and
+// ranking them by the time the whole batch would take (waves x wave time), once per
 // sparsity signature (pattern hash, size, LU entries, method); the choice is cached for
 // the process.  how = 1 measured now, 2 from the cache, 0 default (too few steps to time).
+// A choice is kept as G | lug << 8.
 std::mutex g_tune_mu;
 std::map<std::string, int> g_tune;
 
-krets_status dfd_pick_group(krets_circuit *c, const DevProgram *D, const DfdLay &DL, const double *dv,
-                            const double *dx, size_t stride, int n_inst, double h, int n_steps, int method, int lag,
-                            int *queue, int opts, const WaveTab &wt, const Probe &pr, int &G_out, int &how) {
+std::string dfd_tune_key(const DevProgram *D, int method) {
   char key[96];
   snprintf(key, sizeof key, "%016llx/%d/%zu/%d", (unsigned long long)D->host.signature, D->host.n,
            D->host.lu_col.size(), method);
+  return key;
+}
+
+krets_status dfd_pick(krets_circuit *c, const DevProgram *D, const double *dv, const double *dx, size_t stride,
+                      int n_inst, double h, int n_steps, int method, int lag, int *queue, int opts, const WaveTab &wt,
+                      const Probe &pr, int &G_out, bool &lug_out, int &how) {
+  const std::string key = dfd_tune_key(D, method);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
     if (it != g_tune.end()) {
-      G_out = it->second;
+      G_out = it->second & 0xff;
+      lug_out = (it->second >> 8) & 1;
       how = 2;
       return KRETS_OK;
     }
   }
   G_out = 128;
+  lug_out = false;
   how = 0;
   const int steps = std::min(n_steps, 128);
   if (steps < 16) return KRETS_OK;
-  DfdLaunch L0;
-  krets_status s = dfd_config(128, DL, L0);
-  if (s != KRETS_OK) return s;
-  const int n = D->host.n;
-  const int trial = std::max(1, std::min(n_inst, L0.W * L0.per_sm * device_sm_count()));
-  DevBuf tout, tst;
-  const size_t row = sizeof(double) * (pr.n ? pr.n : n) * ((size_t)steps + 1);
-  CU(cudaMalloc(&tout.p, row * trial));
-  CU(cudaMalloc(&tst.p, sizeof(int) * trial));
-  // the trial instances start from their operating points (row 0 of each waveform, or
-  // the probe run's separate operating points)
-  if (!pr.n && !pr.x0)
-    CU(cudaMemcpy2DAsync(tout.p, row, dx, sizeof(double) * stride, sizeof(double) * n, trial,
-                         cudaMemcpyDeviceToDevice, c->stream));
-  double best = 0.0;
-  for (int G : {128, 64, 32}) {
+  const DevProg &P = D->view;
+  struct Cand { int G; bool lug; };
+  const Cand cands[] = {{128, false}, {64, false}, {32, false}, {128, true}, {64, true}};
+  std::vector<DfdLaunch> cfg;
+  std::vector<DfdLay> lay;
+  int trial_max = 1;
+  for (const Cand &cd : cands) {
+    DfdLay DL{};
     DfdLaunch Lc;
-    if (dfd_config(G, DL, Lc) != KRETS_OK) {
+    if (!dfd_layout(P, DL, cd.lug) || dfd_config(cd.G, cd.lug, DL, Lc) != KRETS_OK) {
       cudaGetLastError();
       continue;
     }
+    cfg.push_back(Lc);
+    lay.push_back(DL);
+    trial_max = std::max(trial_max, std::min(n_inst, Lc.slots()));
+  }
+  const int n = D->host.n;
+  DevBuf tout, tst;
+  const size_t row = sizeof(double) * (pr.n ? pr.n : n) * ((size_t)steps + 1);
+  CU(cudaMalloc(&tout.p, row * trial_max));
+  CU(cudaMalloc(&tst.p, sizeof(int) * trial_max));
+  // the trial instances start from their operating points (row 0 of each waveform, or
+  // the probe run's separate operating points)
+  if (!pr.n && !pr.x0)
+    CU(cudaMemcpy2DAsync(tout.p, row, dx, sizeof(double) * stride, sizeof(double) * n, trial_max,
+                         cudaMemcpyDeviceToDevice, c->stream));
+  double best = 0.0;
+  for (size_t i = 0; i < cfg.size(); ++i) {
+    const DfdLaunch &Lc = cfg[i];
+    const int trial = std::max(1, std::min(n_inst, Lc.slots()));
     const int grid = std::max(1, std::min((trial + Lc.W - 1) / Lc.W, Lc.per_sm * device_sm_count()));
+    df *lug = nullptr;
+    krets_status s = dfd_lu_buffer(c, Lc, grid, P, &lug);
+    if (s != KRETS_OK) return s;
     CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
     CU(cudaEventRecord(c->ev[2], c->stream));
-    Lc.kd<<<grid, G * Lc.W, Lc.smem, c->stream>>>(D->view, c->cfg, DL, dv, trial, h, steps, method, lag,
-                                                  (double *)tout.p, (int *)tst.p, queue, opts, wt, pr,
-                                                  AdjFwd{nullptr, 1, 0, 0, nullptr}, kWholeRun);
+    Lc.kd<<<grid, Lc.G * Lc.W, Lc.smem, c->stream>>>(D->view, c->cfg, lay[i], dv, trial, h, steps, method, lag,
+                                                     (double *)tout.p, (int *)tst.p, queue, opts, wt, pr,
+                                                     AdjFwd{nullptr, 1, 0, 0, nullptr}, kWholeRun, lug);
     g_launches++;
     CU(cudaGetLastError());
     CU(cudaEventRecord(c->ev[3], c->stream));
     CU(cudaEventSynchronize(c->ev[3]));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
-    const double rate = ms > 0.f ? (double)trial * steps / ms : 0.0;
-    if (rate > best) {
-      best = rate;
-      G_out = G;
+    const double waves = std::ceil((double)n_inst / std::max(1, Lc.slots()));
+    const double predicted = waves * ms;  // the whole batch, for these steps
+    if (ms > 0.f && (best == 0.0 || predicted < best)) {
+      best = predicted;
+      G_out = Lc.G;
+      lug_out = Lc.lug;
     }
   }
   how = 1;
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  g_tune[key] = G_out;
+  g_tune[key] = G_out | (lug_out ? 1 << 8 : 0);
   return KRETS_OK;
 }
 
 // Group size of the double-float engine without a trial run: KRETS_GROUP, else the
-// autotuner's cached choice for this sparsity signature, else the default 128.
+// autotuner's cached choice for this sparsity signature, else the default 128.  (The
+// place of the factors does not change the arithmetic, only the group size does.)
 int dfd_cached_group(const DevProgram *D, int method, int &how) {
   const char *genv = getenv("KRETS_GROUP");
   how = 0;
@@ -1155,14 +1233,12 @@ int dfd_cached_group(const DevProgram *D, int method, int &how) {
     const int G = atoi(genv);
     return (G == 32 || G == 64 || G == 128) ? G : 128;
   }
-  char key[96];
-  snprintf(key, sizeof key, "%016llx/%d/%zu/%d", (unsigned long long)D->host.signature, D->host.n,
-           D->host.lu_col.size(), method);
+  const std::string key = dfd_tune_key(D, method);
   std::lock_guard<std::mutex> lk(g_tune_mu);
   auto it = g_tune.find(key);
   if (it == g_tune.end()) return 128;
   how = 2;
-  return it->second;
+  return it->second & 0xff;
 }
 
 // Shared-memory layout of one warp of the warp engine (k_tran_warp, k_tran_warp_df);
@@ -1229,15 +1305,22 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
   // double-float direct: one instance per group of G threads (default 128); it stages only
   // the step-program words before the residual operators, so it fits where the warp
   // engine may not
-  DfdLay DL{};
-  const bool use_dfd = precision == KRETS_PREC_DF && !P.nonlinear && P.sprog_ok && !block_forced && dfd_layout(P, DL);
+  DfdLay DL{}, DLg{};
+  const bool dfd_smem = dfd_layout(P, DL), dfd_glob = dfd_layout(P, DLg, true);
+  const bool use_dfd = precision == KRETS_PREC_DF && !P.nonlinear && P.sprog_ok && !block_forced && (dfd_smem || dfd_glob);
   // Host output of the double-float engine is staged: the transient runs as spans of
   // steps, each written to a device staging buffer and copied into the caller's rows by
-  // one strided copy on a second stream while the next span runs (KRETS_HOST_OUT=inplace
-  // keeps the kernel writing host memory directly where the GPU can).
+  // one strided copy on a second stream while the next span runs.  That is the path for
+  // pinned host buffers, and for any host buffer where the GPU cannot write host memory
+  // in place; pageable buffers on a GPU that shares the host's page tables are written in
+  // place by the kernel, which measured faster for them.  KRETS_HOST_OUT=inplace|staged
+  // forces either.
   const char *hout = getenv("KRETS_HOST_OUT");
-  const bool staged = use_dfd && n_probe <= 0 && n_steps >= 2 && !is_device_ptr(x_out) &&
-                      !(hout && strcmp(hout, "inplace") == 0) &&
+  const size_t out_bytes = sizeof(double) * (size_t)(n_probe > 0 ? n_probe : c->n) * ((size_t)n_steps + 1) * n_inst;
+  const bool host_out = !is_device_ptr(x_out);
+  bool want_staged = host_out && (!direct_host_access() || is_pinned_host(x_out, out_bytes));
+  if (hout) want_staged = host_out && strcmp(hout, "staged") == 0;
+  const bool staged = want_staged && use_dfd && n_probe <= 0 && n_steps >= 2 &&
                       sizeof(double) * (size_t)c->n * ((size_t)n_steps + 1) < ((size_t)1 << 31);  // copy pitch
   CU(cudaEventRecord(c->ev[0], c->stream));
   const int n_out = n_probe > 0 ? n_probe : c->n;
@@ -1314,34 +1397,43 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
       wt.row = d_wrow;
     }
     const char *oenv = getenv("KRETS_DFD_OPTS");
-    const int opts = oenv ? atoi(oenv) : 0;
-    const char *genv = getenv("KRETS_GROUP");
+    const int opts = oenv ? atoi(oenv) : kDfdDefaultOpts;
+    // group size and place of the factors: KRETS_GROUP / KRETS_DFD_LU (smem | global),
+    // else the autotuner
+    const char *genv = getenv("KRETS_GROUP"), *lenv = getenv("KRETS_DFD_LU");
     int G = 128, how = 0;
-    if (genv) {
-      G = atoi(genv);
+    bool lug = !dfd_smem;
+    if (genv || lenv) {
+      if (genv) G = atoi(genv);
       if (G != 32 && G != 64 && G != 128) G = 128;
+      if (lenv) lug = strcmp(lenv, "global") == 0 || !dfd_smem;
     } else {
-      s = dfd_pick_group(c, Dtr, DL, (const double *)dv, (const double *)dx, stride, n_inst, h, n_steps, method,
-                         source_lag, queue, opts, wt, pr, G, how);
+      s = dfd_pick(c, Dtr, (const double *)dv, (const double *)dx, stride, n_inst, h, n_steps, method, source_lag,
+                   queue, opts, wt, pr, G, lug, how);
       if (s != KRETS_OK) return s;
     }
+    if (lug) DL = DLg;
     DfdLaunch Lc;
-    s = dfd_config(G, DL, Lc);
+    s = dfd_config(G, lug, DL, Lc);
     if (s != KRETS_OK) return s;
     const int W = Lc.W;
     int grid = std::max(1, std::min((n_inst + W - 1) / W, Lc.per_sm * device_sm_count()));
+    df *lu_glob = nullptr;
+    s = dfd_lu_buffer(c, Lc, grid, P, &lu_glob);
+    if (s != KRETS_OK) return s;
     c->warps_per_cta = W * G / 32;
     c->grid = grid;
     c->launch_info[0] = G;
     c->launch_info[1] = W;
     c->launch_info[2] = grid;
     c->launch_info[3] = how;
+    c->launch_info[4] = lug ? 1 : 0;
     if (!staged) {
       CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
       CU(cudaEventRecord(c->ev[2], c->stream));
       Lc.kd<<<grid, G * W, Lc.smem, c->stream>>>(P, c->cfg, DL, (const double *)dv, n_inst, h, n_steps, method,
                                                  source_lag, (double *)dx, d_st, queue, opts, wt, pr,
-                                                 AdjFwd{nullptr, 1, 0, 0, nullptr}, kWholeRun);
+                                                 AdjFwd{nullptr, 1, 0, 0, nullptr}, kWholeRun, lu_glob);
     } else {
       // spans of R steps; two staging buffers of n_inst x R rows (KRETS_STAGE_MB each,
       // default 2048), at least 8 spans
@@ -1363,7 +1455,7 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
         Lc.kd<<<grid, G * W, Lc.smem, c->stream>>>(P, c->cfg, DL, (const double *)dv, n_inst, h, s1, method,
                                                    source_lag, stage[j & 1], d_st, queue, opts, wt, pr,
                                                    AdjFwd{nullptr, 1, 0, 0, nullptr},
-                                                   Span{s0, s0, (long long)R * c->n, (df *)tstate.p});
+                                                   Span{s0, s0, (long long)R * c->n, (df *)tstate.p}, lu_glob);
         g_launches++;
         CU(cudaGetLastError());
         CU(cudaEventRecord(kdone[j & 1], c->stream));
@@ -1651,13 +1743,13 @@ krets_status krets_adjoint_tran(krets_circuit *c, int32_t n_inst, const double *
   CU(cudaEventRecord(c->ev[2], c->stream));
   if (split) {
     DfdLaunch Lf;
-    s = dfd_config(128, DL, Lf);
+    s = dfd_config(128, false, DL, Lf);
     if (s != KRETS_OK) return s;
     const int fgrid = std::max(1, std::min((n_inst + Lf.W - 1) / Lf.W, Lf.per_sm * device_sm_count()));
     const AdjFwd af{(df *)tck.p, K, P.n + P.ncap, H.qinv[out_unknown], (double *)d_loss};
     Lf.kd<<<fgrid, 128 * Lf.W, Lf.smem, c->stream>>>(P, c->cfg, DL, (const double *)dv, n_inst, h, n_steps, method,
                                                      0, nullptr, (int *)tstf.p, queue, 0, wt,
-                                                     Probe{nullptr, 0, nullptr}, af, kWholeRun);
+                                                     Probe{nullptr, 0, nullptr}, af, kWholeRun, nullptr);
     g_launches++;
     CU(cudaGetLastError());
     CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
@@ -1712,7 +1804,7 @@ const char *krets_last_error_message(void) { return g_last_error.c_str(); }
 
 krets_status krets_last_launch(const krets_circuit *c, int32_t *info, int32_t cap) {
   if (!c || !info) return fail(KRETS_ERR_INVALID_ARGUMENT, "invalid arguments to krets_last_launch");
-  for (int i = 0; i < cap && i < 4; ++i) info[i] = c->launch_info[i];
+  for (int i = 0; i < cap && i < 5; ++i) info[i] = c->launch_info[i];
   return KRETS_OK;
 }
 
@@ -1819,6 +1911,10 @@ krets_status krets_batch_tran_noalloc(krets_circuit *c, int32_t n_inst, const do
   const bool block_forced = eng && strcmp(eng, "block") == 0;
   DfdLay DL{};
   const bool use_dfd = dfd && !P.nonlinear && P.sprog_ok && !block_forced && dfd_layout(P, DL);
+  if (dfd && !P.nonlinear && P.sprog_ok && !block_forced && !use_dfd)
+    // krets_batch_tran runs such a circuit with its factors in global memory it allocates
+    return fail(KRETS_ERR_INVALID_ARGUMENT, "krets_batch_tran_noalloc: circuit too large for the shared-memory "
+                                            "double-float engine");
   WarpLay WL{};
   const size_t per_warp = warp_layout(P, mixed, WL);
   const bool warp_engine = !use_dfd && !block_forced && P.sprog_ok && per_warp + WL.sprog_bytes <= max_smem_optin();
@@ -1874,11 +1970,11 @@ krets_status krets_batch_tran_noalloc(krets_circuit *c, int32_t n_inst, const do
       wt.row = d_wrow;
     }
     const char *oenv = getenv("KRETS_DFD_OPTS");
-    const int opts = oenv ? atoi(oenv) : 0;
+    const int opts = oenv ? atoi(oenv) : kDfdDefaultOpts;
     int how = 0;
     const int G = dfd_cached_group(Dtr, method, how);  // never a trial run: it would allocate
     DfdLaunch Lc;
-    s = dfd_config(G, DL, Lc);
+    s = dfd_config(G, false, DL, Lc);
     if (s != KRETS_OK) return s;
     const int grid = std::max(1, std::min((n_inst + Lc.W - 1) / Lc.W, Lc.per_sm * device_sm_count()));
     c->warps_per_cta = Lc.W * G / 32;
@@ -1887,10 +1983,11 @@ krets_status krets_batch_tran_noalloc(krets_circuit *c, int32_t n_inst, const do
     c->launch_info[1] = Lc.W;
     c->launch_info[2] = grid;
     c->launch_info[3] = how;
+    c->launch_info[4] = 0;
     CU(cudaEventRecord(c->ev[2], c->stream));
     Lc.kd<<<grid, G * Lc.W, Lc.smem, c->stream>>>(P, c->cfg, DL, d_values, n_inst, h, n_steps, method, source_lag,
                                                   d_x_out, d_inst_status, queue, opts, wt, Probe{nullptr, 0, nullptr},
-                                                  AdjFwd{nullptr, 1, 0, 0, nullptr}, kWholeRun);
+                                                  AdjFwd{nullptr, 1, 0, 0, nullptr}, kWholeRun, nullptr);
   } else {
     const int W = warp_engine_width(WL, per_warp);
     const size_t smem = WL.sprog_bytes + (size_t)W * per_warp;

@@ -264,18 +264,31 @@ uint64_t fnv1a(uint64_t h, uint64_t v) {
 
 // ------------------------------------------------------------------ orderings
 std::vector<int> order_min_degree(int n, const std::vector<std::vector<int>> &adj0) {
+  // Explicit elimination graph; the next vertex is the one of least current degree, the
+  // smallest index among equals, found through a min-heap of (degree, vertex) entries
+  // whose stale entries (a vertex's degree changed since) are skipped when they surface.
   std::vector<std::vector<int>> adj = adj0;
   std::vector<char> gone(n, 0);
   std::vector<int> order;
   order.reserve(n);
+  using Key = std::pair<int, int>;
+  std::priority_queue<Key, std::vector<Key>, std::greater<Key>> heap;
+  for (int v = 0; v < n; ++v) heap.push({(int)adj[v].size(), v});
+  std::vector<int> merged;
   for (int step = 0; step < n; ++step) {
     int best = -1;
-    size_t bd = 0;
-    for (int v = 0; v < n; ++v)
-      if (!gone[v] && (best < 0 || adj[v].size() < bd)) { best = v; bd = adj[v].size(); }
+    while (!heap.empty()) {
+      const Key top = heap.top();
+      heap.pop();
+      if (!gone[top.second] && (int)adj[top.second].size() == top.first) {
+        best = top.second;
+        break;
+      }
+    }
+    const size_t bd = adj[best].size();
     if (bd + 1 == (size_t)(n - step)) {
       // every remaining vertex is adjacent to all others: a clique, whose vertices the
-      // selection above would take in increasing index order (equal degrees throughout)
+      // selection would take in increasing index order (equal degrees throughout)
       for (int v = 0; v < n; ++v)
         if (!gone[v]) order.push_back(v);
       break;
@@ -284,12 +297,14 @@ std::vector<int> order_min_degree(int n, const std::vector<std::vector<int>> &ad
     order.push_back(best);
     const std::vector<int> nb = adj[best];
     for (int u : nb) {
-      std::vector<int> merged;
+      merged.clear();
       merged.reserve(adj[u].size() + nb.size());
       std::set_union(adj[u].begin(), adj[u].end(), nb.begin(), nb.end(), std::back_inserter(merged));
       merged.erase(std::remove_if(merged.begin(), merged.end(), [&](int w) { return w == u || w == best; }),
                    merged.end());
-      adj[u].swap(merged);
+      const bool changed = merged.size() != adj[u].size();
+      adj[u].assign(merged.begin(), merged.end());
+      if (changed) heap.push({(int)adj[u].size(), u});
     }
     adj[best].clear();
   }

@@ -1247,7 +1247,9 @@ __device__ __forceinline__ void df_border(const SProg &S, const df *__restrict__
   gsync<G>(gid);
 }
 
-template <int G, bool UPPER, int SG = G>
+// TAIL: the program may have a dense trailing block (multi-circuit programs); the
+// single-topology engines compile without that code.
+template <int G, bool UPPER, int SG = G, bool TAIL = true>
 __device__ __forceinline__ void df_solve(const SProg &S, const df *__restrict__ lu, df *y, int gl, int gid, int nar) {
   const int nl = UPPER ? S.nulev : S.nlev;
   const int *ptr = UPPER ? S.ulev_ptr : S.lev_ptr;
@@ -1255,15 +1257,15 @@ __device__ __forceinline__ void df_solve(const SProg &S, const df *__restrict__ 
   const int *mx = UPPER ? S.umax : S.lmax;
   const bool w0 = gl < 32;
   if (nar < 0) {  // no narrow-level split: every level on the whole group
-    if (UPPER && S.tail_m) df_dense_upper<G>(S, lu, y, gl, gid);
-    if (UPPER && S.n_brow) df_border<G>(S, lu, y, gl, gid);
+    if (TAIL && UPPER && S.tail_m) df_dense_upper<G>(S, lu, y, gl, gid);
+    if (TAIL && UPPER && S.n_brow) df_border<G>(S, lu, y, gl, gid);
     for (int l = UPPER ? 0 : 1; l < nl; ++l) {
       const int spl = split_lanes<SG>(mx[l]);
       if (spl > 1) df_level_split<UPPER>(S, lu, y, ptr, desc, l, gl, G, spl);
       else df_level<G, UPPER>(S, lu, y, ptr, desc, l, gl, G);
       gsync<G>(gid);
     }
-    if (!UPPER && S.tail_m) df_dense_lower<G>(S, lu, y, gl, gid);
+    if (TAIL && !UPPER && S.tail_m) df_dense_lower<G>(S, lu, y, gl, gid);
     return;
   }
   if (!UPPER) {
@@ -1295,7 +1297,7 @@ __device__ __forceinline__ void df_solve(const SProg &S, const df *__restrict__ 
 
 // Shared-memory layout of one instance of the double-float direct engine.
 struct DfdLay {
-  int lu;     // df[nnz_lu]
+  int lu;     // df[nnz_lu] (shared memory; unused when the factors are in global memory)
   int x;      // df[n]  (solution; the rhs is assembled and solved in place)
   int cdyn;   // df[ndyn] coefficients of the rhs elements (C/h or 2C/h, L/h or 2L/h, source values)
   int cb;     // df[ndyn] rhs coefficients of the step
@@ -1388,8 +1390,11 @@ struct AdjFwd {
 // carried from step to step as its companion current source itself, cb_n = 2 (2C/h) v_{n-1}
 // - cb_{n-1} (the same recurrence as cb_n = (2C/h) v_{n-1} + i_{n-1} with
 // i_{n-1} = (2C/h) v_{n-1} - cb_{n-1}), so the per-step pass that forms the capacitor
-// currents after the solve is not needed; icap holds the currents again on return.
-template <int G, int SG = G, bool CBREC = false>
+// currents after the solve is not needed.  On entry icap holds the capacitor currents
+// (s_begin = 1) or, resuming (s_begin > 1), the companion values a previous call left; on
+// return it holds the companion values, so a run split into spans is bit-identical to one
+// run.
+template <int G, int SG = G, bool CBREC = false, bool TAIL = true>
 __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const df *lu, df *x, const df *cdyn, df *cb,
                                          df *icap, const double *vals, double h, int n_steps, int method, int lag,
                                          double *out, int lnar, int unar, bool int_cvt, int gl, int gid,
@@ -1413,10 +1418,10 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
         pf_val = wt.tab[pf_base + s_begin];
         break;
       }
-  if (CBREC)  // companion currents of the step before s_begin (x and icap are final: the caller synced)
+  if (CBREC)  // companion values of the step before s_begin (x and icap are final: the caller synced)
     for (int d = gl; d < P.ncap; d += G) {
       const int4 dd = S.dyn[d];
-      cb[d] = df_sub(df_mul(cdyn[d], df_sub(df_at(x, dd.y), df_at(x, dd.z))), icap[d]);
+      cb[d] = s_begin > 1 ? icap[d] : df_sub(df_mul(cdyn[d], df_sub(df_at(x, dd.y), df_at(x, dd.z))), icap[d]);
     }
   for (int s = s_begin; s <= n_steps; ++s) {
     const double t = (double)s * h;
@@ -1468,8 +1473,8 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
       x[k] = acc;
     }
     gsync<G>(gid);
-    df_solve<G, false, SG>(S, lu, x, gl, gid, lnar);
-    df_solve<G, true, SG>(S, lu, x, gl, gid, unar);
+    df_solve<G, false, SG, TAIL>(S, lu, x, gl, gid, lnar);
+    df_solve<G, true, SG, TAIL>(S, lu, x, gl, gid, unar);
     if (!CBREC && method == KRETS_METHOD_TR) {
       for (int d = gl; d < P.ncap; d += G) {
         const int4 dd = S.dyn[d];
@@ -1493,13 +1498,8 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
     // orders every read of x before the gather overwrites it.  Callers synchronise the
     // group after the last step.
   }
-  if (CBREC) {  // the capacitor currents of the last step, for a caller that keeps the state
-    gsync<G>(gid);
-    for (int d = gl; d < P.ncap; d += G) {
-      const int4 dd = S.dyn[d];
-      icap[d] = df_sub(df_mul(cdyn[d], df_sub(df_at(x, dd.y), df_at(x, dd.z))), cb[d]);
-    }
-  }
+  if (CBREC)  // the companion values of the last step, for a caller that keeps the state
+    for (int d = gl; d < P.ncap; d += G) icap[d] = cb[d];
   if (af.loss && gl == 0) *af.loss = df_to_double(loss);
   return st;
 }
@@ -1509,8 +1509,9 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
 // launch runs).  Steps s_begin .. n_steps are computed; step s goes to output row
 // s - row_base of the instance, whose rows are `stride` values apart (0: (n_steps + 1)
 // rows of the output width).  With `state` ([n_inst][n + ncap] double-float: x in
-// position space, then the TR capacitor currents) a span with s_begin > 1 resumes from
-// the state the previous span saved, and every span saves its final state there.
+// position space, then the TR capacitor state: currents, or companion values when the
+// spans run with CBREC) a span with s_begin > 1 resumes from the state the previous span
+// saved, and every span saves its final state there.
 struct Span {
   int s_begin, row_base;
   long long stride;
@@ -1518,12 +1519,16 @@ struct Span {
 };
 
 // opts bit 0: run narrow levels on one warp; bit 1: integer-only FP64 output conversion;
-// bit 2: trapezoidal capacitor history as companion currents (dfd_steps CBREC)
-template <int G>
-__global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay L, const double *values, int n_inst,
+// bit 2: trapezoidal capacitor history as companion currents (dfd_steps CBREC).
+// LUG: the factors live in global memory (an L2-resident region per group, lu_glob), the
+// rest of the instance in shared memory: about a third of the shared memory per instance,
+// so up to 14 instances share an SM (each step's critical path is a chain of level
+// barriers; more instances per SM hide it, and fewer waves of instances are needed).
+template <int G, bool LUG = false>
+__global__ void __launch_bounds__(896, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay L, const double *values, int n_inst,
                                                      double h, int n_steps, int method, int lag, double *x_out,
                                                      int *inst_status, int *queue, int opts, WaveTab wt, Probe pr,
-                                                     AdjFwd af, Span sp) {
+                                                     AdjFwd af, Span sp, df *lu_glob) {
   extern __shared__ __align__(16) char smem[];
   const int gl = threadIdx.x % G, gid = threadIdx.x / G;
   {
@@ -1542,8 +1547,9 @@ __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
   // bit 2: trapezoidal capacitor history carried as the companion current (no adjoint pass)
   const bool cbrec = (opts & 4) != 0 && method == KRETS_METHOD_TR && !af.ck;
   char *base = smem + L.sprog_bytes + (size_t)gid * L.bytes;
-  df *lu = reinterpret_cast<df *>(base + L.lu);
-  double *lu64 = reinterpret_cast<double *>(base + L.lu);  // same bytes, set-up only
+  df *lu = LUG ? lu_glob + (size_t)(blockIdx.x * (blockDim.x / G) + gid) * P.nnz_lu
+               : reinterpret_cast<df *>(base + L.lu);
+  double *lu64 = reinterpret_cast<double *>(lu);  // same bytes, set-up only
   df *x = reinterpret_cast<df *>(base + L.x);
   df *cdyn = reinterpret_cast<df *>(base + L.cdyn);
   df *cb = reinterpret_cast<df *>(base + L.cb);
@@ -1579,11 +1585,11 @@ __global__ void __launch_bounds__(640, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
     const bool fatal = gany<G>((st & (KS_SINGULAR | KS_NONFINITE | KS_NOTIMPL)) != 0, gid);
     if (!fatal) {
       if (cbrec)
-        st |= dfd_steps<G, G, true>(P, S, lu, x, cdyn, cb, icap, vals, h, n_steps, method, lag, out, lnar, unar,
+        st |= dfd_steps<G, G, true, false>(P, S, lu, x, cdyn, cb, icap, vals, h, n_steps, method, lag, out, lnar, unar,
                                     int_cvt, gl, gid, wt, pr, a, sp.s_begin, sp.row_base);
       else
-        st |= dfd_steps<G>(P, S, lu, x, cdyn, cb, icap, vals, h, n_steps, method, lag, out, lnar, unar, int_cvt, gl,
-                           gid, wt, pr, a, sp.s_begin, sp.row_base);
+        st |= dfd_steps<G, G, false, false>(P, S, lu, x, cdyn, cb, icap, vals, h, n_steps, method, lag, out, lnar,
+                                            unar, int_cvt, gl, gid, wt, pr, a, sp.s_begin, sp.row_base);
     }
     if (state) {  // the last step's solution level and TR currents are final once the group syncs
       gsync<G>(gid);

@@ -3,7 +3,10 @@ the device at most), run as
 
     python -m krets_gb300.profile_cases tran|multi|adjoint|kernels|op
 
-  tran     k_tran_dfd: 304 instances of the 200-section RLC ladder, TR 1 ps, 1000 steps
+  tran     k_tran_dfd: 2048 instances of the 200-section RLC ladder, TR 1 ps, 200 steps,
+           the configuration the autotuner picks for it on GB300 (64 threads per instance,
+           factors in global memory, 14 instances per SM: one wave), fixed here so that the
+           first k_tran_dfd launch is the measured one
   multi    k_multi_tran (global class): the 152 largest of the first 600 uneven
            netlists, operating point + 100 BE steps at 1 ns
   adjoint  k_adjoint_dfd: 152 instances of the 1000-section RC ladder, TR 1 ns,
@@ -26,9 +29,12 @@ from . import _lib
 def tran():
     from .generators import monte_carlo_values, rlc_ladder
     from .table import element_table
+    import os
+    os.environ.setdefault("KRETS_GROUP", "64")
+    os.environ.setdefault("KRETS_DFD_LU", "global")
     c = rlc_ladder(200)
     t = element_table(c)
-    n_inst, steps = 304, 1000
+    n_inst, steps = 2048, 200
     vals = monte_carlo_values(c, n_inst, sigma=0.1, seed=3)
     g = _lib.GpuCircuit(t, c.size)
     out = _lib.DeviceArray((n_inst, steps + 1, c.size))

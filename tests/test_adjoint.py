@@ -160,3 +160,23 @@ def test_adjoint_single_kernel_form_agrees(monkeypatch):
     l_one, g_one = g.adjoint_tran(vals, 1e-9, 400, out, method="tr", checkpoint_every=64)
     assert np.max(np.abs(l_split - l_one) / np.abs(l_one)) < 1e-12
     assert np.max(np.abs(g_split - g_one)) <= 1e-12 * np.max(np.abs(g_one))
+
+
+def test_adjoint_150_section_ladder_against_central_differences_1e4(oracle_lib):
+    """A 150-section RC ladder (seeded per-instance values, TR 1 ns, 400 steps, loss at
+    V(n20)): the device gradient of every R and C against central differences of the FP64
+    oracle loss at a relative step of 1e-4, where the differences are accurate to ~1e-9
+    (at 1e-6 they are limited by the FP64 loss's own rounding), to 1e-6 relative."""
+    from krets_gb300.generators import rc_ladder_step_values
+    c = rc_ladder_step(150)
+    t = element_table(c)
+    out = c.index_map["V(n20)"]
+    vals = rc_ladder_step_values(c, 3, seed=11)
+    g = _lib.GpuCircuit(t, c.size)
+    loss, grad = g.adjoint_tran(vals, 1e-9, 400, out, checkpoint_every=50)
+    for i in (0, 2):
+        fd = _fd_grad(oracle_lib, t, c.size, vals[i], 1e-9, 400, "tr", out, rel=1e-4)
+        rc = np.isin(t["kind"], (1, 2))
+        err = np.max(np.abs(grad[i][rc] - fd[rc])) / np.max(np.abs(fd[rc]))
+        assert err < GRAD_TOL, (i, err)
+        assert abs(loss[i] - _oracle_loss(oracle_lib, t, c.size, vals[i], 1e-9, 400, "tr", out)) <= LOSS_TOL * loss[i]
