@@ -27,7 +27,8 @@ MODE_DC, MODE_AC, MODE_TRAN = 0, 1, 2
 
 PROG_ARRAYS = ["q", "prow", "lu_rowptr", "lu_col", "lu_diag", "a_rowptr", "a_col", "a_slot", "a_cptr",
                "a_contrib", "b_cptr", "b_contrib", "piv_ptr", "piv", "upd", "lev_ptr", "lev_rows",
-               "ulev_ptr", "ulev_rows", "el_pos", "meta", "tprog", "tpoff", "sprog", "spoff"]
+               "ulev_ptr", "ulev_rows", "el_pos", "meta", "tprog", "tpoff", "sprog", "spoff", "iprog", "ipoff",
+               "imap"]
 
 _EXC = {
     ELEMENT_NOT_FOUND: E.ElementNotFound, MAX_ITERATIONS: E.MaximumIterationsExceeded,

@@ -247,7 +247,7 @@ static void for_each_array(const Program &H, const ProgramImage &X, F &&f) {
   f(H.el_pos); f(X.is_cur);
   f(H.qinv); f(H.ldesc); f(H.udesc); f(H.res_ptr); f(H.res_op);
   f(H.dyn_e); f(H.bd_ptr); f(H.bd_op); f(H.sprog);
-  f(H.tprog); f(H.prow); f(H.xslot);
+  f(H.tprog); f(H.prow); f(H.xslot); f(H.iprog); f(H.imap);
 }
 
 static size_t program_bytes(const Program &H, const ProgramImage &X) {
@@ -307,6 +307,16 @@ static void place_program(const Program &H, const ProgramImage &X, const krets_e
   V.tprog = (const int *)nx();
   V.prow = (const int *)nx();
   V.xslot = (const int *)nx();
+  V.iprog = (const int *)nx();
+  V.imap = (const int *)nx();
+  for (int gi = 0; gi < 2; ++gi) {
+    for (int k = 0; k < 4; ++k) V.ip_off[gi][k] = H.ip_off[gi][k];
+    V.il_slots[gi] = H.il_slots[gi];
+    V.imap_off[gi] = H.imap_off[gi];
+  }
+  V.n_il_lrec = H.n_il_lrec;
+  V.n_il_urec = H.n_il_urec;
+  V.il_ok = H.il_ok ? 1 : 0;
   V.n_coef = H.n_coef;
   V.el = d_el;
   V.ndyn = (int)H.dyn_e.size();
@@ -1079,9 +1089,14 @@ struct DfdLaunch {
   int slots() const { return W * per_sm * device_sm_count(); }
 };
 
+// Interleaved solves: factors in global memory, a 64 or 128-thread group, and a program
+// that has them (k_tran_dfd).
+bool dfd_interleaved(const DevProg &P, bool lug, int G) { return lug && (G == 64 || G == 128) && P.il_ok; }
+
 // Shared-memory layout of one double-float instance (without the factors when lug: they
-// are then in global memory); false when it does not fit a CTA.
-bool dfd_layout(const DevProg &P, DfdLay &DL, bool lug = false) {
+// are then in global memory); false when it does not fit a CTA.  G matters only with lug
+// (the staged program then depends on it).
+bool dfd_layout(const DevProg &P, DfdLay &DL, bool lug = false, int G = 64) {
   size_t cur = 0;
   auto put = [&](int &off, size_t bytes) { off = (int)cur; cur = align16(cur + bytes); };
   if (lug) DL.lu = 0;
@@ -1094,7 +1109,13 @@ bool dfd_layout(const DevProg &P, DfdLay &DL, bool lug = false) {
   if (cur - DL.x < 8 * (size_t)P.ne) cur = DL.x + align16(8 * (size_t)P.ne);
   put(DL.slot, 16);
   DL.bytes = (int)align16(cur);
-  DL.sprog_bytes = (int)align16((size_t)P.sp_off[5] * sizeof(int));
+  if (dfd_interleaved(P, lug, G)) {  // rhs / gather / output sections, then the interleaved program
+    const int gi = G == 128 ? 1 : 0;
+    DL.sprog_bytes = (int)(align16((size_t)(P.sp_off[5] - P.sp_off[7]) * sizeof(int)) +
+                           align16((size_t)(P.ip_off[gi][3] - P.ip_off[gi][0]) * sizeof(int)));
+  } else {
+    DL.sprog_bytes = (int)align16((size_t)P.sp_off[5] * sizeof(int));
+  }
   return (size_t)DL.bytes + DL.sprog_bytes <= max_smem_optin();
 }
 
@@ -1120,7 +1141,9 @@ krets_status dfd_config(int G, bool lug, const DfdLay &DL, DfdLaunch &Lc) {
 krets_status dfd_lu_buffer(krets_circuit *c, const DfdLaunch &Lc, int grid, const DevProg &P, df **out) {
   *out = nullptr;
   if (!Lc.lug) return KRETS_OK;
-  const size_t bytes = sizeof(df) * (size_t)P.nnz_lu * grid * Lc.W;
+  // per group: the CSR factors, then (interleaved solves) their interleaved copy
+  const size_t per = (size_t)P.nnz_lu + (dfd_interleaved(P, true, Lc.G) ? (size_t)P.il_slots[Lc.G == 128 ? 1 : 0] : 0);
+  const size_t bytes = sizeof(df) * per * grid * Lc.W;
   krets_status s = c->ensure_lug(bytes);
   if (s != KRETS_OK) return s;
   *out = (df *)c->lug;
@@ -1158,11 +1181,6 @@ krets_status dfd_pick(krets_circuit *c, const DevProgram *D, const double *dv, c
       return KRETS_OK;
     }
   }
-  G_out = 128;
-  lug_out = false;
-  how = 0;
-  const int steps = std::min(n_steps, 128);
-  if (steps < 16) return KRETS_OK;
   const DevProg &P = D->view;
   struct Cand { int G; bool lug; };
   const Cand cands[] = {{128, false}, {64, false}, {32, false}, {128, true}, {64, true}};
@@ -1172,7 +1190,7 @@ krets_status dfd_pick(krets_circuit *c, const DevProgram *D, const double *dv, c
   for (const Cand &cd : cands) {
     DfdLay DL{};
     DfdLaunch Lc;
-    if (!dfd_layout(P, DL, cd.lug) || dfd_config(cd.G, cd.lug, DL, Lc) != KRETS_OK) {
+    if (!dfd_layout(P, DL, cd.lug, cd.G) || dfd_config(cd.G, cd.lug, DL, Lc) != KRETS_OK) {
       cudaGetLastError();
       continue;
     }
@@ -1180,6 +1198,13 @@ krets_status dfd_pick(krets_circuit *c, const DevProgram *D, const double *dv, c
     lay.push_back(DL);
     trial_max = std::max(trial_max, std::min(n_inst, Lc.slots()));
   }
+  if (cfg.empty()) return fail(KRETS_ERR_INVALID_ARGUMENT, "double-float engine: no layout fits");
+  // default (too few steps to time): the first candidate that fits
+  G_out = cfg[0].G;
+  lug_out = cfg[0].lug;
+  how = 0;
+  const int steps = std::min(n_steps, 128);
+  if (steps < 16) return KRETS_OK;
   const int n = D->host.n;
   DevBuf tout, tst;
   const size_t row = sizeof(double) * (pr.n ? pr.n : n) * ((size_t)steps + 1);
@@ -1412,7 +1437,7 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
                    queue, opts, wt, pr, G, lug, how);
       if (s != KRETS_OK) return s;
     }
-    if (lug) DL = DLg;
+    if (lug && !dfd_layout(P, DL, true, G)) return fail(KRETS_ERR_INVALID_ARGUMENT, "double-float layout does not fit");
     DfdLaunch Lc;
     s = dfd_config(G, lug, DL, Lc);
     if (s != KRETS_OK) return s;

@@ -28,6 +28,26 @@ __device__ __forceinline__ df df_from_double(double v) {
 
 __device__ __forceinline__ double df_to_double(df a) { return (double)a.hi + (double)a.lo; }
 
+// The same value with one FP64 instruction instead of three: a normal FP32 number widens to
+// FP64 exactly by moving its fields (exponent rebased from 127 to 1023, significand shifted
+// up 29 bits), so both parts are widened with integer instructions and only their sum runs
+// on the FP64 pipe (a small fraction of the FP32 rate on this GPU).  Zero, subnormal and
+// non-finite parts take the FP64 conversions; the result is bit-identical to df_to_double.
+__device__ __forceinline__ double f32_widened(unsigned u) {
+  const unsigned long long e = (u >> 23) & 0xff;
+  return __longlong_as_double(((unsigned long long)(u >> 31) << 63) | ((e + 896ull) << 52) |
+                              ((unsigned long long)(u & 0x7fffff) << 29));
+}
+
+__device__ __forceinline__ double df_to_double_fast(df a) {
+  const unsigned hb = __float_as_uint(a.hi), lb = __float_as_uint(a.lo);
+  const unsigned he = (hb >> 23) & 0xff, le = (lb >> 23) & 0xff;
+  const bool lo_zero = (lb & 0x7fffffff) == 0;
+  if (he != 0 && he != 0xff && (lo_zero || (le != 0 && le != 0xff)))
+    return f32_widened(hb) + (lo_zero ? 0.0 : f32_widened(lb));
+  return df_to_double(a);
+}
+
 // hi + lo correctly rounded to FP64 with integer instructions only (no FP64 pipe).
 // Both parts are exact binary fractions.  The sum is formed as a signed integer in units of
 // 2^-32 ulp(hi): 24 + 32 bits hold hi and every bit of lo that can reach the 53-bit result,

@@ -113,6 +113,9 @@ struct DevProg {
   int n_utlev, n_ltlev;
   const int *prow;  // [n] position -> pivot row (unknown index of the row)
   int tail0, tail_m;  // dense trailing block of the LU (tail_m = 0: none)
+  // interleaved solves (Program::iprog; layouts for 64 and 128-thread groups)
+  const int *iprog, *imap;
+  int ip_off[2][4], il_slots[2], imap_off[2], n_il_lrec, n_il_urec, il_ok;
 };
 
 // status bits written by the engine

@@ -453,6 +453,76 @@ static int split_code(int rows, int mx) {
   return code;
 }
 
+// Interleaved ("ELL per level") form of the L and U solves for the double-float engine
+// with its factors in global memory.  Within a level, lane lam of the level's W = rows x
+// lanes-per-row lanes handles row lam / spl and its entries j = lam % spl + i * spl; entry
+// slot i of every lane of the level is stored contiguously (slot base + i * W + lam), so a
+// warp's loads of one slot are consecutive addresses, and so are the columns in shared
+// memory.  Lanes with fewer entries than the level's longest are padded with zero
+// entries, which leave the double-float sums unchanged bit for bit; the entries of a row
+// are visited in the same order as by the row-descriptor solves (df_level,
+// df_level_split), so both forms give identical results.  Lanes per row are the split of
+// the row-descriptor program for the group size (split_code).
+static void pack_interleaved(Program &P) {
+  P.iprog.clear();
+  P.imap.clear();
+  P.il_ok = false;
+  if (!P.sprog_ok || P.tail_m || P.n > 65535) return;
+  const int *lmax = P.sprog.data() + P.sp_off[12], *umax = P.sprog.data() + P.sp_off[13];
+  const int nlev = (int)P.lev_ptr.size() - 1, nulev = (int)P.ulev_ptr.size() - 1;
+  for (int gi = 0; gi < 2; ++gi) {
+    const int g = gi == 0 ? 1 : 2;  // split-code field of 64 / 128-thread groups
+    std::vector<int> rec, rows;
+    std::vector<unsigned short> cols;
+    const int mbase = (int)P.imap.size();
+    int slots = 0;
+    auto level = [&](bool upper, int l) {
+      const int *ptr = upper ? P.ulev_ptr.data() : P.lev_ptr.data();
+      const int *rw = upper ? P.ulev_rows.data() : P.lev_rows.data();
+      const int code = upper ? umax[l] : lmax[l];
+      const int spl = 1 << ((code >> (3 * g)) & 7);
+      const int nr = ptr[l + 1] - ptr[l], W = nr * spl;
+      auto first = [&](int k) { return upper ? P.lu_diag[k] + 1 : P.lu_rowptr[k]; };
+      auto count = [&](int k) { return upper ? P.lu_rowptr[k + 1] - P.lu_diag[k] - 1 : P.lu_diag[k] - P.lu_rowptr[k]; };
+      int mc = 0;
+      for (int t = ptr[l]; t < ptr[l + 1]; ++t) mc = std::max(mc, (count(rw[t]) + spl - 1) / spl);
+      rec.insert(rec.end(), {W, spl, mc, slots, (int)cols.size(), (int)rows.size(), upper ? slots + mc * W : -1, 0});
+      for (int i = 0; i < mc; ++i)
+        for (int lam = 0; lam < W; ++lam) {
+          const int k = rw[ptr[l] + lam / spl], j = lam % spl + i * spl;
+          const bool real = j < count(k);
+          P.imap.push_back(real ? first(k) + j : -1);
+          cols.push_back((unsigned short)(real ? P.lu_col[first(k) + j] : k));
+        }
+      slots += mc * W;
+      for (int t = ptr[l]; t < ptr[l + 1]; ++t) rows.push_back(rw[t]);
+      if (upper) {  // reciprocal diagonals of the level's rows
+        for (int t = ptr[l]; t < ptr[l + 1]; ++t) P.imap.push_back(P.lu_diag[rw[t]]);
+        slots += nr;
+      }
+    };
+    for (int l = 1; l < nlev; ++l) level(false, l);  // L level 0 rows have no L entries
+    for (int l = 0; l < nulev; ++l) level(true, l);
+    P.n_il_lrec = std::max(0, nlev - 1);
+    P.n_il_urec = nulev;
+    P.il_slots[gi] = slots;
+    P.imap_off[gi] = mbase;
+    while (P.iprog.size() % 4) P.iprog.push_back(0);
+    P.ip_off[gi][0] = (int)P.iprog.size();
+    P.iprog.insert(P.iprog.end(), rec.begin(), rec.end());
+    while (P.iprog.size() % 4) P.iprog.push_back(0);
+    P.ip_off[gi][1] = (int)P.iprog.size();
+    P.iprog.insert(P.iprog.end(), rows.begin(), rows.end());
+    while (P.iprog.size() % 4) P.iprog.push_back(0);
+    P.ip_off[gi][2] = (int)P.iprog.size();
+    for (size_t i = 0; i < cols.size(); i += 2)
+      P.iprog.push_back((int)cols[i] | (i + 1 < cols.size() ? (int)cols[i + 1] << 16 : 0));
+    while (P.iprog.size() % 4) P.iprog.push_back(0);
+    P.ip_off[gi][3] = (int)P.iprog.size();
+  }
+  P.il_ok = true;
+}
+
 static void pack_step_program(const krets_element *el, Program &P) {
   const int n = P.n;
   P.sprog.clear();
@@ -921,8 +991,11 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
   }
   pack_step_program(el, P);
   // the transposed program serves the adjoint, which runs single-circuit programs (with
-  // an update list); multi-circuit programs never need it
-  if (mode == MODE_TRAN && !P.tail_m && update_list) pack_transposed_program(P);
+  // an update list); multi-circuit programs never need it, nor the interleaved solves
+  if (mode == MODE_TRAN && !P.tail_m && update_list) {
+    pack_transposed_program(P);
+    pack_interleaved(P);
+  }
   uint64_t sig = 1469598103934665603ull;
   sig = fnv1a(sig, (uint64_t)mode);
   sig = fnv1a(sig, (uint64_t)n);
@@ -1080,11 +1153,18 @@ extern "C" krets_status krets_symbolic_export(const krets_element *elems, int32_
                                     &P.a_slot, &P.a_cptr, &P.a_contrib, &P.b_cptr, &P.b_contrib, &P.piv_ptr,
                                     &P.piv, &P.upd, &P.lev_ptr, &P.lev_rows, &P.ulev_ptr, &P.ulev_rows,
                                     &P.el_pos};
-  if (which < 0 || which > KRETS_PROG_SPOFF) return KRETS_ERR_INVALID_ARGUMENT;
+  if (which < 0 || which > KRETS_PROG_IMAP) return KRETS_ERR_INVALID_ARGUMENT;
   if (which == KRETS_PROG_TPROG || which == KRETS_PROG_TPOFF || which == KRETS_PROG_SPROG ||
-      which == KRETS_PROG_SPOFF) {
+      which == KRETS_PROG_SPOFF || which >= KRETS_PROG_IPROG) {
     std::vector<long long> v;
-    if (which == KRETS_PROG_TPROG) v.assign(P.tprog.begin(), P.tprog.end());
+    if (which == KRETS_PROG_IPROG) v.assign(P.iprog.begin(), P.iprog.end());
+    else if (which == KRETS_PROG_IMAP) v.assign(P.imap.begin(), P.imap.end());
+    else if (which == KRETS_PROG_IPOFF) {
+      for (int gi = 0; gi < 2; ++gi)
+        for (int k = 0; k < 4; ++k) v.push_back(P.ip_off[gi][k]);
+      v.insert(v.end(), {P.il_slots[0], P.il_slots[1], P.imap_off[0], P.imap_off[1], P.n_il_lrec, P.n_il_urec,
+                         P.il_ok ? 1 : 0});
+    } else if (which == KRETS_PROG_TPROG) v.assign(P.tprog.begin(), P.tprog.end());
     else if (which == KRETS_PROG_SPROG) v.assign(P.sprog.begin(), P.sprog.end());
     else if (which == KRETS_PROG_SPOFF) {
       v.assign(P.sp_off, P.sp_off + 16);

@@ -83,6 +83,20 @@ struct Program {
   // < tail0 only.  Row k of the block keeps its dense part at slots
   // lu_rowptr[k+1] - m .. lu_rowptr[k+1] - 1 (columns tail0 .. n-1).
   int tail0 = 0, tail_m = 0;
+  // Interleaved solve programs of the double-float engine with its factors in global
+  // memory, one per group size (layout 0: 64 threads, 1: 128; see pack_interleaved).
+  // Per level of the L solve (levels 1..) and of the U solve: a record
+  //   {W lanes, lanes per row, entry slots per lane, LU base, column base, row base,
+  //    diagonal base (U; -1 for L), 0}
+  // then the rows' positions and the columns (uint16 pairs); entry i of lane lam of a
+  // level sits at LU slot base + i * W + lam.  imap: interleaved LU slot -> CSR slot
+  // (-1: a zero pad).
+  std::vector<int> iprog, imap;
+  int ip_off[2][4] = {{0}};  // records, rows, columns, end (ints into iprog)
+  int il_slots[2] = {0, 0};
+  int imap_off[2] = {0, 0};
+  int n_il_lrec = 0, n_il_urec = 0;
+  bool il_ok = false;
   long long factor_flops = 0;
   int max_row_lu = 0;
   uint64_t signature = 0;

@@ -1385,6 +1385,76 @@ struct AdjFwd {
   double *loss;
 };
 
+// Interleaved solves (factors in global memory; layout: pack_interleaved in the host
+// symbolic pass).  A level record is {W, lanes per row, entry slots per lane, LU base,
+// column base, row base, diagonal base, 0}; lane lam (= thread + m G) of the level handles
+// row lam / spl with its entries j = lam % spl + i spl, visited in the same order as
+// df_level / df_level_split and padded with exact zeros, so the results are identical.
+struct IlProg {
+  const int *lrec, *urec;          // level records, 8 ints each
+  const int *rows;                 // positions of the levels' rows
+  const unsigned short *cols;      // interleaved columns
+  const df *lui;                   // interleaved factors (this instance's region)
+  int nl, nu;                      // L levels (from level 1), U levels
+};
+
+template <bool UPPER>
+__device__ __forceinline__ df il_lane(const int *rec, const IlProg &I, const df *y, int lam, int &k, int &r) {
+  const int W = rec[0], spl = rec[1], mc = rec[2];
+  r = lam / spl;
+  k = I.rows[rec[5] + r];
+  const int sub = lam & (spl - 1);
+  df s = sub == 0 ? y[k] : df{0.f, 0.f};
+  const df *a = I.lui + rec[3] + lam;
+  const unsigned short *c = I.cols + rec[4] + lam;
+  int i = 0;
+  for (; i + 3 < mc; i += 4) {  // four entries' loads in flight
+    df av[4], yv[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      av[q] = a[(size_t)(i + q) * W];
+      yv[q] = y[c[(i + q) * W]];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) s = df_fma_acc(df_neg(av[q]), yv[q], s);
+  }
+  for (; i < mc; ++i) s = df_fma_acc(df_neg(a[(size_t)i * W]), y[c[i * W]], s);
+  return df_norm(s);
+}
+
+template <int G, bool UPPER>
+__device__ __forceinline__ void il_level(const int *rec, const IlProg &I, df *y, int gl) {
+  const int W = rec[0], spl = rec[1];
+  const unsigned mask = lane_mask(spl);
+  for (int lam = gl; lam < W; lam += 2 * G) {  // two lanes' rows in flight per thread
+    const bool two = lam + G < W;
+    int k0, r0, k1 = -1, r1 = 0;
+    df v0 = il_lane<UPPER>(rec, I, y, lam, k0, r0);
+    df v1{0.f, 0.f};
+    if (two) v1 = il_lane<UPPER>(rec, I, y, lam + G, k1, r1);
+    if (spl > 1) {
+      v0 = df_lane_sum(v0, spl, mask);
+      if (two) v1 = df_lane_sum(v1, spl, mask);
+    }
+    if ((lam & (spl - 1)) == 0) {
+      y[k0] = UPPER ? df_mul(v0, I.lui[rec[6] + r0]) : v0;
+      if (two) y[k1] = UPPER ? df_mul(v1, I.lui[rec[6] + r1]) : v1;
+    }
+  }
+}
+
+template <int G>
+__device__ __forceinline__ void il_solve(const IlProg &I, df *y, int gl, int gid) {
+  for (int l = 0; l < I.nl; ++l) {
+    il_level<G, false>(I.lrec + 8 * l, I, y, gl);
+    gsync<G>(gid);
+  }
+  for (int l = 0; l < I.nu; ++l) {
+    il_level<G, true>(I.urec + 8 * l, I, y, gl);
+    gsync<G>(gid);
+  }
+}
+
 // Steps s_begin .. n_steps; the row of step s is out + (s - row_base) * n_out.
 // CBREC (trapezoidal rule, not with an adjoint forward pass): a capacitor's rhs value is
 // carried from step to step as its companion current source itself, cb_n = 2 (2C/h) v_{n-1}
@@ -1401,7 +1471,8 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
                                          WaveTab wt = WaveTab{nullptr, nullptr, 0},
                                          Probe pr = Probe{nullptr, 0, nullptr},
                                          AdjFwd af = AdjFwd{nullptr, 1, 0, 0, nullptr}, int s_begin = 1,
-                                         int row_base = 0) {
+                                         int row_base = 0,
+                                         IlProg il = IlProg{nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0}) {
   const int n_out = pr.n ? pr.n : P.n;
   df loss{0.f, 0.f};  // adjoint forward pass: lane 0 of the group accumulates
   int st = 0;
@@ -1473,8 +1544,12 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
       x[k] = acc;
     }
     gsync<G>(gid);
-    df_solve<G, false, SG, TAIL>(S, lu, x, gl, gid, lnar);
-    df_solve<G, true, SG, TAIL>(S, lu, x, gl, gid, unar);
+    if (il.lui) {
+      il_solve<G>(il, x, gl, gid);
+    } else {
+      df_solve<G, false, SG, TAIL>(S, lu, x, gl, gid, lnar);
+      df_solve<G, true, SG, TAIL>(S, lu, x, gl, gid, unar);
+    }
     if (!CBREC && method == KRETS_METHOD_TR) {
       for (int d = gl; d < P.ncap; d += G) {
         const int4 dd = S.dyn[d];
@@ -1489,7 +1564,7 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
     double *row = out + (size_t)(s - row_base) * n_out;
     for (int j = gl; j < n_out; j += G) {
       const df xv = x[S.qinv[pr.n ? pr.idx[j] : j]];
-      const double v = int_cvt ? df_to_double_int(xv) : df_to_double(xv);
+      const double v = int_cvt ? df_to_double_int(xv) : df_to_double_fast(xv);
       if (!isfinite(v)) st |= KS_NONFINITE;
       __stcs(row + j, v);
     }
@@ -1531,24 +1606,62 @@ __global__ void __launch_bounds__(896, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
                                                      AdjFwd af, Span sp, df *lu_glob) {
   extern __shared__ __align__(16) char smem[];
   const int gl = threadIdx.x % G, gid = threadIdx.x / G;
-  {
+  // With the factors in global memory and a 64 or 128-thread group the solves run from the
+  // interleaved program, and only the step-program sections the step reads besides the
+  // solves are staged (rhs elements, rhs gather, output order, split codes): the row
+  // descriptors and columns of the row-descriptor solves stay in global memory.
+  constexpr int gi = G == 128 ? 1 : 0;
+  const bool il = LUG && (G == 64 || G == 128) && P.il_ok;
+  SProg S;
+  IlProg I{nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0};
+  if (il) {
+    const int w0 = P.sp_off[7], w1 = P.sp_off[5], iw0 = P.ip_off[gi][0], iw1 = P.ip_off[gi][3];
+    const int head = ((w1 - w0) + 3) & ~3;  // words, 16-byte aligned
+    const int4 *src = reinterpret_cast<const int4 *>(P.sprog + w0);
+    int4 *dst = reinterpret_cast<int4 *>(smem);
+    for (int i = threadIdx.x; i < (w1 - w0) / 4; i += blockDim.x) dst[i] = src[i];
+    const int4 *isrc = reinterpret_cast<const int4 *>(P.iprog + iw0);
+    int4 *idst = reinterpret_cast<int4 *>(smem + 4 * head);
+    for (int i = threadIdx.x; i < (iw1 - iw0) / 4; i += blockDim.x) idst[i] = isrc[i];
+    __syncthreads();
+    const int *sm = reinterpret_cast<const int *>(smem);
+    S = SProg{};
+    S.dyn = reinterpret_cast<const int4 *>(sm + (P.sp_off[7] - w0));
+    S.bd_ptr = sm + (P.sp_off[8] - w0);
+    S.bd_op = sm + (P.sp_off[9] - w0);
+    S.qinv = sm + (P.sp_off[10] - w0);
+    const int *ip = sm + head;
+    I.lrec = ip;
+    I.urec = ip + 8 * P.n_il_lrec;
+    I.rows = ip + (P.ip_off[gi][1] - iw0);
+    I.cols = reinterpret_cast<const unsigned short *>(ip + (P.ip_off[gi][2] - iw0));
+    I.nl = P.n_il_lrec;
+    I.nu = P.n_il_urec;
+  } else {
     const int words = P.sp_off[5];  // everything before the residual operators
     const int4 *src = reinterpret_cast<const int4 *>(P.sprog);
     int4 *dst = reinterpret_cast<int4 *>(smem);
     for (int i = threadIdx.x; i < words / 4; i += blockDim.x) dst[i] = src[i];
     __syncthreads();
+    S = sprog_view(P, reinterpret_cast<const int *>(smem));
   }
-  const SProg S = sprog_view(P, reinterpret_cast<const int *>(smem));
-  int lnar = S.nlev, unar = 0;  // narrow-level split points (see df_solve)
-  while (lnar > 1 && S.lev_ptr[lnar] - S.lev_ptr[lnar - 1] <= 64) --lnar;
-  while (unar < S.nulev && S.ulev_ptr[unar + 1] - S.ulev_ptr[unar] <= 64) ++unar;
-  if (!(opts & 1)) lnar = unar = -1;
+  int lnar = -1, unar = -1;  // narrow-level split points (see df_solve)
+  if ((opts & 1) && !il) {
+    lnar = S.nlev;
+    unar = 0;
+    while (lnar > 1 && S.lev_ptr[lnar] - S.lev_ptr[lnar - 1] <= 64) --lnar;
+    while (unar < S.nulev && S.ulev_ptr[unar + 1] - S.ulev_ptr[unar] <= 64) ++unar;
+  }
   const bool int_cvt = (opts & 2) != 0;
   // bit 2: trapezoidal capacitor history carried as the companion current (no adjoint pass)
   const bool cbrec = (opts & 4) != 0 && method == KRETS_METHOD_TR && !af.ck;
   char *base = smem + L.sprog_bytes + (size_t)gid * L.bytes;
-  df *lu = LUG ? lu_glob + (size_t)(blockIdx.x * (blockDim.x / G) + gid) * P.nnz_lu
+  // global-memory factors: per group the CSR factors, then (interleaved solves) their
+  // interleaved copy
+  const size_t greg = (size_t)P.nnz_lu + (il ? (size_t)P.il_slots[gi] : 0);
+  df *lu = LUG ? lu_glob + (size_t)(blockIdx.x * (blockDim.x / G) + gid) * greg
                : reinterpret_cast<df *>(base + L.lu);
+  if (il) I.lui = lu + P.nnz_lu;
   double *lu64 = reinterpret_cast<double *>(lu);  // same bytes, set-up only
   df *x = reinterpret_cast<df *>(base + L.x);
   df *cdyn = reinterpret_cast<df *>(base + L.cdyn);
@@ -1568,6 +1681,15 @@ __global__ void __launch_bounds__(896, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
     double *out = x_out ? x_out + (size_t)inst * stride : nullptr;
     const double *op = pr.x0 ? pr.x0 + (size_t)inst * P.n : out;  // operating point (none: x_0 = 0)
     int st = dfd_setup<G>(P, S, vals, h, method, lu, lu64, coef64, cdyn, gl, gid);
+    if (il) {  // the factors in the interleaved order of the solves (zero pads)
+      gsync<G>(gid);
+      df *lui = lu + P.nnz_lu;
+      const int *map = P.imap + P.imap_off[gi];
+      for (int q = gl; q < P.il_slots[gi]; q += G) {
+        const int m = map[q];
+        lui[q] = m >= 0 ? lu[m] : df{0.f, 0.f};
+      }
+    }
     df *state = sp.state ? sp.state + (size_t)inst * ns : nullptr;
     if (state && sp.s_begin > 1) {  // resume: x and the TR currents where the previous span stopped
       for (int k = gl; k < P.n; k += G) x[k] = state[k];
@@ -1586,10 +1708,10 @@ __global__ void __launch_bounds__(896, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
     if (!fatal) {
       if (cbrec)
         st |= dfd_steps<G, G, true, false>(P, S, lu, x, cdyn, cb, icap, vals, h, n_steps, method, lag, out, lnar, unar,
-                                    int_cvt, gl, gid, wt, pr, a, sp.s_begin, sp.row_base);
+                                    int_cvt, gl, gid, wt, pr, a, sp.s_begin, sp.row_base, I);
       else
         st |= dfd_steps<G, G, false, false>(P, S, lu, x, cdyn, cb, icap, vals, h, n_steps, method, lag, out, lnar,
-                                            unar, int_cvt, gl, gid, wt, pr, a, sp.s_begin, sp.row_base);
+                                            unar, int_cvt, gl, gid, wt, pr, a, sp.s_begin, sp.row_base, I);
     }
     if (state) {  // the last step's solution level and TR currents are final once the group syncs
       gsync<G>(gid);

@@ -375,3 +375,32 @@ def test_config3_full_size_sampled_parity_and_exact_linearity(oracle_lib):
     for i in sample:
         scale = np.abs(2.0 * base[i]).max()
         assert np.abs(doubled[i] - 2.0 * base[i]).max() <= 1e-12 * scale, i
+
+
+@pytest.mark.parametrize("G", ["64", "128"])
+def test_factor_placements_give_identical_bits(oracle_lib, monkeypatch, G):
+    """The double-float engine with its factors in shared memory (row-descriptor solves)
+    and in global memory (interleaved solves, zero-padded levels) runs the same arithmetic:
+    identical bits, on the RLC ladder (TR) and on a random uneven netlist (BE with the
+    reference's source lag); both against the oracle."""
+    from krets_gb300.generators import uneven_table
+    cases = []
+    c = rlc_ladder(100)
+    cases.append((element_table(c), c.size, is_current_mask(c), "tr", False, 1e-12, monte_carlo_values(c, 20, seed=6)))
+    t6, n6 = uneven_table(0)   # n = 630: both placements fit
+    m6 = np.zeros(n6, bool)
+    m6[t6["b"][t6["b"] >= 0]] = True
+    cases.append((t6, n6, m6, "be", True, 1e-9, np.tile(t6["value"], (3, 1))))
+    monkeypatch.setenv("KRETS_GROUP", G)
+    for t, n, mask, method, lag, h, vals in cases:
+        outs = {}
+        for place in ("smem", "global"):
+            monkeypatch.setenv("KRETS_DFD_LU", place)
+            g = _lib.GpuCircuit(t, n)
+            outs[place] = g.batch_tran(vals, h, 300, method, lag=lag, precision=_lib.PREC_DF)
+            assert g.last_launch()["factors"] == ("global memory" if place == "global" else "shared memory")
+        np.testing.assert_array_equal(outs["smem"], outs["global"])
+        ti = t.copy()
+        ti["value"] = vals[0]
+        ref = oracle_lib.tran(ti, n, h, 300, method=method, lag=lag)
+        assert normwise_err(outs["global"][0], ref, mask) < TOL

@@ -201,3 +201,81 @@ def test_multi_circuit_program_dense_tail_solves(built_lib, oracle_lib):
     x = PE.solve_multi(p, n, lu, rhs[p["prow"]])
     xd = np.linalg.solve(A.reshape(n, n), rhs)
     np.testing.assert_allclose(x, xd, rtol=0, atol=1e-10 * np.abs(xd).max())
+
+
+def _il_solve(P, vals, b, gi):
+    """Emulate the interleaved L and U solves of layout gi (64 / 128-thread groups) in FP64."""
+    off = P["ipoff"]
+    rec0, rows0, cols0, end = off[4 * gi:4 * gi + 4]
+    nl, nu = int(off[12]), int(off[13])
+    ip = P["iprog"]
+    rec = ip[rec0:rows0].reshape(-1, 8)[:nl + nu]
+    rows = ip[rows0:cols0]
+    packed = ip[cols0:end].astype(np.int64)
+    cols = np.stack([packed & 0xffff, (packed >> 16) & 0xffff], axis=1).reshape(-1)
+    slots = int(off[8 + gi])
+    imap = P["imap"][int(off[10 + gi]):int(off[10 + gi]) + slots]
+    lui = np.where(imap >= 0, vals[np.maximum(imap, 0)], 0.0)
+    y = b.copy()
+    for li, (W, spl, mc, base, cbase, rbase, dbase, _) in enumerate(rec):
+        upper = li >= nl
+        sums = {}
+        for lam in range(W):
+            r, sub = divmod(lam, spl)
+            k = rows[rbase + r]
+            s = y[k] if sub == 0 else 0.0
+            for i in range(mc):
+                s -= lui[base + i * W + lam] * y[cols[cbase + i * W + lam]]
+            sums.setdefault(r, []).append(s)
+        for r, parts in sums.items():
+            k = rows[rbase + r]
+            v = sum(parts)
+            y[k] = v * lui[dbase + r] if upper else v
+    return y, imap, slots
+
+
+def _csr_solve(P, vals, b):
+    rp, col, dg = P["lu_rowptr"], P["lu_col"], P["lu_diag"]
+    y = b.copy()
+    lp, lr = P["lev_ptr"], P["lev_rows"]
+    for l in range(1, len(lp) - 1):
+        for k in lr[lp[l]:lp[l + 1]]:
+            y[k] -= sum(vals[s] * y[col[s]] for s in range(rp[k], dg[k]))
+    up, ur = P["ulev_ptr"], P["ulev_rows"]
+    for l in range(len(up) - 1):
+        for k in ur[up[l]:up[l + 1]]:
+            y[k] = (y[k] - sum(vals[s] * y[col[s]] for s in range(dg[k] + 1, rp[k + 1]))) * vals[dg[k]]
+    return y
+
+
+@pytest.mark.parametrize("which", ["rlc200", "rc300", "uneven6"])
+def test_interleaved_solve_program_equals_row_solves(built_lib, which):
+    """The interleaved ("ELL per level") solve program of the double-float engine (factors
+    in global memory): every L entry of levels 1.. and every U entry appears exactly once,
+    each U row's reciprocal diagonal once, pads are zero; emulated in FP64 it solves the
+    same triangular systems as the row-descriptor program, for both group-size layouts."""
+    from krets_gb300.generators import rc_ladder_step, rlc_ladder, uneven_table
+    if which == "rlc200":
+        c = rlc_ladder(200)
+        t, n = element_table(c), c.size
+    elif which == "rc300":
+        c = rc_ladder_step(300)
+        t, n = element_table(c), c.size
+    else:
+        t, n = uneven_table(6)
+    P = built_lib.symbolic_export(t, n, built_lib.MODE_TRAN, "tr", 1e-12)
+    assert P["ipoff"][14] == 1
+    rng = np.random.default_rng(3)
+    nnz = len(P["lu_col"])
+    vals = rng.uniform(-0.05, 0.05, nnz)
+    vals[P["lu_diag"]] = rng.uniform(0.5, 1.5, n)
+    b = rng.standard_normal(n)
+    ref = _csr_solve(P, vals, b)
+    rp, dg = P["lu_rowptr"], P["lu_diag"]
+    level0 = set(P["lev_rows"][P["lev_ptr"][0]:P["lev_ptr"][1]].tolist())
+    want = sorted([s for k in range(n) if k not in level0 for s in range(rp[k], dg[k])]
+                  + [s for k in range(n) for s in range(dg[k] + 1, rp[k + 1])] + list(dg))
+    for gi in (0, 1):
+        y, imap, slots = _il_solve(P, vals, b, gi)
+        assert sorted(imap[imap >= 0].tolist()) == want
+        np.testing.assert_allclose(y, ref, rtol=1e-12, atol=1e-12)
