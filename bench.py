@@ -45,7 +45,7 @@ SEED = 3
 METRIC = "circuit-timesteps/sec batched vs plain GPU form at <=1e-9 rel err vs FP64"
 UNIT = "circuit-timesteps/s"
 WORKLOAD = "mc_transient_rlc_ladder_2048x200sec_tr_1ps_10000steps"
-TRAFFIC_PER_CIRCUIT_STEP = (1.403939e9 + 3.843072e6) / (304 * 1000)  # bytes, ncu capture
+TRAFFIC_PER_CIRCUIT_STEP = (2.037667e9 + 36.881e6) / (2048 * 200)  # bytes, ncu capture
 
 
 def dist_env():
@@ -416,7 +416,7 @@ def run_ours(args, rank, world):
         "batched_over_plain": value / plain_rate,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "traffic_note": "ncu DRAM bytes of a 304 x 1000-step capture scaled per circuit-step",
+                     "traffic_note": "ncu DRAM bytes of a 2048 x 200-step capture scaled per circuit-step",
                      "kernel": f"k_tran_dfd<{engine['threads_per_instance']}, factors in "
                                f"{engine['factors']}>", "algorithmic_bytes_per_launch": alg_bytes},
         "cpu_baseline": {"value": cpu_val, "unit": UNIT, "cores": threads, "kind": "port",
