@@ -317,6 +317,10 @@ static void place_program(const Program &H, const ProgramImage &X, const krets_e
   V.n_il_lrec = H.n_il_lrec;
   V.n_il_urec = H.n_il_urec;
   V.il_ok = H.il_ok ? 1 : 0;
+  V.lean_off = H.lean_off;
+  V.n_zrow = H.n_zrow;
+  V.n_ind = H.n_ind;
+  V.lean_ok = H.lean_ok ? 1 : 0;
   V.n_coef = H.n_coef;
   V.el = d_el;
   V.ndyn = (int)H.dyn_e.size();
@@ -1079,8 +1083,10 @@ using DfdKernel = void (*)(DevProg, KCfg, DfdLay, const double *, int, double, i
                            int, WaveTab, Probe, AdjFwd, Span, df *);
 constexpr Span kWholeRun{1, 0, 0, nullptr};
 // default options of the double-float engine (KRETS_DFD_OPTS overrides): trapezoidal
-// capacitor history as companion currents (bit 2), measured 4 % faster on the RLC ladder
-constexpr int kDfdDefaultOpts = 4;
+// capacitor history as companion currents (bit 2), measured 4 % faster on the RLC ladder;
+// output conversion on the FP64 pipe in the direct-rhs step (bit 4; 4.81 -> 4.60 ms on
+// 2048 instances x 200 steps of it: fewer issued instructions than integer widening)
+constexpr int kDfdDefaultOpts = 4 | 16;
 struct DfdLaunch {
   int G = 128, W = 1, per_sm = 0;
   bool lug = false;  // factors in global memory (k_tran_dfd<G, true>)
@@ -1093,24 +1099,44 @@ struct DfdLaunch {
 // that has them (k_tran_dfd).
 bool dfd_interleaved(const DevProg &P, bool lug, int G) { return lug && (G == 64 || G == 128) && P.il_ok; }
 
+// The interleaved step with a direct right-hand side (dfd_steps_lean): a program that has
+// one, TR with companion currents (opts bit 2) or BE; opts bit 3 turns it off.
+bool dfd_lean_step(const DevProg &P, bool lug, int G, int method, int opts) {
+  return dfd_interleaved(P, lug, G) && P.lean_ok && !(opts & 8) &&
+         (method == KRETS_METHOD_BE || (method == KRETS_METHOD_TR && (opts & 4)));
+}
+
 // Shared-memory layout of one double-float instance (without the factors when lug: they
 // are then in global memory); false when it does not fit a CTA.  G matters only with lug
-// (the staged program then depends on it).
-bool dfd_layout(const DevProg &P, DfdLay &DL, bool lug = false, int G = 64) {
+// (the staged program then depends on it), method and opts only for the direct
+// right-hand-side step (method < 0: never that step).
+bool dfd_layout(const DevProg &P, DfdLay &DL, bool lug = false, int G = 64, int method = -1, int opts = 0) {
   size_t cur = 0;
   auto put = [&](int &off, size_t bytes) { off = (int)cur; cur = align16(cur + bytes); };
+  const bool lean = method >= 0 && dfd_lean_step(P, lug, G, method, opts);
+  DL.lean = lean ? 1 : 0;
   if (lug) DL.lu = 0;
   else put(DL.lu, 8 * (size_t)P.nnz_lu);
-  put(DL.x, 8 * (size_t)P.n);
-  put(DL.cdyn, 8 * (size_t)P.ndyn);
-  put(DL.cb, 8 * (size_t)P.ndyn);
+  if (lean) {  // two state buffers of n + 2 (ground zero, write-only slot)
+    put(DL.x, 8 * ((size_t)P.n + 2));
+    put(DL.cb, 8 * ((size_t)P.n + 2));
+    put(DL.cdyn, 8 * (size_t)P.ndyn);
+  } else {
+    put(DL.x, 8 * (size_t)P.n);
+    put(DL.cdyn, 8 * (size_t)P.ndyn);
+    put(DL.cb, 8 * (size_t)P.ndyn);
+  }
   put(DL.icap, 8 * (size_t)P.ncap);
   DL.coef64 = DL.x;  // set-up scratch over x / cdyn / cb / icap (+ padding if needed)
   if (cur - DL.x < 8 * (size_t)P.ne) cur = DL.x + align16(8 * (size_t)P.ne);
   put(DL.slot, 16);
   DL.bytes = (int)align16(cur);
-  if (dfd_interleaved(P, lug, G)) {  // rhs / gather / output sections, then the interleaved program
-    const int gi = G == 128 ? 1 : 0;
+  const int gi = G == 128 ? 1 : 0;
+  if (lean) {  // direct rhs records and unfed rows, output order, then the interleaved program
+    DL.sprog_bytes = (int)(sizeof(int) * ((4 * (size_t)P.ndyn + P.n_zrow + 3) & ~(size_t)3) +
+                           sizeof(int) * (((size_t)P.n + 3) & ~(size_t)3) +
+                           sizeof(int) * (size_t)(P.ip_off[gi][3] - P.ip_off[gi][0]));
+  } else if (dfd_interleaved(P, lug, G)) {  // rhs / gather / output sections, then the interleaved program
     DL.sprog_bytes = (int)(align16((size_t)(P.sp_off[5] - P.sp_off[7]) * sizeof(int)) +
                            align16((size_t)(P.ip_off[gi][3] - P.ip_off[gi][0]) * sizeof(int)));
   } else {
@@ -1190,7 +1216,7 @@ krets_status dfd_pick(krets_circuit *c, const DevProgram *D, const double *dv, c
   for (const Cand &cd : cands) {
     DfdLay DL{};
     DfdLaunch Lc;
-    if (!dfd_layout(P, DL, cd.lug, cd.G) || dfd_config(cd.G, cd.lug, DL, Lc) != KRETS_OK) {
+    if (!dfd_layout(P, DL, cd.lug, cd.G, method, opts) || dfd_config(cd.G, cd.lug, DL, Lc) != KRETS_OK) {
       cudaGetLastError();
       continue;
     }
@@ -1330,8 +1356,10 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
   // double-float direct: one instance per group of G threads (default 128); it stages only
   // the step-program words before the residual operators, so it fits where the warp
   // engine may not
+  const char *oenv = getenv("KRETS_DFD_OPTS");
+  const int opts = oenv ? atoi(oenv) : kDfdDefaultOpts;
   DfdLay DL{}, DLg{};
-  const bool dfd_smem = dfd_layout(P, DL), dfd_glob = dfd_layout(P, DLg, true);
+  const bool dfd_smem = dfd_layout(P, DL), dfd_glob = dfd_layout(P, DLg, true, 64, method, opts);
   const bool use_dfd = precision == KRETS_PREC_DF && !P.nonlinear && P.sprog_ok && !block_forced && (dfd_smem || dfd_glob);
   // Host output of the double-float engine is staged: the transient runs as spans of
   // steps, each written to a device staging buffer and copied into the caller's rows by
@@ -1421,8 +1449,6 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
       wt.tab = (const double *)twave.p;
       wt.row = d_wrow;
     }
-    const char *oenv = getenv("KRETS_DFD_OPTS");
-    const int opts = oenv ? atoi(oenv) : kDfdDefaultOpts;
     // group size and place of the factors: KRETS_GROUP / KRETS_DFD_LU (smem | global),
     // else the autotuner
     const char *genv = getenv("KRETS_GROUP"), *lenv = getenv("KRETS_DFD_LU");
@@ -1437,7 +1463,8 @@ static krets_status batch_tran_impl(krets_circuit *c, int32_t n_inst, const doub
                    queue, opts, wt, pr, G, lug, how);
       if (s != KRETS_OK) return s;
     }
-    if (lug && !dfd_layout(P, DL, true, G)) return fail(KRETS_ERR_INVALID_ARGUMENT, "double-float layout does not fit");
+    if (lug && !dfd_layout(P, DL, true, G, method, opts))
+      return fail(KRETS_ERR_INVALID_ARGUMENT, "double-float layout does not fit");
     DfdLaunch Lc;
     s = dfd_config(G, lug, DL, Lc);
     if (s != KRETS_OK) return s;

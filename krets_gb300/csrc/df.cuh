@@ -14,7 +14,9 @@
 
 namespace krets {
 
-struct df {
+// 8-byte aligned, so that a pair moves with one 64-bit load or store (every df array of
+// the engines starts on a 16-byte boundary of its layout).
+struct __align__(8) df {
   float hi, lo;
 };
 

@@ -116,6 +116,7 @@ struct DevProg {
   // interleaved solves (Program::iprog; layouts for 64 and 128-thread groups)
   const int *iprog, *imap;
   int ip_off[2][4], il_slots[2], imap_off[2], n_il_lrec, n_il_urec, il_ok;
+  int lean_off, n_zrow, n_ind, lean_ok;  // direct right-hand side (in iprog)
 };
 
 // status bits written by the engine

@@ -456,13 +456,16 @@ static int split_code(int rows, int mx) {
 // Interleaved ("ELL per level") form of the L and U solves for the double-float engine
 // with its factors in global memory.  Within a level, lane lam of the level's W = rows x
 // lanes-per-row lanes handles row lam / spl and its entries j = lam % spl + i * spl; entry
-// slot i of every lane of the level is stored contiguously (slot base + i * W + lam), so a
-// warp's loads of one slot are consecutive addresses, and so are the columns in shared
-// memory.  Lanes with fewer entries than the level's longest are padded with zero
-// entries, which leave the double-float sums unchanged bit for bit; the entries of a row
-// are visited in the same order as by the row-descriptor solves (df_level,
-// df_level_split), so both forms give identical results.  Lanes per row are the split of
-// the row-descriptor program for the group size (split_code).
+// slot i of every lane of the level is stored contiguously (first slot + i * W + lam), so
+// a warp's loads of one slot are consecutive addresses, and so are the columns in shared
+// memory (one column per entry slot).  The U rows' reciprocal diagonals follow all entry
+// slots.  Lanes with fewer entries than the level's longest are padded with zero entries,
+// which leave the double-float sums unchanged bit for bit; the entries of a row are
+// visited in the same order as by the row-descriptor solves (df_level, df_level_split),
+// so both forms give identical results.  Lanes per row are the split of the
+// row-descriptor program for the group size (split_code).  A level of at most 32 lanes
+// runs on the group's first warp alone (flag bit 0); when the next level does too, a warp
+// barrier separates them instead of a group barrier (bit 1).
 static void pack_interleaved(Program &P) {
   P.iprog.clear();
   P.imap.clear();
@@ -472,41 +475,45 @@ static void pack_interleaved(Program &P) {
   const int nlev = (int)P.lev_ptr.size() - 1, nulev = (int)P.ulev_ptr.size() - 1;
   for (int gi = 0; gi < 2; ++gi) {
     const int g = gi == 0 ? 1 : 2;  // split-code field of 64 / 128-thread groups
-    std::vector<int> rec, rows;
+    std::vector<int> rec, rows, emap, dmap;
     std::vector<unsigned short> cols;
-    const int mbase = (int)P.imap.size();
-    int slots = 0;
     auto level = [&](bool upper, int l) {
       const int *ptr = upper ? P.ulev_ptr.data() : P.lev_ptr.data();
       const int *rw = upper ? P.ulev_rows.data() : P.lev_rows.data();
       const int code = upper ? umax[l] : lmax[l];
-      const int spl = 1 << ((code >> (3 * g)) & 7);
+      const int lsh = (code >> (3 * g)) & 7, spl = 1 << lsh;
       const int nr = ptr[l + 1] - ptr[l], W = nr * spl;
       auto first = [&](int k) { return upper ? P.lu_diag[k] + 1 : P.lu_rowptr[k]; };
       auto count = [&](int k) { return upper ? P.lu_rowptr[k + 1] - P.lu_diag[k] - 1 : P.lu_diag[k] - P.lu_rowptr[k]; };
       int mc = 0;
       for (int t = ptr[l]; t < ptr[l + 1]; ++t) mc = std::max(mc, (count(rw[t]) + spl - 1) / spl);
-      rec.insert(rec.end(), {W, spl, mc, slots, (int)cols.size(), (int)rows.size(), upper ? slots + mc * W : -1, 0});
+      rec.insert(rec.end(), {W, lsh, mc, (int)emap.size(), (int)rows.size(), upper ? (int)dmap.size() : -1, 0, 0});
       for (int i = 0; i < mc; ++i)
         for (int lam = 0; lam < W; ++lam) {
           const int k = rw[ptr[l] + lam / spl], j = lam % spl + i * spl;
           const bool real = j < count(k);
-          P.imap.push_back(real ? first(k) + j : -1);
+          emap.push_back(real ? first(k) + j : -1);
           cols.push_back((unsigned short)(real ? P.lu_col[first(k) + j] : k));
         }
-      slots += mc * W;
       for (int t = ptr[l]; t < ptr[l + 1]; ++t) rows.push_back(rw[t]);
-      if (upper) {  // reciprocal diagonals of the level's rows
-        for (int t = ptr[l]; t < ptr[l + 1]; ++t) P.imap.push_back(P.lu_diag[rw[t]]);
-        slots += nr;
-      }
+      if (upper)  // reciprocal diagonals of the level's rows
+        for (int t = ptr[l]; t < ptr[l + 1]; ++t) dmap.push_back(P.lu_diag[rw[t]]);
     };
     for (int l = 1; l < nlev; ++l) level(false, l);  // L level 0 rows have no L entries
     for (int l = 0; l < nulev; ++l) level(true, l);
+    const int nrec = (int)rec.size() / 8, eslots = (int)emap.size();
+    for (int r = 0; r < nrec; ++r) {
+      int *R = rec.data() + 8 * r;
+      if (R[5] >= 0) R[5] += eslots;  // diagonals after the entry slots
+      const bool narrow = R[0] <= 32, next_narrow = r + 1 < nrec && R[8] <= 32;
+      R[6] = (narrow ? 1 : 0) | (narrow && next_narrow ? 2 : 0);
+    }
     P.n_il_lrec = std::max(0, nlev - 1);
     P.n_il_urec = nulev;
-    P.il_slots[gi] = slots;
-    P.imap_off[gi] = mbase;
+    P.il_slots[gi] = eslots + (int)dmap.size();
+    P.imap_off[gi] = (int)P.imap.size();
+    P.imap.insert(P.imap.end(), emap.begin(), emap.end());
+    P.imap.insert(P.imap.end(), dmap.begin(), dmap.end());
     while (P.iprog.size() % 4) P.iprog.push_back(0);
     P.ip_off[gi][0] = (int)P.iprog.size();
     P.iprog.insert(P.iprog.end(), rec.begin(), rec.end());
@@ -521,6 +528,63 @@ static void pack_interleaved(Program &P) {
     P.ip_off[gi][3] = (int)P.iprog.size();
   }
   P.il_ok = true;
+}
+
+// Direct right-hand side of the double-float engine's interleaved step: when no row of
+// the right-hand side takes more than one element's companion source, every element
+// writes its value straight into the rows it feeds (no gather pass), and the rows that
+// no element feeds are zeroed.  Appended to iprog at lean_off: one int4 per dynamic
+// element, in dyn order (capacitors, then inductors, then the other sources),
+//   capacitor  {node p, node m, row +, row -}
+//   inductor   {node p, node m, branch position, row << 1 | negated}
+//   other      {e | kind << 24, 0, row +, row -}
+// with position n for a ground node (the state holds a zero there) and n + 1 for a row
+// that is not fed (a write-only scratch slot); then the rows no element feeds.
+static void pack_lean(const krets_element *el, Program &P) {
+  P.lean_ok = false;
+  P.lean_off = P.n_zrow = 0;
+  if (!P.il_ok) return;
+  const int n = P.n, nd = (int)P.dyn_e.size(), sink = n + 1;
+  std::vector<std::vector<int>> feeds(nd);  // per element: row << 1 | negated
+  std::vector<int> zrow;
+  for (int k = 0; k < n; ++k) {
+    const int cnt = P.bd_ptr[k + 1] - P.bd_ptr[k];
+    if (cnt > 1) return;
+    if (cnt == 0) zrow.push_back(k);
+    else feeds[P.bd_op[P.bd_ptr[k]] >> 1].push_back(k << 1 | (P.bd_op[P.bd_ptr[k]] & 1));
+  }
+  std::vector<int> L;
+  for (int d = 0; d < nd; ++d) {
+    const int e = P.dyn_e[d], kind = el[e].kind;
+    const bool cap = d < P.ncap, ind = d >= P.ncap && d < P.ncap + P.n_ind;
+    if (cap != (kind == KRETS_ELEM_C) || ind != (kind == KRETS_ELEM_L)) return;
+    if (kind != KRETS_ELEM_C && kind != KRETS_ELEM_L && kind != KRETS_ELEM_V && kind != KRETS_ELEM_I) return;
+    const std::vector<int> &f = feeds[d];
+    int rp = sink, rm = sink;
+    if (kind == KRETS_ELEM_L || kind == KRETS_ELEM_V) {
+      if (f.size() > 1) return;
+    } else if (f.size() > 2 || (f.size() == 2 && (f[0] & 1) == (f[1] & 1))) {
+      return;
+    }
+    for (int v : f) ((v & 1) ? rm : rp) = v >> 1;
+    auto node = [&](int pos) { return pos < 0 ? n : pos; };
+    const int p = node(P.el_pos[4 * e + 0]), m = node(P.el_pos[4 * e + 1]);
+    if (kind == KRETS_ELEM_C) {
+      L.insert(L.end(), {p, m, rp, rm});
+    } else if (kind == KRETS_ELEM_L) {
+      if (P.el_pos[4 * e + 2] < 0) return;
+      L.insert(L.end(), {p, m, P.el_pos[4 * e + 2], f.empty() ? sink << 1 : f[0]});
+    } else {
+      L.insert(L.end(), {e | (kind << 24), 0, rp, rm});
+    }
+  }
+  while (P.iprog.size() % 4) P.iprog.push_back(0);
+  P.lean_off = (int)P.iprog.size();
+  P.iprog.insert(P.iprog.end(), L.begin(), L.end());
+  P.iprog.insert(P.iprog.end(), zrow.begin(), zrow.end());
+  while (P.iprog.size() % 4) P.iprog.push_back(0);
+  P.n_zrow = (int)zrow.size();
+  P.lean_ok = true;
 }
 
 static void pack_step_program(const krets_element *el, Program &P) {
@@ -963,18 +1027,20 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
       for (int u = P.a_cptr[t]; u < P.a_cptr[t + 1]; ++u) P.res_op.insert(P.res_op.end(), {P.a_col[t], P.a_contrib[u]});
     P.res_ptr[r + 1] = (int)P.res_op.size() / 2;
   }
+  // dynamic elements in the order capacitors, inductors, the rest
   std::vector<int> dyn_of(ne, -1);
-  for (int pass = 0; pass < 2; ++pass)
+  for (int pass = 0; pass < 3; ++pass)
     for (int e = 0; e < ne; ++e) {
       int k = el[e].kind;
-      bool cap = k == KRETS_ELEM_C;
-      bool dyn = cap || k == KRETS_ELEM_L || k == KRETS_ELEM_V || k == KRETS_ELEM_I || k == KRETS_ELEM_D ||
+      bool cap = k == KRETS_ELEM_C, ind = k == KRETS_ELEM_L;
+      bool dyn = cap || ind || k == KRETS_ELEM_V || k == KRETS_ELEM_I || k == KRETS_ELEM_D ||
                  (k == KRETS_ELEM_M && (el[e].flags & KRETS_FLAG_NMOS_RESOLVED));
-      if (!dyn || (pass == 0) != cap) continue;
+      if (!dyn || (pass == 0) != cap || (pass == 1) != ind) continue;
       if (mode == MODE_DC && cap) continue;
       dyn_of[e] = (int)P.dyn_e.size();
       P.dyn_e.push_back(e);
       if (cap) P.ncap++;
+      if (ind) P.n_ind++;
     }
   P.bd_ptr.assign(n + 1, 0);
   for (int r = 0; r < n; ++r) {
@@ -995,6 +1061,7 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
   if (mode == MODE_TRAN && !P.tail_m && update_list) {
     pack_transposed_program(P);
     pack_interleaved(P);
+    pack_lean(el, P);
   }
   uint64_t sig = 1469598103934665603ull;
   sig = fnv1a(sig, (uint64_t)mode);
@@ -1163,7 +1230,7 @@ extern "C" krets_status krets_symbolic_export(const krets_element *elems, int32_
       for (int gi = 0; gi < 2; ++gi)
         for (int k = 0; k < 4; ++k) v.push_back(P.ip_off[gi][k]);
       v.insert(v.end(), {P.il_slots[0], P.il_slots[1], P.imap_off[0], P.imap_off[1], P.n_il_lrec, P.n_il_urec,
-                         P.il_ok ? 1 : 0});
+                         P.il_ok ? 1 : 0, P.lean_off, P.n_zrow, P.n_ind, P.lean_ok ? 1 : 0});
     } else if (which == KRETS_PROG_TPROG) v.assign(P.tprog.begin(), P.tprog.end());
     else if (which == KRETS_PROG_SPROG) v.assign(P.sprog.begin(), P.sprog.end());
     else if (which == KRETS_PROG_SPOFF) {

@@ -61,7 +61,7 @@ struct Program {
   std::vector<int> res_ptr, res_op;
   // elements with a right-hand-side coefficient (C, L, V, I, D), capacitors first
   std::vector<int> dyn_e;
-  int ncap = 0;
+  int ncap = 0, n_ind = 0;  // dyn_e: capacitors first, then inductors
   // rhs contributions per position row, packed dyn_index << 1 | neg
   std::vector<int> bd_ptr, bd_op;
   // compact step program, copied into shared memory by the warp engine (sprog_ok = the
@@ -86,17 +86,20 @@ struct Program {
   // Interleaved solve programs of the double-float engine with its factors in global
   // memory, one per group size (layout 0: 64 threads, 1: 128; see pack_interleaved).
   // Per level of the L solve (levels 1..) and of the U solve: a record
-  //   {W lanes, lanes per row, entry slots per lane, LU base, column base, row base,
-  //    diagonal base (U; -1 for L), 0}
-  // then the rows' positions and the columns (uint16 pairs); entry i of lane lam of a
-  // level sits at LU slot base + i * W + lam.  imap: interleaved LU slot -> CSR slot
-  // (-1: a zero pad).
+  //   {W lanes, log2 lanes per row, entry slots per lane, first entry slot, row base,
+  //    diagonal slot base (U; -1 for L), flags, 0}
+  // then the rows' positions and the columns (uint16 pairs, one per entry slot); entry i
+  // of lane lam of a level sits at slot first + i * W + lam, the U rows' reciprocal
+  // diagonals after all entry slots.  imap: interleaved slot -> CSR slot (-1: a zero pad).
+  // Then (pack_lean) the direct right-hand-side records at lean_off.
   std::vector<int> iprog, imap;
   int ip_off[2][4] = {{0}};  // records, rows, columns, end (ints into iprog)
   int il_slots[2] = {0, 0};
   int imap_off[2] = {0, 0};
   int n_il_lrec = 0, n_il_urec = 0;
   bool il_ok = false;
+  int lean_off = 0, n_zrow = 0;  // direct right-hand side (pack_lean)
+  bool lean_ok = false;
   long long factor_flops = 0;
   int max_row_lu = 0;
   uint64_t signature = 0;

@@ -1306,6 +1306,12 @@ struct DfdLay {
   int coef64; // double[ne] set-up scratch (aliases x / cdyn / cb / icap and padding)
   int bytes;  // per instance
   int sprog_bytes;
+  // 1: the interleaved step with a direct right-hand side (dfd_steps_lean; factors in
+  // global memory): x holds n + 2 values (a zero for ground at n, a write-only slot at
+  // n + 1), cb is the second state buffer (n + 2 values), icap the capacitor companion
+  // values; the staged program is the direct right-hand side, qinv and the interleaved
+  // solves
+  int lean;
 };
 
 // Set-up of one instance for the double-float direct engine: FP64 coefficients, LU
@@ -1330,7 +1336,7 @@ __device__ __forceinline__ int dfd_setup(const DevProg &P, const SProg &S, const
                      : g_factor64<G>(P, lu64, gl, gid);
   for (int sl = gl; sl < P.nnz_lu; sl += G) lu[sl] = df_from_double(lu64[sl]);
   for (int d = gl; d < P.ndyn; d += G) {
-    const int e = S.dyn[d].x & 0xffffff;
+    const int e = P.dyn_e[d];
     const krets_element &E = P.el[e];
     const double val = vals ? vals[e] : E.value;
     double c = val;
@@ -1386,73 +1392,132 @@ struct AdjFwd {
 };
 
 // Interleaved solves (factors in global memory; layout: pack_interleaved in the host
-// symbolic pass).  A level record is {W, lanes per row, entry slots per lane, LU base,
-// column base, row base, diagonal base, 0}; lane lam (= thread + m G) of the level handles
-// row lam / spl with its entries j = lam % spl + i spl, visited in the same order as
-// df_level / df_level_split and padded with exact zeros, so the results are identical.
+// symbolic pass).  A level record is two int4: {W, log2 lanes per row, entry slots per
+// lane, first entry slot} and {row base, diagonal slot base, flags, 0}; lane lam of the
+// level handles row lam >> lsh with its entries j = lam % spl + i spl (slot first + i W +
+// lam), visited in the same order as df_level / df_level_split and padded with exact
+// zeros, so the results are identical.  Flag bit 0: the level has at most 32 lanes and
+// runs on the group's first warp alone; bit 1: so does the next level, and a warp barrier
+// separates the two instead of a group barrier.
 struct IlProg {
-  const int *lrec, *urec;          // level records, 8 ints each
+  const int4 *rec;                 // level records (L levels from level 1, then U levels)
   const int *rows;                 // positions of the levels' rows
-  const unsigned short *cols;      // interleaved columns
+  const unsigned short *cols;      // column of every entry slot
   const df *lui;                   // interleaved factors (this instance's region)
   int nl, nu;                      // L levels (from level 1), U levels
 };
 
-template <bool UPPER>
-__device__ __forceinline__ df il_lane(const int *rec, const IlProg &I, const df *y, int lam, int &k, int &r) {
-  const int W = rec[0], spl = rec[1], mc = rec[2];
-  r = lam / spl;
-  k = I.rows[rec[5] + r];
-  const int sub = lam & (spl - 1);
-  df s = sub == 0 ? y[k] : df{0.f, 0.f};
-  const df *a = I.lui + rec[3] + lam;
-  const unsigned short *c = I.cols + rec[4] + lam;
-  int i = 0;
-  for (; i + 3 < mc; i += 4) {  // four entries' loads in flight
-    df av[4], yv[4];
+// One level on GG threads (gl < GG).  Lane lam = base + gl (and base + GG + gl when the
+// level is wider than GG); a lane past the level's width repeats the loads of its last
+// lane (in range) and drops the result, so loop trip counts and shuffles are uniform over
+// each warp and the rows of a lane group are never split (W is a multiple of spl).
+template <int GG, bool UPPER>
+__device__ __forceinline__ void il_level(const int4 A, const int4 B, const IlProg &I, df *y, int gl) {
+  const int W = A.x, lsh = A.y, mc = A.z, spl = 1 << lsh;
+  for (int base = 0; base < W; base += 2 * GG) {
+    const int lam0 = min(base + gl, W - 1);
+    const int r0 = lam0 >> lsh;
+    const int k0 = I.rows[B.x + r0];
+    const bool w0 = base + gl < W && (lam0 & (spl - 1)) == 0;
+    df s0 = (lam0 & (spl - 1)) == 0 ? y[k0] : df{0.f, 0.f};
+    df d0{0.f, 0.f};
+    if (UPPER) d0 = I.lui[B.y + r0];
+    int o0 = A.w + lam0;
+    if (base + GG < W) {  // a second lane per thread (uniform over the group)
+      const int lam1 = min(base + GG + gl, W - 1);
+      const int r1 = lam1 >> lsh;
+      const int k1 = I.rows[B.x + r1];
+      const bool w1 = base + GG + gl < W && (lam1 & (spl - 1)) == 0;
+      df s1 = (lam1 & (spl - 1)) == 0 ? y[k1] : df{0.f, 0.f};
+      df d1{0.f, 0.f};
+      if (UPPER) d1 = I.lui[B.y + r1];
+      int o1 = A.w + lam1;
+      int i = 0;
+      for (; i + 1 < mc; i += 2) {  // two entries of each lane in flight
+        const df a0 = I.lui[o0], a1 = I.lui[o1], b0 = I.lui[o0 + W], b1 = I.lui[o1 + W];
+        const df y0 = y[I.cols[o0]], y1 = y[I.cols[o1]], z0 = y[I.cols[o0 + W]], z1 = y[I.cols[o1 + W]];
+        s0 = df_fma_acc(df_neg(a0), y0, s0);
+        s1 = df_fma_acc(df_neg(a1), y1, s1);
+        s0 = df_fma_acc(df_neg(b0), z0, s0);
+        s1 = df_fma_acc(df_neg(b1), z1, s1);
+        o0 += 2 * W;
+        o1 += 2 * W;
+      }
+      if (i < mc) {
+        const df a0 = I.lui[o0], a1 = I.lui[o1];
+        const df y0 = y[I.cols[o0]], y1 = y[I.cols[o1]];
+        s0 = df_fma_acc(df_neg(a0), y0, s0);
+        s1 = df_fma_acc(df_neg(a1), y1, s1);
+      }
+      s0 = df_norm(s0);
+      s1 = df_norm(s1);
+      for (int o = spl >> 1; o > 0; o >>= 1) {
+        df t0, t1;
+        t0.hi = __shfl_xor_sync(kFull, s0.hi, o);
+        t0.lo = __shfl_xor_sync(kFull, s0.lo, o);
+        t1.hi = __shfl_xor_sync(kFull, s1.hi, o);
+        t1.lo = __shfl_xor_sync(kFull, s1.lo, o);
+        s0 = df_add(s0, t0);
+        s1 = df_add(s1, t1);
+      }
+      if (w0) y[k0] = UPPER ? df_mul(s0, d0) : s0;
+      if (w1) y[k1] = UPPER ? df_mul(s1, d1) : s1;
+    } else {
+      int i = 0;
+      for (; i + 3 < mc; i += 4) {  // four entries in flight
+        df av[4], yv[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      av[q] = a[(size_t)(i + q) * W];
-      yv[q] = y[c[(i + q) * W]];
+        for (int q = 0; q < 4; ++q) {
+          av[q] = I.lui[o0 + q * W];
+          yv[q] = y[I.cols[o0 + q * W]];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) s0 = df_fma_acc(df_neg(av[q]), yv[q], s0);
+        o0 += 4 * W;
+      }
+      for (; i < mc; ++i, o0 += W) s0 = df_fma_acc(df_neg(I.lui[o0]), y[I.cols[o0]], s0);
+      s0 = df_norm(s0);
+      for (int o = spl >> 1; o > 0; o >>= 1) {
+        df t0;
+        t0.hi = __shfl_xor_sync(kFull, s0.hi, o);
+        t0.lo = __shfl_xor_sync(kFull, s0.lo, o);
+        s0 = df_add(s0, t0);
+      }
+      if (w0) y[k0] = UPPER ? df_mul(s0, d0) : s0;
     }
-#pragma unroll
-    for (int q = 0; q < 4; ++q) s = df_fma_acc(df_neg(av[q]), yv[q], s);
   }
-  for (; i < mc; ++i) s = df_fma_acc(df_neg(a[(size_t)i * W]), y[c[i * W]], s);
-  return df_norm(s);
 }
 
-template <int G, bool UPPER>
-__device__ __forceinline__ void il_level(const int *rec, const IlProg &I, df *y, int gl) {
-  const int W = rec[0], spl = rec[1];
-  const unsigned mask = lane_mask(spl);
-  for (int lam = gl; lam < W; lam += 2 * G) {  // two lanes' rows in flight per thread
-    const bool two = lam + G < W;
-    int k0, r0, k1 = -1, r1 = 0;
-    df v0 = il_lane<UPPER>(rec, I, y, lam, k0, r0);
-    df v1{0.f, 0.f};
-    if (two) v1 = il_lane<UPPER>(rec, I, y, lam + G, k1, r1);
-    if (spl > 1) {
-      v0 = df_lane_sum(v0, spl, mask);
-      if (two) v1 = df_lane_sum(v1, spl, mask);
-    }
-    if ((lam & (spl - 1)) == 0) {
-      y[k0] = UPPER ? df_mul(v0, I.lui[rec[6] + r0]) : v0;
-      if (two) y[k1] = UPPER ? df_mul(v1, I.lui[rec[6] + r1]) : v1;
-    }
-  }
-}
-
+// L then U solve in place on y; every thread of the group calls it, and it returns after
+// a group barrier (y final).
 template <int G>
 __device__ __forceinline__ void il_solve(const IlProg &I, df *y, int gl, int gid) {
-  for (int l = 0; l < I.nl; ++l) {
-    il_level<G, false>(I.lrec + 8 * l, I, y, gl);
-    gsync<G>(gid);
+  const int nt = I.nl + I.nu;
+  for (int l = 0; l < nt; ++l) {
+    const int4 A = I.rec[2 * l], B = I.rec[2 * l + 1];
+    if (!(B.z & 1)) {
+      if (l < I.nl) il_level<G, false>(A, B, I, y, gl);
+      else il_level<G, true>(A, B, I, y, gl);
+    } else if (gl < 32) {
+      if (l < I.nl) il_level<32, false>(A, B, I, y, gl);
+      else il_level<32, true>(A, B, I, y, gl);
+    }
+    if (B.z & 2) __syncwarp();
+    else gsync<G>(gid);
   }
-  for (int l = 0; l < I.nu; ++l) {
-    il_level<G, true>(I.urec + 8 * l, I, y, gl);
-    gsync<G>(gid);
-  }
+}
+
+// FP64 value of a double-float (df_to_double_fast), flagging a non-finite result in st;
+// the fast path's parts are finite normal numbers, so only the general path can give one.
+__device__ __forceinline__ double df_out(df a, int &st) {
+  const unsigned hb = __float_as_uint(a.hi), lb = __float_as_uint(a.lo);
+  const unsigned he = (hb >> 23) & 0xff, le = (lb >> 23) & 0xff;
+  const bool lo_zero = (lb & 0x7fffffff) == 0;
+  if (he != 0 && he != 0xff && (lo_zero || (le != 0 && le != 0xff)))
+    return f32_widened(hb) + (lo_zero ? 0.0 : f32_widened(lb));
+  const double v = df_to_double(a);
+  if (!isfinite(v)) st |= KS_NONFINITE;
+  return v;
 }
 
 // Steps s_begin .. n_steps; the row of step s is out + (s - row_base) * n_out.
@@ -1472,7 +1537,7 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
                                          Probe pr = Probe{nullptr, 0, nullptr},
                                          AdjFwd af = AdjFwd{nullptr, 1, 0, 0, nullptr}, int s_begin = 1,
                                          int row_base = 0,
-                                         IlProg il = IlProg{nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0}) {
+                                         IlProg il = IlProg{nullptr, nullptr, nullptr, nullptr, 0, 0}) {
   const int n_out = pr.n ? pr.n : P.n;
   df loss{0.f, 0.f};  // adjoint forward pass: lane 0 of the group accumulates
   int st = 0;
@@ -1579,6 +1644,107 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
   return st;
 }
 
+// The interleaved step with a direct right-hand side (pack_lean), for the trapezoidal
+// rule with companion currents (as dfd_steps with CBREC) or backward Euler.  Each step
+// reads the previous solution in x, writes the right-hand side into b (every element
+// writes the rows it feeds, the rows no element feeds are zeroed: no gather pass and one
+// barrier less than dfd_steps), solves in place on b and writes the output row from b;
+// then x and b swap, so on return x holds the last solution.  lrec / zrow / qinv are the
+// staged direct right-hand-side records, unfed rows and output order.  cb holds the
+// capacitor companion values (on entry at s_begin = 1 the capacitor currents, resuming
+// the companion values a previous call left; on return the companion values).  Every
+// value is formed with the same operations in the same order as dfd_steps with the
+// gather (a row fed by one element takes 0 + v = v exactly), so the results are
+// bit-identical to it.
+template <int G, bool TR>
+__device__ __forceinline__ int dfd_steps_lean(const DevProg &P, const int4 *lrec, const int *zrow, const int *qinv,
+                                              const IlProg &I, df *&x, df *&b, const df *cdyn, df *cb,
+                                              const double *vals, double h, int n_steps, int lag, double *out, int gl,
+                                              int gid, WaveTab wt, Probe pr, int s_begin, int row_base,
+                                              bool cvt64) {
+  const int n_out = pr.n ? pr.n : P.n;
+  const int ncap = P.ncap, nlc = P.ncap + P.n_ind, nd = P.ndyn, nz = P.n_zrow;
+  int st = 0;
+  int pf_d = -1;  // first tabulated source of this thread: next value loaded a step ahead
+  size_t pf_base = 0;
+  double pf_val = 0.0;
+  if (wt.tab && s_begin <= n_steps)
+    for (int d = nlc + gl; d < nd; d += G)
+      if ((int)((unsigned)lrec[d].x >> 24) == KRETS_ELEM_V && wt.row[d] >= 0) {
+        pf_d = d;
+        pf_base = (size_t)wt.row[d] * wt.stride;
+        pf_val = wt.tab[pf_base + s_begin];
+        break;
+      }
+  if (TR && s_begin == 1)  // capacitor currents -> companion values of step 0
+    for (int d = gl; d < ncap; d += G) {
+      const int4 r = lrec[d];
+      cb[d] = df_sub(df_mul(cdyn[d], df_sub(x[r.x], x[r.y])), cb[d]);
+    }
+  for (int s = s_begin; s <= n_steps; ++s) {
+    for (int d = gl; d < ncap; d += G) {
+      const int4 r = lrec[d];
+      const df vprev = df_sub(x[r.x], x[r.y]);
+      df v;
+      if (TR) {
+        const df c2{2.f * cdyn[d].hi, 2.f * cdyn[d].lo};  // exact doubling
+        v = df_fma(c2, vprev, df_neg(cb[d]));
+        cb[d] = v;
+      } else {
+        v = df_mul(cdyn[d], vprev);
+      }
+      b[r.z] = v;
+      b[r.w] = df_neg(v);
+    }
+    for (int d = ncap + gl; d < nlc; d += G) {
+      const int4 r = lrec[d];
+      const df li = df_neg(df_mul(cdyn[d], x[r.z]));
+      const df v = TR ? df_sub(li, df_sub(x[r.x], x[r.y])) : li;
+      b[r.w >> 1] = (r.w & 1) ? df_neg(v) : v;
+    }
+    for (int d = nlc + gl; d < nd; d += G) {
+      const int4 r = lrec[d];
+      df v;
+      if ((int)((unsigned)r.x >> 24) == KRETS_ELEM_V) {
+        if (d == pf_d) {
+          v = df_from_double(pf_val);
+          if (s < n_steps) pf_val = wt.tab[pf_base + s + 1];
+        } else {
+          const int e = r.x & 0xffffff;
+          const krets_element &E = P.el[e];
+          const int wr = wt.tab ? wt.row[d] : -1;
+          if (wr >= 0) v = df_from_double(wt.tab[(size_t)wr * wt.stride + s]);
+          else if (E.wave == KRETS_WAVE_NONE) v = cdyn[d];  // the DC value, split at set-up
+          else v = df_from_double(wave_value(E, vals ? vals[e] : E.value, lag ? (double)(s - 1) * h : (double)s * h));
+        }
+      } else {  // current source
+        v = cdyn[d];
+      }
+      b[r.z] = v;
+      b[r.w] = df_neg(v);
+    }
+    for (int i = gl; i < nz; i += G) b[zrow[i]] = df{0.f, 0.f};
+    gsync<G>(gid);  // b assembled (and every read of x done)
+    il_solve<G>(I, b, gl, gid);
+    double *row = out + (size_t)(s - row_base) * n_out;
+    if (cvt64) {  // conversions and the add on the FP64 pipe (same value as df_out)
+      for (int j = gl; j < n_out; j += G) {
+        const double v = df_to_double(b[qinv[pr.n ? pr.idx[j] : j]]);
+        if ((__double2hiint(v) & 0x7ff00000) == 0x7ff00000) st |= KS_NONFINITE;
+        __stcs(row + j, v);
+      }
+    } else {
+      for (int j = gl; j < n_out; j += G) __stcs(row + j, df_out(b[qinv[pr.n ? pr.idx[j] : j]], st));
+    }
+    // no barrier: the next step reads b (final since the last solve level) and writes the
+    // other buffer, whose last readers finished before this step's first barrier
+    df *t = x;
+    x = b;
+    b = t;
+  }
+  return st;
+}
+
 // A span of the time steps for one launch, so that a long transient can run as several
 // launches (each writing its rows to a staging buffer that is copied out while the next
 // launch runs).  Steps s_begin .. n_steps are computed; step s goes to output row
@@ -1594,7 +1760,9 @@ struct Span {
 };
 
 // opts bit 0: run narrow levels on one warp; bit 1: integer-only FP64 output conversion;
-// bit 2: trapezoidal capacitor history as companion currents (dfd_steps CBREC).
+// bit 2: trapezoidal capacitor history as companion currents (dfd_steps CBREC); bit 3: no
+// direct right-hand side (host side); bit 4: the direct-rhs step converts its output on
+// the FP64 pipe instead of widening the parts with integer instructions.
 // LUG: the factors live in global memory (an L2-resident region per group, lu_glob), the
 // rest of the instance in shared memory: about a third of the shared memory per instance,
 // so up to 14 instances share an SM (each step's critical path is a chain of level
@@ -1608,36 +1776,58 @@ __global__ void __launch_bounds__(896, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
   const int gl = threadIdx.x % G, gid = threadIdx.x / G;
   // With the factors in global memory and a 64 or 128-thread group the solves run from the
   // interleaved program, and only the step-program sections the step reads besides the
-  // solves are staged (rhs elements, rhs gather, output order, split codes): the row
-  // descriptors and columns of the row-descriptor solves stay in global memory.
+  // solves are staged: the row descriptors and columns of the row-descriptor solves stay
+  // in global memory.
   constexpr int gi = G == 128 ? 1 : 0;
   const bool il = LUG && (G == 64 || G == 128) && P.il_ok;
-  SProg S;
-  IlProg I{nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0};
-  if (il) {
-    const int w0 = P.sp_off[7], w1 = P.sp_off[5], iw0 = P.ip_off[gi][0], iw1 = P.ip_off[gi][3];
-    const int head = ((w1 - w0) + 3) & ~3;  // words, 16-byte aligned
-    const int4 *src = reinterpret_cast<const int4 *>(P.sprog + w0);
-    int4 *dst = reinterpret_cast<int4 *>(smem);
-    for (int i = threadIdx.x; i < (w1 - w0) / 4; i += blockDim.x) dst[i] = src[i];
+  // the host sized the layout for the direct right-hand-side step (L.lean); a program
+  // without one (never launched so) stages nothing and fails its instances
+  const bool bad_lean = L.lean && !(il && P.lean_ok);
+  const bool lean = L.lean && !bad_lean;
+  SProg S = SProg{};
+  IlProg I{nullptr, nullptr, nullptr, nullptr, 0, 0};
+  const int4 *lrec = nullptr;
+  const int *zrow = nullptr, *qinv = nullptr;
+  if (il && !bad_lean) {
+    // staged: the rhs sections (direct right-hand side, unfed rows and output order; or
+    // rhs elements, gather and output order), then the interleaved program
+    const int iw0 = P.ip_off[gi][0], iw1 = P.ip_off[gi][3];
+    int head;  // words before the interleaved program, 16-byte aligned
+    if (lean) {
+      const int lw = (4 * P.ndyn + P.n_zrow + 3) & ~3, qw = (P.n + 3) & ~3;
+      const int4 *src = reinterpret_cast<const int4 *>(P.iprog + P.lean_off);
+      int4 *dst = reinterpret_cast<int4 *>(smem);
+      for (int i = threadIdx.x; i < lw / 4; i += blockDim.x) dst[i] = src[i];
+      const int4 *qsrc = reinterpret_cast<const int4 *>(P.sprog + P.sp_off[10]);
+      for (int i = threadIdx.x; i < qw / 4; i += blockDim.x) dst[lw / 4 + i] = qsrc[i];
+      head = lw + qw;
+      const int *sm = reinterpret_cast<const int *>(smem);
+      lrec = reinterpret_cast<const int4 *>(sm);
+      zrow = sm + 4 * P.ndyn;
+      qinv = sm + lw;
+    } else {
+      const int w0 = P.sp_off[7], w1 = P.sp_off[5];
+      head = ((w1 - w0) + 3) & ~3;
+      const int4 *src = reinterpret_cast<const int4 *>(P.sprog + w0);
+      int4 *dst = reinterpret_cast<int4 *>(smem);
+      for (int i = threadIdx.x; i < (w1 - w0) / 4; i += blockDim.x) dst[i] = src[i];
+      const int *sm = reinterpret_cast<const int *>(smem);
+      S.dyn = reinterpret_cast<const int4 *>(sm + (P.sp_off[7] - w0));
+      S.bd_ptr = sm + (P.sp_off[8] - w0);
+      S.bd_op = sm + (P.sp_off[9] - w0);
+      S.qinv = sm + (P.sp_off[10] - w0);
+    }
     const int4 *isrc = reinterpret_cast<const int4 *>(P.iprog + iw0);
     int4 *idst = reinterpret_cast<int4 *>(smem + 4 * head);
     for (int i = threadIdx.x; i < (iw1 - iw0) / 4; i += blockDim.x) idst[i] = isrc[i];
     __syncthreads();
-    const int *sm = reinterpret_cast<const int *>(smem);
-    S = SProg{};
-    S.dyn = reinterpret_cast<const int4 *>(sm + (P.sp_off[7] - w0));
-    S.bd_ptr = sm + (P.sp_off[8] - w0);
-    S.bd_op = sm + (P.sp_off[9] - w0);
-    S.qinv = sm + (P.sp_off[10] - w0);
-    const int *ip = sm + head;
-    I.lrec = ip;
-    I.urec = ip + 8 * P.n_il_lrec;
+    const int *ip = reinterpret_cast<const int *>(smem) + head;
+    I.rec = reinterpret_cast<const int4 *>(ip);
     I.rows = ip + (P.ip_off[gi][1] - iw0);
     I.cols = reinterpret_cast<const unsigned short *>(ip + (P.ip_off[gi][2] - iw0));
     I.nl = P.n_il_lrec;
     I.nu = P.n_il_urec;
-  } else {
+  } else if (!bad_lean) {
     const int words = P.sp_off[5];  // everything before the residual operators
     const int4 *src = reinterpret_cast<const int4 *>(P.sprog);
     int4 *dst = reinterpret_cast<int4 *>(smem);
@@ -1655,6 +1845,8 @@ __global__ void __launch_bounds__(896, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
   const bool int_cvt = (opts & 2) != 0;
   // bit 2: trapezoidal capacitor history carried as the companion current (no adjoint pass)
   const bool cbrec = (opts & 4) != 0 && method == KRETS_METHOD_TR && !af.ck;
+  // the direct right-hand-side step runs TR with companion currents, or BE
+  const bool lean_ok = lean && !af.ck && (cbrec || method == KRETS_METHOD_BE);
   char *base = smem + L.sprog_bytes + (size_t)gid * L.bytes;
   // global-memory factors: per group the CSR factors, then (interleaved solves) their
   // interleaved copy
@@ -1699,13 +1891,28 @@ __global__ void __launch_bounds__(896, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
       for (int j = gl; j < pr.n; j += G) out[j] = op[pr.idx[j]];  // probe row 0
       for (int d = gl; d < P.ncap; d += G) icap[d] = df{0.f, 0.f};
     }
+    if (lean && gl == 0) {  // ground reads zero in both state buffers
+      x[P.n] = df{0.f, 0.f};
+      cb[P.n] = df{0.f, 0.f};
+    }
+    if (bad_lean || (lean && !lean_ok)) st |= KS_NOTIMPL;
     AdjFwd a = af;
     if (af.ck) {
       a.ck = af.ck + (size_t)inst * ((n_steps + af.K - 1) / af.K) * af.ck_words;
       a.loss = af.loss + inst;
     }
     const bool fatal = gany<G>((st & (KS_SINGULAR | KS_NONFINITE | KS_NOTIMPL)) != 0, gid);
-    if (!fatal) {
+    df *xfin = x;  // where the last solution is
+    if (!fatal && lean) {
+      df *xs = x, *bs = cb;
+      if (cbrec)
+        st |= dfd_steps_lean<G, true>(P, lrec, zrow, qinv, I, xs, bs, cdyn, icap, vals, h, n_steps, lag, out, gl,
+                                      gid, wt, pr, sp.s_begin, sp.row_base, (opts & 16) != 0);
+      else
+        st |= dfd_steps_lean<G, false>(P, lrec, zrow, qinv, I, xs, bs, cdyn, icap, vals, h, n_steps, lag, out, gl,
+                                       gid, wt, pr, sp.s_begin, sp.row_base, (opts & 16) != 0);
+      xfin = xs;
+    } else if (!fatal) {
       if (cbrec)
         st |= dfd_steps<G, G, true, false>(P, S, lu, x, cdyn, cb, icap, vals, h, n_steps, method, lag, out, lnar, unar,
                                     int_cvt, gl, gid, wt, pr, a, sp.s_begin, sp.row_base, I);
@@ -1715,7 +1922,7 @@ __global__ void __launch_bounds__(896, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
     }
     if (state) {  // the last step's solution level and TR currents are final once the group syncs
       gsync<G>(gid);
-      for (int k = gl; k < P.n; k += G) state[k] = x[k];
+      for (int k = gl; k < P.n; k += G) state[k] = xfin[k];
       for (int d = gl; d < P.ncap; d += G) state[P.n + d] = icap[d];
     }
     if (gl == 0) slot[1] = 0;

@@ -404,3 +404,44 @@ def test_factor_placements_give_identical_bits(oracle_lib, monkeypatch, G):
         ti["value"] = vals[0]
         ref = oracle_lib.tran(ti, n, h, 300, method=method, lag=lag)
         assert normwise_err(outs["global"][0], ref, mask) < TOL
+
+
+MIXED_DIRECT = ("V1 in 0 SIN(0 1 1e9 0 0 0)\nR1 in a 50\nL1 a b 1n\nC1 b 0 1p\nR2 b c 100\n"
+                "C3 c d 1p\nR3 d 0 1k\nI1 e 0 1m\nR4 e 0 1k\n")
+
+
+@pytest.mark.parametrize("G", ["64", "128"])
+def test_direct_rhs_step_gives_identical_bits(oracle_lib, monkeypatch, G):
+    """The interleaved double-float step with a direct right-hand side (each element writes
+    the rows it feeds, no gather pass; output converted on the FP64 pipe or by integer
+    widening) and the one with the gather pass (KRETS_DFD_OPTS bit 3) give identical bits: TR with companion currents and BE on the RLC ladder, and TR on
+    a netlist with a floating capacitor, a current source and a tabulated SIN source; also
+    when the transient runs as spans resuming from saved state (staged host output).
+    Against the oracle in both error measures."""
+    c = rlc_ladder(100)
+    m = parse_circuit_description(MIXED_DIRECT)
+    cases = [(c, "tr", 1e-12, monte_carlo_values(c, 20, seed=6)),
+             (c, "be", 1e-12, monte_carlo_values(c, 7, seed=8)),
+             (m, "tr", 2e-11, monte_carlo_values(m, 9, seed=3))]
+    monkeypatch.setenv("KRETS_GROUP", G)
+    monkeypatch.setenv("KRETS_DFD_LU", "global")
+    for ckt, method, h, vals in cases:
+        t = element_table(ckt)
+        outs = {}
+        # 20: the default (direct rhs, output converted on the FP64 pipe), 4: direct rhs with
+        # integer widening of the output, 12: the gather pass
+        for opts in ("20", "4", "12"):
+            monkeypatch.setenv("KRETS_DFD_OPTS", opts)
+            g = _lib.GpuCircuit(t, ckt.size)
+            outs[opts] = g.batch_tran(vals, h, 300, method, lag=False, precision=_lib.PREC_DF)
+        np.testing.assert_array_equal(outs["20"], outs["12"])
+        np.testing.assert_array_equal(outs["4"], outs["12"])
+        monkeypatch.delenv("KRETS_DFD_OPTS")
+        monkeypatch.setenv("KRETS_HOST_OUT", "staged")
+        spans = _lib.GpuCircuit(t, ckt.size).batch_tran(vals, h, 300, method, lag=False, precision=_lib.PREC_DF)
+        monkeypatch.delenv("KRETS_HOST_OUT")
+        np.testing.assert_array_equal(spans, outs["20"])
+        ti = t.copy()
+        ti["value"] = vals[-1]
+        ref = oracle_lib.tran(ti, ckt.size, h, 300, method=method, lag=False)
+        assert rel_err(outs["20"][-1], ref, is_current_mask(ckt)) < TOL

@@ -217,20 +217,30 @@ def _il_solve(P, vals, b, gi):
     imap = P["imap"][int(off[10 + gi]):int(off[10 + gi]) + slots]
     lui = np.where(imap >= 0, vals[np.maximum(imap, 0)], 0.0)
     y = b.copy()
-    for li, (W, spl, mc, base, cbase, rbase, dbase, _) in enumerate(rec):
+    n_entry = 0
+    for li, (W, lsh, mc, first, rbase, dbase, flags, _) in enumerate(rec):
         upper = li >= nl
+        spl = 1 << lsh
+        assert W % spl == 0 and (dbase >= 0) == upper
+        # bit 0: a level of at most 32 lanes (first warp alone); bit 1: so is the next one
+        narrow_next = li + 1 < len(rec) and rec[li + 1][0] <= 32
+        assert flags == (W <= 32) | (2 * (W <= 32 and narrow_next))
+        assert first == n_entry
+        n_entry += mc * W
         sums = {}
         for lam in range(W):
             r, sub = divmod(lam, spl)
             k = rows[rbase + r]
             s = y[k] if sub == 0 else 0.0
             for i in range(mc):
-                s -= lui[base + i * W + lam] * y[cols[cbase + i * W + lam]]
+                slot = first + i * W + lam
+                s -= lui[slot] * y[cols[slot]]
             sums.setdefault(r, []).append(s)
         for r, parts in sums.items():
             k = rows[rbase + r]
             v = sum(parts)
             y[k] = v * lui[dbase + r] if upper else v
+    assert len(cols) >= n_entry
     return y, imap, slots
 
 
@@ -279,3 +289,60 @@ def test_interleaved_solve_program_equals_row_solves(built_lib, which):
         y, imap, slots = _il_solve(P, vals, b, gi)
         assert sorted(imap[imap >= 0].tolist()) == want
         np.testing.assert_allclose(y, ref, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("which", ["rlc200", "rc300", "uneven6", "rlc_sin"])
+def test_direct_rhs_program_equals_gather(built_lib, which):
+    """The direct right-hand side of the interleaved double-float step (every element
+    writes the rows it feeds, unfed rows are zeroed) forms the same right-hand side as the
+    gather pass over the step program's rhs operators, for any element values; a netlist
+    with a row fed by two elements has no direct program."""
+    from krets_gb300.generators import rc_ladder_step, rlc_ladder, uneven_table
+    from krets_gb300.netlist import parse_circuit_description
+    if which == "rlc200":
+        c = rlc_ladder(200)
+        t, n = element_table(c), c.size
+    elif which == "rc300":
+        c = rc_ladder_step(300)
+        t, n = element_table(c), c.size
+    elif which == "rlc_sin":
+        # a floating capacitor (two rows, opposite signs) and a current source
+        c = parse_circuit_description("V1 in 0 SIN(0 1 1e9 0 0 0)\nR1 in a 50\nL1 a b 1n\nC1 b 0 1p\n"
+                                      "R2 b c 100\nC3 c d 1p\nR3 d 0 1k\nI1 e 0 1m\nR4 e 0 1k\n")
+        t, n = element_table(c), c.size
+    else:
+        t, n = uneven_table(6)
+    P = built_lib.symbolic_export(t, n, built_lib.MODE_TRAN, "tr", 1e-12)
+    off, sp, spo = P["ipoff"], P["sprog"], P["spoff"]
+    lean_off, n_zrow, n_ind, lean_ok = (int(v) for v in off[15:19])
+    dyn = sp[spo[7]:spo[8]].reshape(-1, 4)
+    nd = len(dyn)
+    bd_ptr = sp[spo[8]:spo[8] + n + 1]
+    bd_op = sp[spo[9]:spo[9] + int(bd_ptr[-1])]
+    kinds = dyn[:, 0] >> 24
+    fed_twice = np.any(np.diff(bd_ptr) > 1)
+    if fed_twice:
+        assert lean_ok == 0 and which == "uneven6"
+        return
+    assert lean_ok == 1
+    ncap = int(np.sum(kinds == 2))   # KRETS_ELEM_C, then KRETS_ELEM_L
+    assert np.all(kinds[:ncap] == 2) and np.all(kinds[ncap:ncap + n_ind] == 3) and n_ind == np.sum(kinds == 3)
+    rng = np.random.default_rng(5)
+    cb = rng.standard_normal(nd)
+    ref = np.zeros(n)
+    for k in range(n):
+        for u in range(bd_ptr[k], bd_ptr[k + 1]):
+            ref[k] += -cb[bd_op[u] >> 1] if bd_op[u] & 1 else cb[bd_op[u] >> 1]
+    L = P["iprog"][lean_off:lean_off + 4 * nd].reshape(-1, 4)
+    zrow = P["iprog"][lean_off + 4 * nd:lean_off + 4 * nd + n_zrow]
+    b = np.full(n + 2, np.nan)
+    for d in range(nd):
+        if ncap <= d < ncap + n_ind:            # inductor: {p, m, branch, row << 1 | neg}
+            p, m, w, rw = L[d]
+            assert w == dyn[d][3] and {int(p), int(m)} <= set(range(n + 1))
+            b[rw >> 1] = -cb[d] if rw & 1 else cb[d]
+        else:                                   # {p, m | e|kind, 0, row +, row -}
+            b[L[d][2]] = cb[d]
+            b[L[d][3]] = -cb[d]
+    b[zrow] = 0.0
+    np.testing.assert_array_equal(b[:n], ref)
