@@ -358,7 +358,8 @@ krets_status krets_batch_tran_noalloc(krets_circuit *c, int32_t n_inst, const do
 #define KRETS_PROG_SPOFF 24 /* its section offsets (16), border chunk and row counts */
 #define KRETS_PROG_IPROG 25 /* interleaved solve programs (transient mode, single circuit) */
 #define KRETS_PROG_IPOFF 26 /* {ip_off[2][4], il_slots[2], imap_off[2], n_il_lrec, n_il_urec, il_ok,
-                               lean_off, n_zrow, n_ind, lean_ok} */
+                               lean_off, n_zrow, n_ind, lean_ok, ip_off[4], il_slots, imap_off}:
+                               layouts for 64, 128 and (last) 32-thread groups */
 #define KRETS_PROG_IMAP 27  /* interleaved factor slot -> CSR slot (-1: zero pad) */
 #define KRETS_MODE_DC 0
 #define KRETS_MODE_AC 1

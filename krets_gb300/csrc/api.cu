@@ -309,7 +309,7 @@ static void place_program(const Program &H, const ProgramImage &X, const krets_e
   V.xslot = (const int *)nx();
   V.iprog = (const int *)nx();
   V.imap = (const int *)nx();
-  for (int gi = 0; gi < 2; ++gi) {
+  for (int gi = 0; gi < 3; ++gi) {
     for (int k = 0; k < 4; ++k) V.ip_off[gi][k] = H.ip_off[gi][k];
     V.il_slots[gi] = H.il_slots[gi];
     V.imap_off[gi] = H.imap_off[gi];
@@ -1095,9 +1095,12 @@ struct DfdLaunch {
   int slots() const { return W * per_sm * device_sm_count(); }
 };
 
-// Interleaved solves: factors in global memory, a 64 or 128-thread group, and a program
-// that has them (k_tran_dfd).
-bool dfd_interleaved(const DevProg &P, bool lug, int G) { return lug && (G == 64 || G == 128) && P.il_ok; }
+// Interleaved solves: factors in global memory and a program that has them (k_tran_dfd;
+// one layout per group size).
+bool dfd_interleaved(const DevProg &P, bool lug, int G) { return lug && P.il_ok; }
+
+// interleaved layout of a group size (G = 64, 128, 32)
+int il_layout(int G) { return G == 64 ? 0 : G == 128 ? 1 : 2; }
 
 // The interleaved step with a direct right-hand side (dfd_steps_lean): a program that has
 // one, TR with companion currents (opts bit 2) or BE; opts bit 3 turns it off.
@@ -1131,7 +1134,7 @@ bool dfd_layout(const DevProg &P, DfdLay &DL, bool lug = false, int G = 64, int 
   if (cur - DL.x < 8 * (size_t)P.ne) cur = DL.x + align16(8 * (size_t)P.ne);
   put(DL.slot, 16);
   DL.bytes = (int)align16(cur);
-  const int gi = G == 128 ? 1 : 0;
+  const int gi = il_layout(G);
   if (lean) {  // direct rhs records and unfed rows, output order, then the interleaved program
     DL.sprog_bytes = (int)(sizeof(int) * ((4 * (size_t)P.ndyn + P.n_zrow + 3) & ~(size_t)3) +
                            sizeof(int) * (((size_t)P.n + 3) & ~(size_t)3) +
@@ -1168,7 +1171,7 @@ krets_status dfd_lu_buffer(krets_circuit *c, const DfdLaunch &Lc, int grid, cons
   *out = nullptr;
   if (!Lc.lug) return KRETS_OK;
   // per group: the CSR factors, then (interleaved solves) their interleaved copy
-  const size_t per = (size_t)P.nnz_lu + (dfd_interleaved(P, true, Lc.G) ? (size_t)P.il_slots[Lc.G == 128 ? 1 : 0] : 0);
+  const size_t per = (size_t)P.nnz_lu + (dfd_interleaved(P, true, Lc.G) ? (size_t)P.il_slots[il_layout(Lc.G)] : 0);
   const size_t bytes = sizeof(df) * per * grid * Lc.W;
   krets_status s = c->ensure_lug(bytes);
   if (s != KRETS_OK) return s;
@@ -1209,7 +1212,7 @@ krets_status dfd_pick(krets_circuit *c, const DevProgram *D, const double *dv, c
   }
   const DevProg &P = D->view;
   struct Cand { int G; bool lug; };
-  const Cand cands[] = {{128, false}, {64, false}, {32, false}, {128, true}, {64, true}};
+  const Cand cands[] = {{128, false}, {64, false}, {32, false}, {128, true}, {64, true}, {32, true}};
   std::vector<DfdLaunch> cfg;
   std::vector<DfdLay> lay;
   int trial_max = 1;

@@ -115,7 +115,7 @@ struct DevProg {
   int tail0, tail_m;  // dense trailing block of the LU (tail_m = 0: none)
   // interleaved solves (Program::iprog; layouts for 64 and 128-thread groups)
   const int *iprog, *imap;
-  int ip_off[2][4], il_slots[2], imap_off[2], n_il_lrec, n_il_urec, il_ok;
+  int ip_off[3][4], il_slots[3], imap_off[3], n_il_lrec, n_il_urec, il_ok;  // layouts: G = 64, 128, 32
   int lean_off, n_zrow, n_ind, lean_ok;  // direct right-hand side (in iprog)
 };
 

@@ -473,8 +473,8 @@ static void pack_interleaved(Program &P) {
   if (!P.sprog_ok || P.tail_m || P.n > 65535) return;
   const int *lmax = P.sprog.data() + P.sp_off[12], *umax = P.sprog.data() + P.sp_off[13];
   const int nlev = (int)P.lev_ptr.size() - 1, nulev = (int)P.ulev_ptr.size() - 1;
-  for (int gi = 0; gi < 2; ++gi) {
-    const int g = gi == 0 ? 1 : 2;  // split-code field of 64 / 128-thread groups
+  for (int gi = 0; gi < 3; ++gi) {
+    const int g = gi == 0 ? 1 : gi == 1 ? 2 : 0;  // split-code field of 64 / 128 / 32-thread groups
     std::vector<int> rec, rows, emap, dmap;
     std::vector<unsigned short> cols;
     auto level = [&](bool upper, int l) {
@@ -1231,6 +1231,8 @@ extern "C" krets_status krets_symbolic_export(const krets_element *elems, int32_
         for (int k = 0; k < 4; ++k) v.push_back(P.ip_off[gi][k]);
       v.insert(v.end(), {P.il_slots[0], P.il_slots[1], P.imap_off[0], P.imap_off[1], P.n_il_lrec, P.n_il_urec,
                          P.il_ok ? 1 : 0, P.lean_off, P.n_zrow, P.n_ind, P.lean_ok ? 1 : 0});
+      for (int k = 0; k < 4; ++k) v.push_back(P.ip_off[2][k]);  // the 32-thread layout
+      v.insert(v.end(), {P.il_slots[2], P.imap_off[2]});
     } else if (which == KRETS_PROG_TPROG) v.assign(P.tprog.begin(), P.tprog.end());
     else if (which == KRETS_PROG_SPROG) v.assign(P.sprog.begin(), P.sprog.end());
     else if (which == KRETS_PROG_SPOFF) {

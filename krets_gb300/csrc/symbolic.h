@@ -84,7 +84,7 @@ struct Program {
   // lu_rowptr[k+1] - m .. lu_rowptr[k+1] - 1 (columns tail0 .. n-1).
   int tail0 = 0, tail_m = 0;
   // Interleaved solve programs of the double-float engine with its factors in global
-  // memory, one per group size (layout 0: 64 threads, 1: 128; see pack_interleaved).
+  // memory, one per group size (layout 0: 64 threads, 1: 128, 2: 32; see pack_interleaved).
   // Per level of the L solve (levels 1..) and of the U solve: a record
   //   {W lanes, log2 lanes per row, entry slots per lane, first entry slot, row base,
   //    diagonal slot base (U; -1 for L), flags, 0}
@@ -93,9 +93,9 @@ struct Program {
   // diagonals after all entry slots.  imap: interleaved slot -> CSR slot (-1: a zero pad).
   // Then (pack_lean) the direct right-hand-side records at lean_off.
   std::vector<int> iprog, imap;
-  int ip_off[2][4] = {{0}};  // records, rows, columns, end (ints into iprog)
-  int il_slots[2] = {0, 0};
-  int imap_off[2] = {0, 0};
+  int ip_off[3][4] = {{0}};  // records, rows, columns, end (ints into iprog)
+  int il_slots[3] = {0, 0, 0};
+  int imap_off[3] = {0, 0, 0};
   int n_il_lrec = 0, n_il_urec = 0;
   bool il_ok = false;
   int lean_off = 0, n_zrow = 0;  // direct right-hand side (pack_lean)

@@ -1464,18 +1464,14 @@ __device__ __forceinline__ void il_level(const int4 A, const int4 B, const IlPro
       if (w1) y[k1] = UPPER ? df_mul(s1, d1) : s1;
     } else {
       int i = 0;
-      for (; i + 3 < mc; i += 4) {  // four entries in flight
-        df av[4], yv[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          av[q] = I.lui[o0 + q * W];
-          yv[q] = y[I.cols[o0 + q * W]];
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) s0 = df_fma_acc(df_neg(av[q]), yv[q], s0);
-        o0 += 4 * W;
+      for (; i + 1 < mc; i += 2) {  // two entries in flight
+        const df a0 = I.lui[o0], b0 = I.lui[o0 + W];
+        const df y0 = y[I.cols[o0]], z0 = y[I.cols[o0 + W]];
+        s0 = df_fma_acc(df_neg(a0), y0, s0);
+        s0 = df_fma_acc(df_neg(b0), z0, s0);
+        o0 += 2 * W;
       }
-      for (; i < mc; ++i, o0 += W) s0 = df_fma_acc(df_neg(I.lui[o0]), y[I.cols[o0]], s0);
+      if (i < mc) s0 = df_fma_acc(df_neg(I.lui[o0]), y[I.cols[o0]], s0);
       s0 = df_norm(s0);
       for (int o = spl >> 1; o > 0; o >>= 1) {
         df t0;
@@ -1488,23 +1484,24 @@ __device__ __forceinline__ void il_level(const int4 A, const int4 B, const IlPro
   }
 }
 
+// Levels l0 .. l1 - 1 of one triangle, each followed by the barrier its flags ask for.
+template <int G, bool UPPER>
+__device__ __forceinline__ void il_levels(const IlProg &I, df *y, int l0, int l1, int gl, int gid) {
+  for (int l = l0; l < l1; ++l) {
+    const int4 A = I.rec[2 * l], B = I.rec[2 * l + 1];
+    if (!(B.z & 1)) il_level<G, UPPER>(A, B, I, y, gl);
+    else if (gl < 32) il_level<32, UPPER>(A, B, I, y, gl);
+    if (B.z & 2) __syncwarp();
+    else gsync<G>(gid);
+  }
+}
+
 // L then U solve in place on y; every thread of the group calls it, and it returns after
 // a group barrier (y final).
 template <int G>
 __device__ __forceinline__ void il_solve(const IlProg &I, df *y, int gl, int gid) {
-  const int nt = I.nl + I.nu;
-  for (int l = 0; l < nt; ++l) {
-    const int4 A = I.rec[2 * l], B = I.rec[2 * l + 1];
-    if (!(B.z & 1)) {
-      if (l < I.nl) il_level<G, false>(A, B, I, y, gl);
-      else il_level<G, true>(A, B, I, y, gl);
-    } else if (gl < 32) {
-      if (l < I.nl) il_level<32, false>(A, B, I, y, gl);
-      else il_level<32, true>(A, B, I, y, gl);
-    }
-    if (B.z & 2) __syncwarp();
-    else gsync<G>(gid);
-  }
+  il_levels<G, false>(I, y, 0, I.nl, gl, gid);
+  il_levels<G, true>(I, y, I.nl, I.nl + I.nu, gl, gid);
 }
 
 // FP64 value of a double-float (df_to_double_fast), flagging a non-finite result in st;
@@ -1774,12 +1771,11 @@ __global__ void __launch_bounds__(896, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
                                                      AdjFwd af, Span sp, df *lu_glob) {
   extern __shared__ __align__(16) char smem[];
   const int gl = threadIdx.x % G, gid = threadIdx.x / G;
-  // With the factors in global memory and a 64 or 128-thread group the solves run from the
-  // interleaved program, and only the step-program sections the step reads besides the
+  // With the factors in global memory the solves run from the interleaved program, and only the step-program sections the step reads besides the
   // solves are staged: the row descriptors and columns of the row-descriptor solves stay
   // in global memory.
-  constexpr int gi = G == 128 ? 1 : 0;
-  const bool il = LUG && (G == 64 || G == 128) && P.il_ok;
+  constexpr int gi = G == 64 ? 0 : G == 128 ? 1 : 2;
+  const bool il = LUG && P.il_ok;
   // the host sized the layout for the direct right-hand-side step (L.lean); a program
   // without one (never launched so) stages nothing and fails its instances
   const bool bad_lean = L.lean && !(il && P.lean_ok);

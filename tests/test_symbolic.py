@@ -204,17 +204,19 @@ def test_multi_circuit_program_dense_tail_solves(built_lib, oracle_lib):
 
 
 def _il_solve(P, vals, b, gi):
-    """Emulate the interleaved L and U solves of layout gi (64 / 128-thread groups) in FP64."""
+    """Emulate the interleaved L and U solves of layout gi (64 / 128 / 32-thread groups) in FP64."""
     off = P["ipoff"]
-    rec0, rows0, cols0, end = off[4 * gi:4 * gi + 4]
+    # layouts 0 and 1 first, the 32-thread layout's offsets, slots and map base at the end
+    base4, slot_at, map_at = (4 * gi, 8 + gi, 10 + gi) if gi < 2 else (19, 23, 24)
+    rec0, rows0, cols0, end = off[base4:base4 + 4]
     nl, nu = int(off[12]), int(off[13])
     ip = P["iprog"]
     rec = ip[rec0:rows0].reshape(-1, 8)[:nl + nu]
     rows = ip[rows0:cols0]
     packed = ip[cols0:end].astype(np.int64)
     cols = np.stack([packed & 0xffff, (packed >> 16) & 0xffff], axis=1).reshape(-1)
-    slots = int(off[8 + gi])
-    imap = P["imap"][int(off[10 + gi]):int(off[10 + gi]) + slots]
+    slots = int(off[slot_at])
+    imap = P["imap"][int(off[map_at]):int(off[map_at]) + slots]
     lui = np.where(imap >= 0, vals[np.maximum(imap, 0)], 0.0)
     y = b.copy()
     n_entry = 0
@@ -263,7 +265,7 @@ def test_interleaved_solve_program_equals_row_solves(built_lib, which):
     """The interleaved ("ELL per level") solve program of the double-float engine (factors
     in global memory): every L entry of levels 1.. and every U entry appears exactly once,
     each U row's reciprocal diagonal once, pads are zero; emulated in FP64 it solves the
-    same triangular systems as the row-descriptor program, for both group-size layouts."""
+    same triangular systems as the row-descriptor program, for the three group-size layouts."""
     from krets_gb300.generators import rc_ladder_step, rlc_ladder, uneven_table
     if which == "rlc200":
         c = rlc_ladder(200)
@@ -285,7 +287,7 @@ def test_interleaved_solve_program_equals_row_solves(built_lib, which):
     level0 = set(P["lev_rows"][P["lev_ptr"][0]:P["lev_ptr"][1]].tolist())
     want = sorted([s for k in range(n) if k not in level0 for s in range(rp[k], dg[k])]
                   + [s for k in range(n) for s in range(dg[k] + 1, rp[k + 1])] + list(dg))
-    for gi in (0, 1):
+    for gi in (0, 1, 2):
         y, imap, slots = _il_solve(P, vals, b, gi)
         assert sorted(imap[imap >= 0].tolist()) == want
         np.testing.assert_allclose(y, ref, rtol=1e-12, atol=1e-12)
