@@ -200,6 +200,7 @@ class MultiCircuit:
         off = np.zeros(len(self.tables) + 1, dtype=np.int64)
         off[1:] = np.cumsum([len(t) for t in self.tables])
         self.method = method
+        self.h = None
         h_ = ctypes.c_void_p()
         check(lib().krets_multi_create(len(self.tables), ptr(el), ptr(off), ptr(self.sizes), METHOD[method], h,
                                        ctypes.byref(h_)), "multi_create")

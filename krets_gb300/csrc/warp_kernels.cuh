@@ -1418,8 +1418,9 @@ __device__ __forceinline__ void il_level(const int4 A, const int4 B, const IlPro
     const int lam0 = min(base + gl, W - 1);
     const int r0 = lam0 >> lsh;
     const int k0 = I.rows[B.x + r0];
-    const bool w0 = base + gl < W && (lam0 & (spl - 1)) == 0;
-    df s0 = (lam0 & (spl - 1)) == 0 ? y[k0] : df{0.f, 0.f};
+    const bool f0 = (lam0 & (spl - 1)) == 0, w0 = base + gl < W && f0;
+    const df t0 = y[k0];  // in range for every lane; kept only by a row's first lane
+    df s0{f0 ? t0.hi : 0.f, f0 ? t0.lo : 0.f};
     df d0{0.f, 0.f};
     if (UPPER) d0 = I.lui[B.y + r0];
     int o0 = A.w + lam0;
@@ -1427,8 +1428,9 @@ __device__ __forceinline__ void il_level(const int4 A, const int4 B, const IlPro
       const int lam1 = min(base + GG + gl, W - 1);
       const int r1 = lam1 >> lsh;
       const int k1 = I.rows[B.x + r1];
-      const bool w1 = base + GG + gl < W && (lam1 & (spl - 1)) == 0;
-      df s1 = (lam1 & (spl - 1)) == 0 ? y[k1] : df{0.f, 0.f};
+      const bool f1 = (lam1 & (spl - 1)) == 0, w1 = base + GG + gl < W && f1;
+      const df t1 = y[k1];
+      df s1{f1 ? t1.hi : 0.f, f1 ? t1.lo : 0.f};
       df d1{0.f, 0.f};
       if (UPPER) d1 = I.lui[B.y + r1];
       int o1 = A.w + lam1;
@@ -1460,8 +1462,10 @@ __device__ __forceinline__ void il_level(const int4 A, const int4 B, const IlPro
         s0 = df_add(s0, t0);
         s1 = df_add(s1, t1);
       }
-      if (w0) y[k0] = UPPER ? df_mul(s0, d0) : s0;
-      if (w1) y[k1] = UPPER ? df_mul(s1, d1) : s1;
+      // the values on every lane, the stores predicated (no branch around the product)
+      const df v0 = UPPER ? df_mul(s0, d0) : s0, v1 = UPPER ? df_mul(s1, d1) : s1;
+      if (w0) y[k0] = v0;
+      if (w1) y[k1] = v1;
     } else {
       int i = 0;
       for (; i + 1 < mc; i += 2) {  // two entries in flight
@@ -1479,7 +1483,8 @@ __device__ __forceinline__ void il_level(const int4 A, const int4 B, const IlPro
         t0.lo = __shfl_xor_sync(kFull, s0.lo, o);
         s0 = df_add(s0, t0);
       }
-      if (w0) y[k0] = UPPER ? df_mul(s0, d0) : s0;
+      const df v0 = UPPER ? df_mul(s0, d0) : s0;
+      if (w0) y[k0] = v0;
     }
   }
 }

@@ -273,3 +273,27 @@ def uneven_table(index: int, seed: int = 4):
             rec["wave"] = 1
             rec["wp"][:7] = w
     return t, counter
+
+
+def dense_block_table(m: int, seed: int = 7):
+    """(element table, n) of a netlist whose LU is dense: a 1 V source at node 1, a resistor
+    between every pair of the m nodes (log-uniform 1 kOhm-100 kOhm) and a capacitor from
+    every node to ground (1 pF); n = m + 1, and the LU ends in a dense block of m - 1 rows
+    (the multi-circuit engine takes up to 65534 elements: m <= 361).  Used to time the
+    dense-block set-up and solves of that engine as a function of m."""
+    from .table import ELEM_DTYPE
+    rng = np.random.default_rng(seed)
+    pairs = [(i, j) for i in range(m) for j in range(i + 1, m)]
+    t = np.zeros(1 + len(pairs) + m, dtype=ELEM_DTYPE)
+    t["g"] = -1
+    t["b"] = -1
+    t[0]["kind"], t[0]["b"], t[0]["p"], t[0]["m"], t[0]["value"] = 4, 0, 1, -1, 1.0
+    # node k (0-based) is unknown k + 1: node 1 first seen with the source, the others in
+    # the order the pair list meets them, which is increasing
+    for r, (i, j) in enumerate(pairs, start=1):
+        t[r]["kind"], t[r]["p"], t[r]["m"] = 1, i + 1, j + 1
+        t[r]["value"] = 10.0 ** rng.uniform(3, 5)
+    for k in range(m):
+        r = 1 + len(pairs) + k
+        t[r]["kind"], t[r]["p"], t[r]["m"], t[r]["value"] = 2, k + 1, -1, 1e-12
+    return t, m + 1

@@ -16,6 +16,8 @@ the device at most), run as
            mixed, double-float; nonlinear FP64 and mixed), adaptive transient, 64 small
            uneven netlists
   op       k_op: the plain operating point of the 1001-unknown ladder, three times
+  dense    k_multi_tran set-up (operating point and transient factorisations) and 100 BE
+           steps of one circuit whose LU is a dense block of m - 1 rows, m = 96 .. 352
 """
 from __future__ import annotations
 
@@ -116,7 +118,28 @@ def op():
     return g.timing()
 
 
-CASES = {"tran": tran, "multi": multi, "adjoint": adjoint, "kernels": kernels, "op": op}
+def dense():
+    from .generators import dense_block_table
+    rows = []
+    for m in (96, 128, 192, 256, 352):
+        t, n = dense_block_table(m)
+        meta = _lib.symbolic_export(t, n, _lib.MODE_TRAN, "be", 1e-9, ordering=0x1ff)["meta"]
+        mc = _lib.MultiCircuit([t], [n], method="be", h=1e-9)
+        times = []
+        for steps in (0, 0, 100, 100):
+            out = _lib.DeviceArray(mc.total(steps))
+            mc.tran(steps, out=out)
+            times.append(mc.timing()[0])
+            del out
+        setup, with_steps = min(times[:2]), min(times[2:])
+        rows.append((m, int(meta[8]), setup, (with_steps - setup) / 100))
+        print(f"m {m}: dense block {int(meta[8])}, set-up + OP {setup:.3f} ms, "
+              f"per BE step {(with_steps - setup) / 100 * 1e3:.1f} us", flush=True)
+        mc.close()
+    return rows[-1][2], rows[-1][2]
+
+
+CASES = {"tran": tran, "multi": multi, "adjoint": adjoint, "kernels": kernels, "op": op, "dense": dense}
 
 if __name__ == "__main__":
     k, c = CASES[sys.argv[1]]()
