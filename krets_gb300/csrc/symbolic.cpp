@@ -163,9 +163,16 @@ struct GP {
 constexpr int kFillCapExceeded = -100;
 constexpr int kMinDenseTail = 64;  // smallest dense trailing block solved as a dense block  // gp_factor gave up: more L+U entries than the cap
 
+// dense_from < n: columns dense_from .. n-1 of the ordering form a clique of the
+// elimination graph (minimum degree's last vertices), so their Schur complement is
+// structurally dense.  They are finished by a dense right-looking LU with the same
+// pivoting rule: each such column is first reduced by the sparse pivots only (the
+// left-looking steps below, without choosing a pivot), and the remaining c x c block is
+// factored in place; its L and U patterns are the full block.  This replaces the
+// left-looking steps' O(c^3) graph traversals and scattered updates for that block.
 template <typename T>
 int gp_factor(int n, const std::vector<int> &ap, const std::vector<int> &ai, const std::vector<T> &ax,
-              const std::vector<int> &q, double tau, GP &F, size_t fill_cap = 0) {
+              const std::vector<int> &q, double tau, GP &F, size_t fill_cap = 0, int dense_from = -1) {
   F.n = n;
   F.lp.assign(n + 1, 0);
   F.up.assign(n + 1, 0);
@@ -174,7 +181,44 @@ int gp_factor(int n, const std::vector<int> &ap, const std::vector<int> &ai, con
   F.pinv.assign(n, -1);
   std::vector<T> lx, xv(n, T(0));
   std::vector<int> mark(n, -1), stack(n), pstack(n), reach(n);
-  for (int k = 0; k < n; ++k) {
+  const int kd = (dense_from >= 0 && dense_from < n) ? dense_from : n;
+  // reach of column col among the finished pivots (marks with stamp k), in topological
+  // order at reach[top..n); returns top
+  auto find_reach = [&](int col, int k) {
+    int top = n;
+    for (int p = ap[col]; p < ap[col + 1]; ++p) {
+      int r0 = ai[p];
+      if (mark[r0] == k) continue;
+      int head = 0;
+      stack[0] = r0;
+      while (head >= 0) {
+        int j = stack[head];
+        int jp = F.pinv[j];
+        if (mark[j] != k) {
+          mark[j] = k;
+          pstack[head] = jp < 0 ? 0 : F.lp[jp];
+        }
+        bool done = true;
+        if (jp >= 0) {
+          int end = F.lp[jp + 1];
+          for (int pp = pstack[head]; pp < end; ++pp) {
+            int i = F.li[pp];
+            if (mark[i] == k) continue;
+            pstack[head] = pp + 1;
+            stack[++head] = i;
+            done = false;
+            break;
+          }
+        }
+        if (done) {
+          --head;
+          reach[--top] = j;
+        }
+      }
+    }
+    return top;
+  };
+  for (int k = 0; k < kd; ++k) {
     F.lp[k] = (int)F.li.size();
     F.up[k] = (int)F.ui.size();
     int col = q[k];
@@ -247,6 +291,79 @@ int gp_factor(int n, const std::vector<int> &ap, const std::vector<int> &ai, con
       xv[i] = T(0);
     }
   }
+  if (kd < n) {
+    const int c = n - kd;
+    std::vector<int> R, rpos(n, -1);  // the rows without a pivot, and their block position
+    for (int r = 0; r < n; ++r)
+      if (F.pinv[r] < 0) {
+        rpos[r] = (int)R.size();
+        R.push_back(r);
+      }
+    if ((int)R.size() != c) return KRETS_ERR_DECOMPOSITION_FAILED;
+    std::vector<T> S((size_t)c * c, T(0));  // S[i c + j]: row R[i], block column j
+    std::vector<std::vector<int>> usp(c);  // sparse pivots each block column reaches
+    for (int j = 0; j < c; ++j) {
+      const int k = kd + j, col = q[k];
+      const int top = find_reach(col, k);
+      for (int p = top; p < n; ++p) xv[reach[p]] = T(0);
+      for (int p = ap[col]; p < ap[col + 1]; ++p) xv[ai[p]] += ax[p];
+      for (int p = top; p < n; ++p) {
+        const int jr = reach[p], jp = F.pinv[jr];
+        if (jp < 0) continue;
+        const T xj = xv[jr];
+        for (int pp = F.lp[jp]; pp < F.lp[jp + 1]; ++pp) xv[F.li[pp]] -= lx[pp] * xj;
+      }
+      for (int p = top; p < n; ++p) {
+        const int i = reach[p];
+        if (F.pinv[i] >= 0) usp[j].push_back(F.pinv[i]);
+        else S[(size_t)rpos[i] * c + j] = xv[i];
+        xv[i] = T(0);
+      }
+    }
+    std::vector<char> used(c, 0);
+    std::vector<int> piv_row(c);
+    for (int j = 0; j < c; ++j) {
+      const int k = kd + j, col = q[k];
+      int ip = -1;
+      double amax = -1.0;
+      for (int i = 0; i < c; ++i)
+        if (!used[i]) {
+          const double a = std::abs(S[(size_t)i * c + j]);
+          if (a > amax) { amax = a; ip = i; }
+        }
+      if (ip < 0 || !(amax > 0.0) || !std::isfinite(amax)) return KRETS_ERR_DECOMPOSITION_FAILED;
+      const int dr = rpos[col];  // diagonal preference, as in the sparse steps
+      if (dr >= 0 && !used[dr] && std::abs(S[(size_t)dr * c + j]) >= tau * amax) ip = dr;
+      const T piv = S[(size_t)ip * c + j];
+      F.min_ratio = std::min(F.min_ratio, std::abs(piv) / amax);
+      used[ip] = 1;
+      piv_row[j] = ip;
+      F.pinv[R[ip]] = k;
+      const T *urow = S.data() + (size_t)ip * c;
+      for (int i = 0; i < c; ++i) {
+        if (used[i]) continue;
+        T *ri = S.data() + (size_t)i * c;
+        const T l = ri[j] / piv;
+        ri[j] = l;
+        for (int jj = j + 1; jj < c; ++jj) ri[jj] -= l * urow[jj];
+      }
+    }
+    // patterns: U column k = the sparse pivots it reaches, every earlier block pivot and
+    // its own pivot; L column k = the block rows not pivoted yet
+    std::vector<char> done(c, 0);
+    for (int j = 0; j < c; ++j) {
+      const int k = kd + j;
+      F.lp[k] = (int)F.li.size();
+      F.up[k] = (int)F.ui.size();
+      F.ui.insert(F.ui.end(), usp[j].begin(), usp[j].end());
+      for (int t = 0; t < j; ++t) F.ui.push_back(kd + t);
+      F.ui.push_back(k);
+      done[piv_row[j]] = 1;
+      for (int i = 0; i < c; ++i)
+        if (!done[i]) F.li.push_back(R[i]);
+      if (fill_cap && F.li.size() + F.ui.size() > fill_cap) return kFillCapExceeded;
+    }
+  }
   F.lp[n] = (int)F.li.size();
   F.up[n] = (int)F.ui.size();
   return KRETS_OK;
@@ -263,38 +380,88 @@ uint64_t fnv1a(uint64_t h, uint64_t v) {
 }  // namespace
 
 // ------------------------------------------------------------------ orderings
-std::vector<int> order_min_degree(int n, const std::vector<std::vector<int>> &adj0) {
+std::vector<int> order_min_degree(int n, const std::vector<std::vector<int>> &adj0, int *clique) {
   // Explicit elimination graph; the next vertex is the one of least current degree, the
   // smallest index among equals, found through a min-heap of (degree, vertex) entries
   // whose stale entries (a vertex's degree changed since) are skipped when they surface.
+  // Once at most 4096 vertices remain and the eliminated vertex has 24 or more
+  // neighbours, the remaining graph moves to bit rows (one bit per remaining vertex):
+  // merging a neighbourhood is then a few word ORs instead of a sorted-list union, and
+  // degrees (popcounts) are the same, so the order is the same.
   std::vector<std::vector<int>> adj = adj0;
+  if (clique) *clique = 0;
   std::vector<char> gone(n, 0);
-  std::vector<int> order;
+  std::vector<int> order, deg(n);
   order.reserve(n);
   using Key = std::pair<int, int>;
   std::priority_queue<Key, std::vector<Key>, std::greater<Key>> heap;
-  for (int v = 0; v < n; ++v) heap.push({(int)adj[v].size(), v});
+  for (int v = 0; v < n; ++v) {
+    deg[v] = (int)adj[v].size();
+    heap.push({deg[v], v});
+  }
   std::vector<int> merged;
+  bool bit_rows = false;
+  int W = 0;
+  std::vector<int> cid(n, -1), orig;  // bit-row phase: compact index of a vertex, and back
+  std::vector<uint64_t> bits, nbrow;
   for (int step = 0; step < n; ++step) {
     int best = -1;
     while (!heap.empty()) {
       const Key top = heap.top();
       heap.pop();
-      if (!gone[top.second] && (int)adj[top.second].size() == top.first) {
+      if (!gone[top.second] && deg[top.second] == top.first) {
         best = top.second;
         break;
       }
     }
-    const size_t bd = adj[best].size();
-    if (bd + 1 == (size_t)(n - step)) {
+    const int bd = deg[best];
+    if (bd + 1 == n - step) {
       // every remaining vertex is adjacent to all others: a clique, whose vertices the
       // selection would take in increasing index order (equal degrees throughout)
       for (int v = 0; v < n; ++v)
         if (!gone[v]) order.push_back(v);
+      if (clique) *clique = n - step;
       break;
+    }
+    if (!bit_rows && n - step <= 4096 && bd >= 24) {
+      for (int v = 0; v < n; ++v)
+        if (!gone[v]) {
+          cid[v] = (int)orig.size();
+          orig.push_back(v);
+        }
+      W = ((int)orig.size() + 63) / 64;
+      bits.assign(orig.size() * (size_t)W, 0);
+      for (size_t i = 0; i < orig.size(); ++i) {
+        for (int u : adj[orig[i]]) bits[i * W + (cid[u] >> 6)] |= 1ull << (cid[u] & 63);
+        std::vector<int>().swap(adj[orig[i]]);
+      }
+      nbrow.resize(W);
+      bit_rows = true;
     }
     gone[best] = 1;
     order.push_back(best);
+    if (bit_rows) {
+      const int b = cid[best];
+      std::copy(bits.begin() + (size_t)b * W, bits.begin() + (size_t)(b + 1) * W, nbrow.begin());
+      for (int w = 0; w < W; ++w)
+        for (uint64_t x = nbrow[w]; x; x &= x - 1) {
+          const int i = w * 64 + __builtin_ctzll(x);
+          uint64_t *row = bits.data() + (size_t)i * W;
+          int d = 0;
+          for (int t = 0; t < W; ++t) {
+            row[t] |= nbrow[t];
+            if (t == (i >> 6)) row[t] &= ~(1ull << (i & 63));
+            if (t == (b >> 6)) row[t] &= ~(1ull << (b & 63));
+            d += __builtin_popcountll(row[t]);
+          }
+          const int u = orig[i];
+          if (d != deg[u]) {
+            deg[u] = d;
+            heap.push({d, u});
+          }
+        }
+      continue;
+    }
     const std::vector<int> nb = adj[best];
     for (int u : nb) {
       merged.clear();
@@ -304,7 +471,8 @@ std::vector<int> order_min_degree(int n, const std::vector<std::vector<int>> &ad
                    merged.end());
       const bool changed = merged.size() != adj[u].size();
       adj[u].assign(merged.begin(), merged.end());
-      if (changed) heap.push({(int)adj[u].size(), u});
+      deg[u] = (int)adj[u].size();
+      if (changed) heap.push({deg[u], u});
     }
     adj[best].clear();
   }
@@ -787,7 +955,7 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
                             const std::vector<MEntry> &M, const std::vector<BEntry> &B,
                             const std::vector<int> &q, Program &P, std::string &msg, bool rep_diode_zero,
                             const std::vector<int> &xslot, int n_coef, size_t fill_cap = 0,
-                            bool update_list = true, bool dense_tail = false) {
+                            bool update_list = true, bool dense_tail = false, int dense_from = -1) {
   P = Program();
   P.mode = mode;
   P.method = method;
@@ -827,11 +995,11 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
   int st;
   const double tau = 1e-3;  // threshold partial pivoting (diagonal kept when >= tau * column max)
   if (mode == MODE_AC) {
-    st = gp_factor<std::complex<double>>(n, ap, ai, axz, q, tau, F, fill_cap);
+    st = gp_factor<std::complex<double>>(n, ap, ai, axz, q, tau, F, fill_cap, dense_from);
   } else {
     std::vector<double> axr(axz.size());
     for (size_t k = 0; k < axz.size(); ++k) axr[k] = axz[k].real();
-    st = gp_factor<double>(n, ap, ai, axr, q, tau, F, fill_cap);
+    st = gp_factor<double>(n, ap, ai, axr, q, tau, F, fill_cap, dense_from);
   }
   if (st == kFillCapExceeded) return st;
   if (st != KRETS_OK) {
@@ -859,12 +1027,16 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
     P.max_row_lu = std::max(P.max_row_lu, (int)rows[k].size());
   }
   P.lu_col.resize(P.lu_rowptr[n]);
-  std::vector<std::unordered_map<int, int>> slot(n);
+  // slot of column c in row k (rows sorted by column), -1 if absent
+  auto slot_of = [&](int k, int c) {
+    const int *b = P.lu_col.data() + P.lu_rowptr[k], *e = P.lu_col.data() + P.lu_rowptr[k + 1];
+    const int *it = std::lower_bound(b, e, c);
+    return (it != e && *it == c) ? (int)(it - P.lu_col.data()) : -1;
+  };
   for (int k = 0; k < n; ++k) {
     for (size_t t = 0; t < rows[k].size(); ++t) {
       int s = P.lu_rowptr[k] + (int)t;
       P.lu_col[s] = rows[k][t];
-      slot[k][rows[k][t]] = s;
       if (rows[k][t] == k) P.lu_diag[k] = s;
     }
     if (P.lu_diag[k] < 0) {
@@ -893,31 +1065,14 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
   // ---- factorisation program (IKJ)
   P.piv_ptr.assign(n + 1, 0);
   if (!update_list) {
-    // no explicit update list (the device merges each U row into the pattern of row k):
-    // count the work and check that every update lands inside the static pattern (rows
-    // k and j both in the dense trailing block need no check: U row j's columns all lie
-    // in the block, where row k holds every column)
-    const int t0 = P.tail_m ? P.tail0 : n;
-    for (int k = 0; k < n; ++k) {
+    // no explicit update list (the device merges each U row into the pattern of row k;
+    // the pattern is the fill of this very factorisation, so every update lands in it,
+    // and the device reports a row whose update finds no slot): count the work only
+    for (int k = 0; k < n; ++k)
       for (int s = P.lu_rowptr[k]; s < P.lu_diag[k]; ++s) {
         const int j = P.lu_col[s];
-        if (k >= t0 && j >= t0) {
-          P.factor_flops += 2 * (P.lu_rowptr[j + 1] - P.lu_diag[j] - 1) + 1;
-          continue;
-        }
-        int p = s + 1;
-        for (int t = P.lu_diag[j] + 1; t < P.lu_rowptr[j + 1]; ++t) {
-          const int c = P.lu_col[t];
-          while (p < P.lu_rowptr[k + 1] && P.lu_col[p] < c) ++p;
-          if (p >= P.lu_rowptr[k + 1] || P.lu_col[p] != c) {
-            msg = "internal: fill entry missing from static pattern";
-            return KRETS_ERR_UNEXPECTED;
-          }
-          P.factor_flops += 2;
-        }
-        P.factor_flops += 1;
+        P.factor_flops += 2 * (P.lu_rowptr[j + 1] - P.lu_diag[j] - 1) + 1;
       }
-    }
   }
   for (int k = 0; k < n && update_list; ++k) {
     for (int s = P.lu_rowptr[k]; s < P.lu_diag[k]; ++s) {
@@ -925,12 +1080,12 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
       int ub = (int)P.upd.size() / 2;
       for (int t = P.lu_diag[j] + 1; t < P.lu_rowptr[j + 1]; ++t) {
         int c = P.lu_col[t];
-        auto it = slot[k].find(c);
-        if (it == slot[k].end()) {
+        const int at = slot_of(k, c);
+        if (at < 0) {
           msg = "internal: fill entry missing from static pattern";
           return KRETS_ERR_UNEXPECTED;
         }
-        P.upd.push_back(it->second);
+        P.upd.push_back(at);
         P.upd.push_back(t);
         P.factor_flops += 2;
       }
@@ -990,12 +1145,12 @@ static int build_with_order(const krets_element *el, int ne, int n, int mode, in
     while (t2 < am.size() && am[t2].first == am[t].first) P.a_contrib.push_back(M[am[t2++].second].code);
     P.a_cptr.push_back((int)P.a_contrib.size());
     P.a_col.push_back(c);
-    auto it = slot[r].find(c);
-    if (it == slot[r].end()) {
+    const int at = slot_of(r, c);
+    if (at < 0) {
       msg = "internal: A entry outside the LU pattern";
       return KRETS_ERR_UNEXPECTED;
     }
-    P.a_slot.push_back(it->second);
+    P.a_slot.push_back(at);
     P.a_rowptr[r + 1]++;
     t = t2;
   }
@@ -1155,6 +1310,7 @@ int build_program(const krets_element *el, int ne, int n, int mode, int method, 
   std::string best_msg;
   for (int o : cands) {
     std::vector<int> q;
+    int clique = 0;  // minimum degree: size of the final clique of the elimination graph
     if (o == ORDER_NATURAL) {
       // the natural order is a candidate only for small systems (chains, tests): on a
       // general graph its fill grows towards n^2
@@ -1163,7 +1319,7 @@ int build_program(const krets_element *el, int ne, int n, int mode, int method, 
       std::iota(q.begin(), q.end(), 0);
     } else if (o == ORDER_MINDEG) {
       if (n > 20000) continue;
-      q = order_min_degree(n, adj);
+      q = order_min_degree(n, adj, &clique);
     } else {
       int top_sep = 0;
       q = order_nested_dissection(n, adj, &top_sep);
@@ -1174,11 +1330,13 @@ int build_program(const krets_element *el, int ne, int n, int mode, int method, 
     }
     Program P;
     std::string m2;
+    // programs with a dense trailing block finish a large final clique as a dense block
+    const int dense_from = dense_tail && clique >= kMinDenseTail ? n - clique : -1;
     int st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, true, xslot, n_coef, fill_cap,
-                              update_list, dense_tail);
+                              update_list, dense_tail, dense_from);
     if (st == KRETS_ERR_DECOMPOSITION_FAILED)  // only singular without diode / NMOS conductances
       st = build_with_order(el, ne, n, mode, method, h, f, M, B, q, P, m2, false, xslot, n_coef, fill_cap,
-                            update_list, dense_tail);
+                            update_list, dense_tail, dense_from);
     if (st == kFillCapExceeded) continue;
     if (st != KRETS_OK) {
       if (best_st != KRETS_OK) { best_st = st; best_msg = m2; }
