@@ -479,8 +479,12 @@ std::vector<int> order_min_degree(int n, const std::vector<std::vector<int>> &ad
   return order;
 }
 
-std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<int>> &adj, int *top_sep) {
+std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<int>> &adj, int *top_sep,
+                                         int max_top_sep) {
+  // max_top_sep > 0: stop as soon as the first separator is larger (the caller then
+  // discards the ordering; *top_sep reports the size)
   if (top_sep) *top_sep = 0;
+  bool stop = false;
   std::vector<int> order;
   order.reserve(n);
   std::vector<int> in_set(n, -1), level(n, -1);
@@ -488,6 +492,7 @@ std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<in
   const int kLeaf = 1;
   // explicit stack of vertex sets to avoid deep recursion
   std::function<void(std::vector<int> &)> nd = [&](std::vector<int> &V) {
+    if (stop) return;
     if ((int)V.size() <= kLeaf) {
       std::sort(V.begin(), V.end());
       order.insert(order.end(), V.begin(), V.end());
@@ -570,6 +575,10 @@ std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<in
       for (int l = best + 1; l < L; ++l) B.insert(B.end(), levels[l].begin(), levels[l].end());
       std::vector<int> S = levels[best];
       if (top_sep && *top_sep == 0) *top_sep = (int)S.size();  // the first separator found
+      if (max_top_sep > 0 && (int)S.size() > max_top_sep) {
+        stop = true;
+        return;
+      }
       nd(A);
       nd(B);
       std::sort(S.begin(), S.end());
@@ -1322,11 +1331,12 @@ int build_program(const krets_element *el, int ne, int n, int mode, int method, 
       q = order_min_degree(n, adj, &clique);
     } else {
       int top_sep = 0;
-      q = order_nested_dissection(n, adj, &top_sep);
+      const int sep_cap = std::max(16, (int)(2.0 * std::sqrt((double)n)));
+      q = order_nested_dissection(n, adj, &top_sep, fill_cap ? sep_cap : 0);
       // bisection by BFS levels suits chains, ladders and meshes (separators of a few
       // vertices, or ~sqrt(n)); on irregular graphs its first separator is already large and
       // its fill beyond the minimum-degree one, so it is not factored once that is known
-      if (fill_cap && top_sep > std::max(16, (int)(2.0 * std::sqrt((double)n)))) continue;
+      if (fill_cap && top_sep > sep_cap) continue;
     }
     Program P;
     std::string m2;

@@ -114,6 +114,7 @@ int build_program(const krets_element *el, int ne, int n, int mode, int method, 
 
 // Exposed for tests of the symbolic pass itself.
 std::vector<int> order_min_degree(int n, const std::vector<std::vector<int>> &adj, int *clique = nullptr);
-std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<int>> &adj, int *top_sep = nullptr);
+std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<int>> &adj, int *top_sep = nullptr,
+                                         int max_top_sep = 0);
 
 }  // namespace krets
