@@ -300,7 +300,7 @@ int gp_factor(int n, const std::vector<int> &ap, const std::vector<int> &ai, con
         R.push_back(r);
       }
     if ((int)R.size() != c) return KRETS_ERR_DECOMPOSITION_FAILED;
-    std::vector<T> S((size_t)c * c, T(0));  // S[i c + j]: row R[i], block column j
+    std::vector<T> S((size_t)c * c, T(0));  // S[j c + i]: block column j, row R[i]
     std::vector<std::vector<int>> usp(c);  // sparse pivots each block column reaches
     for (int j = 0; j < c; ++j) {
       const int k = kd + j, col = q[k];
@@ -316,36 +316,37 @@ int gp_factor(int n, const std::vector<int> &ap, const std::vector<int> &ai, con
       for (int p = top; p < n; ++p) {
         const int i = reach[p];
         if (F.pinv[i] >= 0) usp[j].push_back(F.pinv[i]);
-        else S[(size_t)rpos[i] * c + j] = xv[i];
+        else S[(size_t)j * c + rpos[i]] = xv[i];
         xv[i] = T(0);
       }
     }
     std::vector<char> used(c, 0);
     std::vector<int> piv_row(c);
-    for (int j = 0; j < c; ++j) {
+    std::vector<T> lcol(c);
+    for (int j = 0; j < c; ++j) {  // right-looking, by columns (contiguous over the rows)
       const int k = kd + j, col = q[k];
+      T *cj = S.data() + (size_t)j * c;
       int ip = -1;
       double amax = -1.0;
       for (int i = 0; i < c; ++i)
         if (!used[i]) {
-          const double a = std::abs(S[(size_t)i * c + j]);
+          const double a = std::abs(cj[i]);
           if (a > amax) { amax = a; ip = i; }
         }
       if (ip < 0 || !(amax > 0.0) || !std::isfinite(amax)) return KRETS_ERR_DECOMPOSITION_FAILED;
       const int dr = rpos[col];  // diagonal preference, as in the sparse steps
-      if (dr >= 0 && !used[dr] && std::abs(S[(size_t)dr * c + j]) >= tau * amax) ip = dr;
-      const T piv = S[(size_t)ip * c + j];
+      if (dr >= 0 && !used[dr] && std::abs(cj[dr]) >= tau * amax) ip = dr;
+      const T piv = cj[ip];
       F.min_ratio = std::min(F.min_ratio, std::abs(piv) / amax);
       used[ip] = 1;
       piv_row[j] = ip;
       F.pinv[R[ip]] = k;
-      const T *urow = S.data() + (size_t)ip * c;
-      for (int i = 0; i < c; ++i) {
-        if (used[i]) continue;
-        T *ri = S.data() + (size_t)i * c;
-        const T l = ri[j] / piv;
-        ri[j] = l;
-        for (int jj = j + 1; jj < c; ++jj) ri[jj] -= l * urow[jj];
+      for (int i = 0; i < c; ++i) lcol[i] = used[i] ? T(0) : cj[i] / piv;
+      for (int jj = j + 1; jj < c; ++jj) {
+        T *cc = S.data() + (size_t)jj * c;
+        const T u = cc[ip];
+        if (u == T(0)) continue;
+        for (int i = 0; i < c; ++i) cc[i] -= lcol[i] * u;
       }
     }
     // patterns: U column k = the sparse pivots it reaches, every earlier block pivot and
