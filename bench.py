@@ -223,6 +223,7 @@ def run_ours(args, rank, world):
     from krets_gb300 import _lib
     from krets_gb300.table import is_current_mask
 
+    stage("headline: set-up")
     c, t, vals = workload(rank)
     n = c.size
     g = _lib.GpuCircuit(t, n)
@@ -286,6 +287,7 @@ def run_ours(args, rank, world):
 
     errs = sampled_err()
     # the other two precision modes of the same engine, one pass each (not the headline)
+    stage("headline: precision variants")
     variants = {}
     for name, prec in (("mixed_fp32_lu_df_refinement", _lib.PREC_MIXED), ("fp64", _lib.PREC_FP64)):
         step(prec)
@@ -342,6 +344,7 @@ def run_ours(args, rank, world):
     peak, peak_kind = measured_peak_hbm()
     achieved = alg_bytes / k_s / 1e9
 
+    stage("headline: CPU baseline")
     # CPU baseline: optimised oracle (factor once) on the host cores, bounded sample
     threads = os.cpu_count() or 1
     r1, dt1 = cpu_rate(t, vals, n, [0], 500, False, 1)
@@ -351,6 +354,7 @@ def run_ours(args, rank, world):
     n_sample = max(threads, min(8 * threads, int(15.0 * threads / max(per_inst_s, 1e-3))))
     cpu_val, cpu_dt = cpu_rate(t, vals, n, list(range(n_sample)), N_STEPS, False, threads)
 
+    stage("headline: end to end")
     # end to end: host values in, host waveforms out, through the C ABI, with the caller's
     # buffers in pinned (page-locked) host memory, registered once before the timed calls.
     # The sample is every instance when the waveforms fit in 60 % of the available host
@@ -855,12 +859,18 @@ def compact(line):
     return c
 
 
+def stage(msg):
+    """Progress on stderr (the JSON line is the only stdout output)."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
 def other_configs(args, world, reference):
     """Configurations 1, 2, 4 and 5 at --steps 2 each (same timing rules), compacted."""
     a = argparse.Namespace(**vars(args))
     a.steps = 2
     out = {}
     for name, fn in WORKLOADS.items():
+        stage(f"other configuration: {name}")
         t0 = time.perf_counter()
         try:
             c = compact(fn(a, world, reference))

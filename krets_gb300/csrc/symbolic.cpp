@@ -485,7 +485,7 @@ std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<in
   // max_top_sep > 0: stop as soon as the first separator is larger (the caller then
   // discards the ordering; *top_sep reports the size)
   if (top_sep) *top_sep = 0;
-  bool stop = false;
+  bool stop = false, first_done = false;
   std::vector<int> order;
   order.reserve(n);
   std::vector<int> in_set(n, -1), level(n, -1);
@@ -575,10 +575,13 @@ std::vector<int> order_nested_dissection(int n, const std::vector<std::vector<in
       for (int l = 0; l < best; ++l) A.insert(A.end(), levels[l].begin(), levels[l].end());
       for (int l = best + 1; l < L; ++l) B.insert(B.end(), levels[l].begin(), levels[l].end());
       std::vector<int> S = levels[best];
-      if (top_sep && *top_sep == 0) *top_sep = (int)S.size();  // the first separator found
-      if (max_top_sep > 0 && (int)S.size() > max_top_sep) {
-        stop = true;
-        return;
+      if (!first_done) {  // the first separator found
+        first_done = true;
+        if (top_sep) *top_sep = (int)S.size();
+        if (max_top_sep > 0 && (int)S.size() > max_top_sep) {
+          stop = true;
+          return;
+        }
       }
       nd(A);
       nd(B);
@@ -1338,6 +1341,7 @@ int build_program(const krets_element *el, int ne, int n, int mode, int method, 
       // vertices, or ~sqrt(n)); on irregular graphs its first separator is already large and
       // its fill beyond the minimum-degree one, so it is not factored once that is known
       if (fill_cap && top_sep > sep_cap) continue;
+      if ((int)q.size() != n) continue;  // stopped early: no ordering
     }
     Program P;
     std::string m2;

@@ -348,3 +348,33 @@ def test_direct_rhs_program_equals_gather(built_lib, which):
             b[L[d][3]] = -cb[d]
     b[zrow] = 0.0
     np.testing.assert_array_equal(b[:n], ref)
+
+
+def test_orderings_of_a_path_joined_to_an_expander(built_lib):
+    """A path whose first nested-dissection separator is one vertex, joined to a random
+    expander whose own separators are large: every mode yields a full permutation (the
+    dissection may stop early only at its first separator, and an ordering it left
+    unfinished is never used)."""
+    from krets_gb300.table import ELEM_DTYPE
+    rng = np.random.default_rng(1)
+    L, m, deg = 300, 400, 8
+    edges = [(i, i + 1) for i in range(L)]
+    E = set()
+    while len(E) < m * deg // 2:
+        a, b = rng.integers(0, m, 2)
+        if a != b:
+            E.add((L + min(a, b), L + max(a, b)))
+    edges += sorted(E)
+    nn = L + m
+    t = np.zeros(1 + len(edges) + nn, dtype=ELEM_DTYPE)
+    t["g"], t["b"] = -1, -1
+    t[0]["kind"], t[0]["b"], t[0]["p"], t[0]["m"], t[0]["value"] = 4, 0, 1, -1, 1.0
+    for r, (i, j) in enumerate(edges, start=1):
+        t[r]["kind"], t[r]["p"], t[r]["m"], t[r]["value"] = 1, i + 1, j + 1, 1e3
+    for k in range(nn):
+        r = 1 + len(edges) + k
+        t[r]["kind"], t[r]["p"], t[r]["m"], t[r]["value"] = 2, k + 1, -1, 1e-12
+    for mode in (built_lib.MODE_DC, built_lib.MODE_TRAN):
+        for ordering in (-1, 0x1ff):   # single-circuit and multi-circuit programs
+            P = built_lib.symbolic_export(t, nn + 1, mode, "be", 1e-9, ordering=ordering)
+            assert sorted(P["q"].tolist()) == list(range(nn + 1))
