@@ -23,6 +23,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import faulthandler
 import json
 import os
 import statistics
@@ -883,6 +884,7 @@ def other_configs(args, world, reference):
 
 
 def main():
+    faulthandler.enable()  # a native crash prints the Python stacks on stderr
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
