@@ -1133,33 +1133,6 @@ __device__ __forceinline__ void df_dense_update(const SProg &S, const int4 *td, 
   }
 }
 
-// L2 prefetches for the dense-block solves with the factors in global memory (the lines
-// come from DRAM while the current block is still being solved; hints only, every
-// address inside the rows' dense parts): lane i of the first warp fetches row kb + i of
-// diagonal block kb; in dense_prefetch_update lane gl of the other warps fetches a line
-// of the rows it updates first for block kb.
-__device__ __forceinline__ void dense_prefetch_tile(const SProg &S, const int4 *td, const df *lu, int kb, int nb,
-                                                    int i) {
-  if (i < nb) {
-    const char *p = reinterpret_cast<const char *>(lu + (S.dense_rows ? S.dense_rows[kb + i] : dense_base(td[kb + i])) + kb);
-    asm volatile("prefetch.L2 [%0];" ::"l"(p));
-    if (nb > 16) asm volatile("prefetch.L2 [%0];" ::"l"(p + 128));
-    asm volatile("prefetch.L2 [%0];" ::"l"(p + 8 * nb - 1));
-  }
-}
-
-template <int G>
-__device__ __forceinline__ void dense_prefetch_update(const SProg &S, const int4 *td, const df *lu, int kb, int nb,
-                                                      int r_begin, int r_end, int gl) {
-  constexpr int R = G / 8;
-  const int sub = gl & 7;
-  if (sub > 2 || (sub == 1 && nb <= 16)) return;
-  for (int r = r_begin + (gl >> 3); r < r_end && r < r_begin + 2 * R; r += R) {
-    const char *p = reinterpret_cast<const char *>(lu + (S.dense_rows ? S.dense_rows[r] : dense_base(td[r])) + kb);
-    asm volatile("prefetch.L2 [%0];" ::"l"(sub < 2 ? p + 128 * sub : p + 8 * nb - 1));
-  }
-}
-
 // Diagonal block rows of the first warp: lane i holds row kb + i; with a staging tile the
 // block is loaded once (all loads in flight) and read from shared memory.
 __device__ __forceinline__ const df *dense_diag_rows(const SProg &S, const df *__restrict__ lu, int base, int kb,
@@ -1183,8 +1156,6 @@ __device__ __forceinline__ void df_dense_lower(const SProg &S, const df *__restr
   const int4 *td = S.ldesc + S.lev_ptr[S.nlev - 1];
   for (int kb = 0; kb < m; kb += 32) {
     const int nb = min(32, m - kb);
-    if (gl >= 32 && S.dense_stage && kb + nb < m)  // the others wait: fetch their first update rows
-      dense_prefetch_update<G>(S, td, lu, kb, nb, kb + nb, m, gl);
     if (gl < 32) {
       const int i = gl;
       df yi{0.f, 0.f};
@@ -1205,7 +1176,6 @@ __device__ __forceinline__ void df_dense_lower(const SProg &S, const df *__restr
     }
     gsync<G>(gid);
     if (kb + nb < m) {
-      if (gl < 32 && S.dense_stage) dense_prefetch_tile(S, td, lu, kb + 32, min(32, m - kb - 32), gl);
       df_dense_update<G, false>(S, td, lu, y, t0, kb, nb, kb + nb, m, gl);
       gsync<G>(gid);
     }
@@ -1218,7 +1188,6 @@ __device__ __forceinline__ void df_dense_upper(const SProg &S, const df *__restr
   const int4 *td = S.ldesc + S.lev_ptr[S.nlev - 1];
   for (int kb = ((m - 1) / 32) * 32; kb >= 0; kb -= 32) {
     const int nb = min(32, m - kb);
-    if (gl >= 32 && S.dense_stage && kb > 0) dense_prefetch_update<G>(S, td, lu, kb, nb, 0, kb, gl);
     if (gl < 32) {
       const int i = gl;
       df yi{0.f, 0.f};
@@ -1240,7 +1209,6 @@ __device__ __forceinline__ void df_dense_upper(const SProg &S, const df *__restr
     }
     gsync<G>(gid);
     if (kb > 0) {
-      if (gl < 32 && S.dense_stage) dense_prefetch_tile(S, td, lu, kb - 32, 32, gl);
       df_dense_update<G, true>(S, td, lu, y, t0, kb, nb, 0, kb, gl);
       gsync<G>(gid);
     }
