@@ -288,9 +288,15 @@ def test_double_float_group_size_autotuner(oracle_lib, monkeypatch):
         assert rel_err(x[i], ref, mask) < TOL and rel_err(y[i], ref, mask) < TOL
 
 
-def test_probe_only_transient_equals_full_waveform_columns():
+@pytest.mark.parametrize("place", ["auto", "global"])
+def test_probe_only_transient_equals_full_waveform_columns(monkeypatch, place):
     """The probe-only run writes exactly the probed columns of the full double-float run
-    (same arithmetic, bit for bit), row 0 included; out-of-range probes are rejected."""
+    (same arithmetic, bit for bit), row 0 included; out-of-range probes are rejected.  With
+    the factors in global memory (64-thread groups) both runs take the direct
+    right-hand-side step."""
+    if place == "global":
+        monkeypatch.setenv("KRETS_GROUP", "64")
+        monkeypatch.setenv("KRETS_DFD_LU", "global")
     c = rlc_ladder(40)
     t = element_table(c)
     vals = monte_carlo_values(c, 37, seed=17)
@@ -420,12 +426,13 @@ def test_direct_rhs_step_gives_identical_bits(oracle_lib, monkeypatch, G):
     Against the oracle in both error measures."""
     c = rlc_ladder(100)
     m = parse_circuit_description(MIXED_DIRECT)
-    cases = [(c, "tr", 1e-12, monte_carlo_values(c, 20, seed=6)),
-             (c, "be", 1e-12, monte_carlo_values(c, 7, seed=8)),
-             (m, "tr", 2e-11, monte_carlo_values(m, 9, seed=3))]
+    cases = [(c, "tr", False, 1e-12, monte_carlo_values(c, 20, seed=6)),
+             (c, "be", False, 1e-12, monte_carlo_values(c, 7, seed=8)),
+             (c, "be", True, 1e-12, monte_carlo_values(c, 5, seed=9)),   # the reference's source lag
+             (m, "tr", False, 2e-11, monte_carlo_values(m, 9, seed=3))]
     monkeypatch.setenv("KRETS_GROUP", G)
     monkeypatch.setenv("KRETS_DFD_LU", "global")
-    for ckt, method, h, vals in cases:
+    for ckt, method, lag, h, vals in cases:
         t = element_table(ckt)
         outs = {}
         # 20: the default (direct rhs, output converted on the FP64 pipe), 4: direct rhs with
@@ -433,15 +440,15 @@ def test_direct_rhs_step_gives_identical_bits(oracle_lib, monkeypatch, G):
         for opts in ("20", "4", "12"):
             monkeypatch.setenv("KRETS_DFD_OPTS", opts)
             g = _lib.GpuCircuit(t, ckt.size)
-            outs[opts] = g.batch_tran(vals, h, 300, method, lag=False, precision=_lib.PREC_DF)
+            outs[opts] = g.batch_tran(vals, h, 300, method, lag=lag, precision=_lib.PREC_DF)
         np.testing.assert_array_equal(outs["20"], outs["12"])
         np.testing.assert_array_equal(outs["4"], outs["12"])
         monkeypatch.delenv("KRETS_DFD_OPTS")
         monkeypatch.setenv("KRETS_HOST_OUT", "staged")
-        spans = _lib.GpuCircuit(t, ckt.size).batch_tran(vals, h, 300, method, lag=False, precision=_lib.PREC_DF)
+        spans = _lib.GpuCircuit(t, ckt.size).batch_tran(vals, h, 300, method, lag=lag, precision=_lib.PREC_DF)
         monkeypatch.delenv("KRETS_HOST_OUT")
         np.testing.assert_array_equal(spans, outs["20"])
         ti = t.copy()
         ti["value"] = vals[-1]
-        ref = oracle_lib.tran(ti, ckt.size, h, 300, method=method, lag=False)
+        ref = oracle_lib.tran(ti, ckt.size, h, 300, method=method, lag=lag)
         assert rel_err(outs["20"][-1], ref, is_current_mask(ckt)) < TOL
