@@ -128,8 +128,11 @@ def host_buffer(shape, dtype=np.float64) -> np.ndarray:
 
 class PinnedBuffer:
     """A host array page-locked through the library (krets_host_register) until close():
-    the double-float batched transient copies its results into pinned memory at the
-    host link's rate.  `.array` is the numpy view; its pages are touched first."""
+    the double-float batched transient copies its results into pinned memory span by span
+    with the copy engines.  Where the GPU shares the host's page tables (NVLink-C2C) an
+    ordinary array written in place is faster once the buffer is reused; pinning pays for
+    one call into fresh memory, or where the GPU cannot map host memory.  `.array` is the
+    numpy view; its pages are touched first."""
 
     def __init__(self, shape, dtype=np.float64):
         self.array = host_buffer(shape, dtype)
