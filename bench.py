@@ -555,7 +555,7 @@ def workload_ac(args, world, reference):
     z = g.batch_ac(None, f, precision=_lib.PREC_MIXED)[0]
     e2e_ms = g.timing()[1]
     mask = is_current_mask(c)
-    sample = np.arange(0, len(f), 97)
+    sample = np.arange(len(f))   # every point (the oracle takes ~1 s for all of them)
     refz = O.ac(t, c.size, f[sample])
     err = [0.0, 0.0]
     for j, i in enumerate(sample):   # per frequency point: each is its own system
@@ -567,7 +567,7 @@ def workload_ac(args, world, reference):
     peak, pk = measured_peak_hbm()
     return _line(args, world, "AC points/sec", len(f) / k_s, "points/s", wl, {
         "ms_per_step": statistics.mean(cs), "dtype": "c64 factor, c128 refinement", "max_rel_err_vs_fp64": err[0],
-        "max_elementwise_err_vs_fp64": err[1], "accuracy_sample": f"every 97th of {len(f)} points",
+        "max_elementwise_err_vs_fp64": err[1], "accuracy_sample": f"all {len(f)} points",
         "roofline": {"bound": "hbm", "achieved": alg / k_s / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": alg / k_s / 1e9 / peak, "traffic": None, "peak_kind": pk, "kernel": "k_ac_batch<1>",
                      "algorithmic_bytes_per_launch": alg},

@@ -102,7 +102,11 @@ __device__ __forceinline__ void df_tsolve(const int *T, const int *toff, int nut
 // One forward step of the double-float engine on x (in place), as k_tran_dfd; row splits
 // chosen for a group of SG threads (the forward pass splits rows for the whole CTA, the
 // recomputation for its half, so recomputed states match the forward pass's to rounding).
-template <int G, int SG>
+// CBREC (trapezoidal rule): the capacitor history is carried as the companion current in
+// cb itself (cb <- 2 (2C/h) v - cb, as dfd_steps), so no pass after the solve forms the
+// currents and the step ends at the solve's last barrier (the next step's first barrier
+// orders every read of x before the gather overwrites it).
+template <int G, int SG, bool CBREC = false>
 __device__ __forceinline__ void adj_forward_step(const DevProg &P, const SProg &S, const df *lu, df *x, const df *cdyn,
                                                  df *cb, df *icap, const double *vals, int method, int step, double h,
                                                  const WaveTab &wt, int gl, int gid) {
@@ -112,7 +116,12 @@ __device__ __forceinline__ void adj_forward_step(const DevProg &P, const SProg &
     df v{0.f, 0.f};
     if (kind == KRETS_ELEM_C) {
       const df vprev = df_sub(df_at(x, dd.y), df_at(x, dd.z));
-      v = method == KRETS_METHOD_TR ? df_fma(cdyn[d], vprev, icap[d]) : df_mul(cdyn[d], vprev);
+      if (CBREC) {
+        const df c2{2.f * cdyn[d].hi, 2.f * cdyn[d].lo};  // exact doubling
+        v = df_fma(c2, vprev, df_neg(cb[d]));
+      } else {
+        v = method == KRETS_METHOD_TR ? df_fma(cdyn[d], vprev, icap[d]) : df_mul(cdyn[d], vprev);
+      }
     } else if (kind == KRETS_ELEM_L) {
       const df li = df_neg(df_mul(cdyn[d], x[dd.w]));
       v = method == KRETS_METHOD_TR ? df_sub(li, df_sub(df_at(x, dd.y), df_at(x, dd.z))) : li;
@@ -140,6 +149,7 @@ __device__ __forceinline__ void adj_forward_step(const DevProg &P, const SProg &
   gsync<G>(gid);
   df_solve<G, false, SG>(S, lu, x, gl, gid, -1);
   df_solve<G, true, SG>(S, lu, x, gl, gid, -1);
+  if (CBREC) return;
   if (method == KRETS_METHOD_TR) {
     for (int d = gl; d < P.ncap; d += G) {
       const int4 dd = S.dyn[d];
@@ -450,9 +460,20 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
             }
             for (int d = hl; d < P.ncap; d += GH) icap[d] = ck[n + d];
             gsync<GH>(2);
-            for (int s = s0 + 1; s <= s1; ++s) {
-              adj_forward_step<GH, GH>(P, S, lu, x, cdyn, cb, icap, vals, method, s, h, wt, hl, 2);
-              for (int k = hl; k < n; k += GH) sg[(size_t)(s - s0) * n + k] = x[k];
+            if (tr) {  // companion currents of step s0 from the checkpoint's currents
+              for (int d = hl; d < P.ncap; d += GH) {
+                const int4 dd = S.dyn[d];
+                cb[d] = df_sub(df_mul(cdyn[d], df_sub(df_at(x, dd.y), df_at(x, dd.z))), icap[d]);
+              }
+              for (int s = s0 + 1; s <= s1; ++s) {
+                adj_forward_step<GH, GH, true>(P, S, lu, x, cdyn, cb, icap, vals, method, s, h, wt, hl, 2);
+                for (int k = hl; k < n; k += GH) sg[(size_t)(s - s0) * n + k] = x[k];
+              }
+            } else {
+              for (int s = s0 + 1; s <= s1; ++s) {
+                adj_forward_step<GH, GH>(P, S, lu, x, cdyn, cb, icap, vals, method, s, h, wt, hl, 2);
+                for (int k = hl; k < n; k += GH) sg[(size_t)(s - s0) * n + k] = x[k];
+              }
             }
           }
           if (j + 1 < J) segment_gradient(j + 1);
