@@ -229,7 +229,10 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
   int crow[RD];              // backward half: dynamic element's row positions (C: p | m << 16, L: branch)
   int cc0[RK], cc1[RK];      // backward half: up to two C^T terms per row, -1 none, cc1 = -2: use the list
   int erow[RE], ecol[RE];    // recompute half: element's row / column positions (p | m << 16, L: branch)
-  int ekind = 0;             // recompute half: 3 bits per element: 0 none, 1 R, 2 C, 3 L, 4 source
+  int ekind = 0;             // owned elements: 3 bits each: 0 none, 1 R, 2 C, 3 L, 4 source
+  // the backward half, faster per segment, forms the gradient terms of about 3/8 of the
+  // elements (slots i < RB), the recompute half the rest
+  constexpr int RB = (RE * 3 + 4) / 8;
   const int J = (n_steps + K - 1) / K;          // segments
   const size_t ck_words = (size_t)n + P.ncap;  // per checkpoint, in df
   const size_t seg_words = (size_t)(K + 1) * n, hist_words = (size_t)K * n;
@@ -367,12 +370,15 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
             }
           }
         }
-      } else {
+      }
+      // element caches: the backward half owns slots i < RB of its lane's elements, the
+      // recompute half the others (their gradient terms are formed by the owner)
 #pragma unroll
-        for (int i = 0; i < RE; ++i) {
-          const int e = hl + i * GH;
-          erow[i] = ecol[i] = kNone | (kNone << 16);
-          if (e < P.ne) {
+      for (int i = 0; i < RE; ++i) {
+        const int e = hl + i * GH;
+        erow[i] = ecol[i] = kNone | (kNone << 16);
+        if (e < P.ne && (back_half ? i < RB : i >= RB)) {
+          {
             const int4 a = adj[e];
             const int4 pos = P.el_pos[e];
             const int kind = a.x & 0xff;
@@ -448,6 +454,10 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
             df *hn = hs + (size_t)(nn - s0 - 1) * n;
             for (int k = hl; k < n; k += GH) hn[k] = lam[k];
           }
+          if (RB > 0) {  // the segment's lambda history complete: its owned gradient terms
+            gsync<GH>(1);
+            segment_gradient(j);
+          }
         } else {
           if (j > 0) {
             // ---- recompute segment j-1 from its checkpoint into buffer (j-1) % 3
@@ -480,13 +490,13 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
         }
         __syncthreads();
       }
-      if (!back_half) {
-        segment_gradient(0);
-        // scale and write the gradient
+      if (!back_half) segment_gradient(0);
+      {
+        // scale and write the gradient, each half its own elements
 #pragma unroll
         for (int i = 0; i < RE; ++i) {
           const int e = hl + i * GH;
-          if (e >= P.ne) continue;
+          if (e >= P.ne || !(back_half ? i < RB : i >= RB)) continue;
           const int kind = (ekind >> (3 * i)) & 7;
           const double val = vals ? vals[e] : P.el[e].value;
           const double gsum = df_to_double(gr[i]);
