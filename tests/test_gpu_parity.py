@@ -383,7 +383,7 @@ def test_config3_full_size_sampled_parity_and_exact_linearity(oracle_lib):
         assert np.abs(doubled[i] - 2.0 * base[i]).max() <= 1e-12 * scale, i
 
 
-@pytest.mark.parametrize("G", ["64", "128"])
+@pytest.mark.parametrize("G", ["32", "64", "128"])
 def test_factor_placements_give_identical_bits(oracle_lib, monkeypatch, G):
     """The double-float engine with its factors in shared memory (row-descriptor solves)
     and in global memory (interleaved solves, zero-padded levels) runs the same arithmetic:
@@ -416,7 +416,7 @@ MIXED_DIRECT = ("V1 in 0 SIN(0 1 1e9 0 0 0)\nR1 in a 50\nL1 a b 1n\nC1 b 0 1p\nR
                 "C3 c d 1p\nR3 d 0 1k\nI1 e 0 1m\nR4 e 0 1k\n")
 
 
-@pytest.mark.parametrize("G", ["64", "128"])
+@pytest.mark.parametrize("G", ["32", "64", "128"])
 def test_direct_rhs_step_gives_identical_bits(oracle_lib, monkeypatch, G):
     """The interleaved double-float step with a direct right-hand side (each element writes
     the rows it feeds, no gather pass; output converted on the FP64 pipe or by integer
