@@ -1663,7 +1663,7 @@ __device__ __forceinline__ int dfd_steps_lean(const DevProg &P, const int4 *lrec
                                               const IlProg &I, df *&x, df *&b, const df *cdyn, df *cb,
                                               const double *vals, double h, int n_steps, int lag, double *out, int gl,
                                               int gid, WaveTab wt, Probe pr, int s_begin, int row_base,
-                                              bool cvt64, bool wb) {
+                                              bool cvt64) {
   const int n_out = pr.n ? pr.n : P.n;
   const int ncap = P.ncap, nlc = P.ncap + P.n_ind, nd = P.ndyn, nz = P.n_zrow;
   int st = 0;
@@ -1733,15 +1733,10 @@ __device__ __forceinline__ int dfd_steps_lean(const DevProg &P, const int4 *lrec
       for (int j = gl; j < n_out; j += G) {
         const double v = df_to_double(b[qinv[pr.n ? pr.idx[j] : j]]);
         if ((__double2hiint(v) & 0x7ff00000) == 0x7ff00000) st |= KS_NONFINITE;
-        if (wb) row[j] = v;
-        else __stcs(row + j, v);
+        __stcs(row + j, v);
       }
     } else {
-      for (int j = gl; j < n_out; j += G) {
-        const double v = df_out(b[qinv[pr.n ? pr.idx[j] : j]], st);
-        if (wb) row[j] = v;
-        else __stcs(row + j, v);
-      }
+      for (int j = gl; j < n_out; j += G) __stcs(row + j, df_out(b[qinv[pr.n ? pr.idx[j] : j]], st));
     }
     // no barrier: the next step reads b (final since the last solve level) and writes the
     // other buffer, whose last readers finished before this step's first barrier
@@ -1769,8 +1764,7 @@ struct Span {
 // opts bit 0: run narrow levels on one warp; bit 1: integer-only FP64 output conversion;
 // bit 2: trapezoidal capacitor history as companion currents (dfd_steps CBREC); bit 3: no
 // direct right-hand side (host side); bit 4: the direct-rhs step converts its output on
-// the FP64 pipe instead of widening the parts with integer instructions; bit 5: it stores
-// the output rows with ordinary (write-back) stores instead of streaming ones.
+// the FP64 pipe instead of widening the parts with integer instructions.
 // LUG: the factors live in global memory (an L2-resident region per group, lu_glob), the
 // rest of the instance in shared memory: about a third of the shared memory per instance,
 // so up to 14 instances share an SM (each step's critical path is a chain of level
@@ -1914,12 +1908,10 @@ __global__ void __launch_bounds__(896, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
       df *xs = x, *bs = cb;
       if (cbrec)
         st |= dfd_steps_lean<G, true>(P, lrec, zrow, qinv, I, xs, bs, cdyn, icap, vals, h, n_steps, lag, out, gl,
-                                      gid, wt, pr, sp.s_begin, sp.row_base, (opts & 16) != 0,
-                                      (opts & 32) != 0);
+                                      gid, wt, pr, sp.s_begin, sp.row_base, (opts & 16) != 0);
       else
         st |= dfd_steps_lean<G, false>(P, lrec, zrow, qinv, I, xs, bs, cdyn, icap, vals, h, n_steps, lag, out, gl,
-                                       gid, wt, pr, sp.s_begin, sp.row_base, (opts & 16) != 0,
-                                      (opts & 32) != 0);
+                                       gid, wt, pr, sp.s_begin, sp.row_base, (opts & 16) != 0);
       xfin = xs;
     } else if (!fatal) {
       if (cbrec)
