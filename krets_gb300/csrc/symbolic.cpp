@@ -342,11 +342,12 @@ int gp_factor(int n, const std::vector<int> &ap, const std::vector<int> &ai, con
       piv_row[j] = ip;
       F.pinv[R[ip]] = k;
       for (int i = 0; i < c; ++i) lcol[i] = used[i] ? T(0) : cj[i] / piv;
+      const T *__restrict__ lc = lcol.data();
       for (int jj = j + 1; jj < c; ++jj) {
-        T *cc = S.data() + (size_t)jj * c;
+        T *__restrict__ cc = S.data() + (size_t)jj * c;
         const T u = cc[ip];
         if (u == T(0)) continue;
-        for (int i = 0; i < c; ++i) cc[i] -= lcol[i] * u;
+        for (int i = 0; i < c; ++i) cc[i] -= lc[i] * u;
       }
     }
     // patterns: U column k = the sparse pivots it reaches, every earlier block pivot and
