@@ -353,6 +353,11 @@ __device__ __forceinline__ double sum_rhs(const DevProg &P, int k, const double 
 // ------------------------------------------------------------------ factor / solves
 // In-place static-pivot LU of lu[] (values in position space).  Returns status bits.
 // Status bits are OR-ed into *status (shared or global) by the threads that see them.
+// The diagonal slots hold the reciprocal pivots 1/u_kk on exit (usolve multiplies by
+// them): a row's pivots then cost one multiply each instead of a division, which in FP64
+// is a chain of about ten instructions on a pipe that issues at 1/64 of the FP32 rate,
+// and a factorisation's deepest rows run one pivot after another.  Rows of one level read
+// only the diagonals of earlier levels, so a row inverts its own pivot when it finishes.
 template <typename T>
 __device__ void factor(const DevProg &P, T *lu, int *status) {
   int bad = 0;
@@ -362,16 +367,18 @@ __device__ void factor(const DevProg &P, T *lu, int *status) {
       int k = P.lev_rows[t];
       for (int pi = P.piv_ptr[k]; pi < P.piv_ptr[k + 1]; ++pi) {
         int4 pv = P.piv[pi];
-        T l_kj = lu[pv.x] / lu[P.lu_diag[pv.y]];
+        T l_kj = lu[pv.x] * lu[P.lu_diag[pv.y]];
         lu[pv.x] = l_kj;
         for (int u = pv.z; u < pv.w; ++u) {
           int2 d = P.upd[u];
           lu[d.x] = lu[d.x] - l_kj * lu[d.y];
         }
       }
-      T dk = lu[P.lu_diag[k]];
+      const int dg = P.lu_diag[k];
+      T dk = lu[dg];
       if (!(scal<T>::mag(dk) > 0)) bad |= KS_SINGULAR;
       else if (!scal<T>::finite(dk)) bad |= KS_NONFINITE;
+      lu[dg] = T(1) / dk;
     }
     __syncthreads();
   }
@@ -402,7 +409,7 @@ __device__ void usolve(const DevProg &P, const T *lu, V *y) {
       V s = y[k];
       int dg = P.lu_diag[k];
       for (int u = dg + 1; u < P.lu_rowptr[k + 1]; ++u) s = s - V(lu[u]) * y[P.lu_col[u]];
-      y[k] = s / V(lu[dg]);
+      y[k] = s * V(lu[dg]);  // reciprocal pivot
     }
     __syncthreads();
   }
