@@ -499,25 +499,53 @@ krets_status dev_view(const void *user, size_t bytes, bool in, cudaStream_t s, D
 }
 
 // Program arrays a launch of at most one CTA per SM warms into L1 (see warm_l1):
-// factorisation, solves, then stamps.  Empty when CTAs share SMs.
-OpWarm plan_warm(const DevProgram *D, int n_inst) {
+// factorisation, solves, then stamps; only the stamps when the first group is staged in
+// shared memory (plan_stage).  Empty when CTAs share SMs.
+OpWarm plan_warm(const DevProgram *D, int n_inst, bool staged = false) {
   OpWarm w{};
   if (n_inst > device_sm_count()) return w;
   const DevProg &V = D->view;
   const Program &H = D->host;
-  const struct { const void *p; size_t words; } fs[] = {
-      {V.piv_ptr, H.piv_ptr.size()}, {V.piv, H.piv.size()},         {V.upd, H.upd.size()},
-      {V.lu_diag, H.lu_diag.size()}, {V.lev_rows, H.lev_rows.size()}, {V.lu_rowptr, H.lu_rowptr.size()},
-      {V.lu_col, H.lu_col.size()},   {V.ulev_rows, H.ulev_rows.size()}, {V.lu_src, H.lu_col.size()},
-      {V.a_cptr, H.a_cptr.size()},   {V.a_contrib, H.a_contrib.size()}, {V.b_cptr, H.b_cptr.size()},
-      {V.b_contrib, H.b_contrib.size()}};
+  const struct { const void *p; size_t words; bool fac; } fs[] = {
+      {V.piv_ptr, H.piv_ptr.size(), true},    {V.piv, H.piv.size(), true},
+      {V.upd, H.upd.size(), true},            {V.lu_diag, H.lu_diag.size(), true},
+      {V.lev_rows, H.lev_rows.size(), true},  {V.lu_rowptr, H.lu_rowptr.size(), true},
+      {V.lu_col, H.lu_col.size(), true},      {V.ulev_rows, H.ulev_rows.size(), true},
+      {V.lu_src, H.lu_col.size(), false},     {V.a_cptr, H.a_cptr.size(), false},
+      {V.a_contrib, H.a_contrib.size(), false}, {V.b_cptr, H.b_cptr.size(), false},
+      {V.b_contrib, H.b_contrib.size(), false}};
   for (const auto &f : fs) {
-    if (f.words == 0 || w.count == 16) continue;
+    if (f.words == 0 || w.count == 16 || (staged && f.fac)) continue;
     w.ptr[w.count] = static_cast<const char *>(f.p);
     w.bytes[w.count] = (int)(4 * f.words);
     ++w.count;
   }
   return w;
+}
+
+// Shared-memory copies of the factorisation and solve arrays (see stage_fac) for launches
+// of at most one CTA per SM whose workspace leaves room for them; L.bytes grows by the
+// staged region, so the launch sizes its dynamic shared memory for both.
+OpStage plan_stage(const DevProgram *D, int n_inst, Lay &L) {
+  OpStage S{};
+  if (n_inst > device_sm_count()) return S;
+  const Program &H = D->host;
+  const size_t words[10] = {H.lev_ptr.size(),   H.lev_rows.size(), H.piv_ptr.size(),   H.lu_diag.size(),
+                            H.lu_rowptr.size(), H.lu_col.size(),   H.ulev_ptr.size(),  H.ulev_rows.size(),
+                            H.piv.size(),       H.upd.size()};
+  const size_t off = align16(L.bytes);
+  size_t at = 0;
+  for (int a = 0; a < 10; ++a) {
+    const size_t n16 = (words[a] * 4 + 15) / 16;
+    S.at[a] = (int)at;
+    S.n16[a] = (int)n16;
+    at += 16 * n16;
+  }
+  if (off + at > (size_t)max_smem_optin()) return OpStage{};
+  S.on = 1;
+  S.off = (int)off;
+  L.bytes = off + at;
+  return S;
 }
 
 krets_status run_op(krets_circuit *c, DevProgram *D, int n_inst, const double *d_values, double *d_x,
@@ -526,10 +554,11 @@ krets_status run_op(krets_circuit *c, DevProgram *D, int n_inst, const double *d
   int grid;
   size_t smem;
   char *gws;
+  const OpStage stage = plan_stage(D, n_inst, L);
   krets_status s = plan_launch(c, k_op, L, threads, n_inst, grid, smem, gws);
   if (s != KRETS_OK) return s;
   k_op<<<grid, threads, smem, c->stream>>>(D->view, c->cfg, L, gws, d_values, d_x, out_stride, d_status, d_iters,
-                                          n_inst, plan_warm(D, n_inst));
+                                          n_inst, plan_warm(D, n_inst, stage.on), stage);
   g_launches++;
   CU(cudaGetLastError());
   return KRETS_OK;
@@ -797,12 +826,13 @@ krets_status run_dc(krets_circuit *c, int32_t sweep_elem, double start, double s
   int threads = plain_threads(D->view), grid;
   size_t smem;
   char *gws;
+  const OpStage stage = plan_stage(D, n_inst, L);
   s = plan_launch(c, k_dc_sweep, L, threads, n_inst, grid, smem, gws);
   if (s) return s;
   CU(cudaEventRecord(c->ev[2], c->stream));
   k_dc_sweep<<<grid, threads, smem, c->stream>>>(D->view, c->cfg, L, gws, sweep_elem, start, step, np,
                                                  (const double *)dv, n_inst, (size_t)c->n * np, (double *)dx,
-                                                 d_status, plan_warm(D, n_inst));
+                                                 d_status, plan_warm(D, n_inst, stage.on), stage);
   g_launches++;
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[3], c->stream));

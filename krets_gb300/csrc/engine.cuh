@@ -351,6 +351,22 @@ __device__ __forceinline__ double sum_rhs(const DevProg &P, int k, const double 
 }
 
 // ------------------------------------------------------------------ factor / solves
+// The arrays the factorisation and the two solves read.  They come from the program in
+// global memory (fac_view), or from copies in shared memory that a single-CTA solve makes
+// first (k_op, k_dc_sweep): the factorisation's deepest rows then wait on shared-memory
+// rather than L2 latency at every pivot.
+struct FacView {
+  int nlev, nulev;
+  const int *lev_ptr, *lev_rows, *piv_ptr, *lu_diag, *lu_rowptr, *lu_col, *ulev_ptr, *ulev_rows;
+  const int4 *piv;
+  const int2 *upd;
+};
+
+__device__ __forceinline__ FacView fac_view(const DevProg &P) {
+  return FacView{P.nlev,      P.nulev,     P.lev_ptr, P.lev_rows, P.piv_ptr, P.lu_diag,
+                 P.lu_rowptr, P.lu_col,    P.ulev_ptr, P.ulev_rows, P.piv,     P.upd};
+}
+
 // In-place static-pivot LU of lu[] (values in position space).  Returns status bits.
 // Status bits are OR-ed into *status (shared or global) by the threads that see them.
 // The diagonal slots hold the reciprocal pivots 1/u_kk on exit (usolve multiplies by
@@ -359,22 +375,22 @@ __device__ __forceinline__ double sum_rhs(const DevProg &P, int k, const double 
 // and a factorisation's deepest rows run one pivot after another.  Rows of one level read
 // only the diagonals of earlier levels, so a row inverts its own pivot when it finishes.
 template <typename T>
-__device__ void factor(const DevProg &P, T *lu, int *status) {
+__device__ __forceinline__ void factor_v(const FacView &F, T *lu, int *status) {
   int bad = 0;
-  for (int l = 0; l < P.nlev; ++l) {
-    int r0 = P.lev_ptr[l], r1 = P.lev_ptr[l + 1];
+  for (int l = 0; l < F.nlev; ++l) {
+    int r0 = F.lev_ptr[l], r1 = F.lev_ptr[l + 1];
     for (int t = r0 + threadIdx.x; t < r1; t += blockDim.x) {
-      int k = P.lev_rows[t];
-      for (int pi = P.piv_ptr[k]; pi < P.piv_ptr[k + 1]; ++pi) {
-        int4 pv = P.piv[pi];
-        T l_kj = lu[pv.x] * lu[P.lu_diag[pv.y]];
+      int k = F.lev_rows[t];
+      for (int pi = F.piv_ptr[k]; pi < F.piv_ptr[k + 1]; ++pi) {
+        int4 pv = F.piv[pi];
+        T l_kj = lu[pv.x] * lu[F.lu_diag[pv.y]];
         lu[pv.x] = l_kj;
         for (int u = pv.z; u < pv.w; ++u) {
-          int2 d = P.upd[u];
+          int2 d = F.upd[u];
           lu[d.x] = lu[d.x] - l_kj * lu[d.y];
         }
       }
-      const int dg = P.lu_diag[k];
+      const int dg = F.lu_diag[k];
       T dk = lu[dg];
       if (!(scal<T>::mag(dk) > 0)) bad |= KS_SINGULAR;
       else if (!scal<T>::finite(dk)) bad |= KS_NONFINITE;
@@ -387,13 +403,13 @@ __device__ void factor(const DevProg &P, T *lu, int *status) {
 }
 
 template <typename T, typename V>
-__device__ void lsolve(const DevProg &P, const T *lu, V *y) {
-  for (int l = 1; l < P.nlev; ++l) {  // level 0 rows have no L entries
-    int r0 = P.lev_ptr[l], r1 = P.lev_ptr[l + 1];
+__device__ __forceinline__ void lsolve_v(const FacView &F, const T *lu, V *y) {
+  for (int l = 1; l < F.nlev; ++l) {  // level 0 rows have no L entries
+    int r0 = F.lev_ptr[l], r1 = F.lev_ptr[l + 1];
     for (int t = r0 + threadIdx.x; t < r1; t += blockDim.x) {
-      int k = P.lev_rows[t];
+      int k = F.lev_rows[t];
       V s = y[k];
-      for (int u = P.lu_rowptr[k]; u < P.lu_diag[k]; ++u) s = s - V(lu[u]) * y[P.lu_col[u]];
+      for (int u = F.lu_rowptr[k]; u < F.lu_diag[k]; ++u) s = s - V(lu[u]) * y[F.lu_col[u]];
       y[k] = s;
     }
     __syncthreads();
@@ -401,18 +417,33 @@ __device__ void lsolve(const DevProg &P, const T *lu, V *y) {
 }
 
 template <typename T, typename V>
-__device__ void usolve(const DevProg &P, const T *lu, V *y) {
-  for (int l = 0; l < P.nulev; ++l) {
-    int r0 = P.ulev_ptr[l], r1 = P.ulev_ptr[l + 1];
+__device__ __forceinline__ void usolve_v(const FacView &F, const T *lu, V *y) {
+  for (int l = 0; l < F.nulev; ++l) {
+    int r0 = F.ulev_ptr[l], r1 = F.ulev_ptr[l + 1];
     for (int t = r0 + threadIdx.x; t < r1; t += blockDim.x) {
-      int k = P.ulev_rows[t];
+      int k = F.ulev_rows[t];
       V s = y[k];
-      int dg = P.lu_diag[k];
-      for (int u = dg + 1; u < P.lu_rowptr[k + 1]; ++u) s = s - V(lu[u]) * y[P.lu_col[u]];
+      int dg = F.lu_diag[k];
+      for (int u = dg + 1; u < F.lu_rowptr[k + 1]; ++u) s = s - V(lu[u]) * y[F.lu_col[u]];
       y[k] = s * V(lu[dg]);  // reciprocal pivot
     }
     __syncthreads();
   }
+}
+
+template <typename T>
+__device__ void factor(const DevProg &P, T *lu, int *status) {
+  factor_v<T>(fac_view(P), lu, status);
+}
+
+template <typename T, typename V>
+__device__ void lsolve(const DevProg &P, const T *lu, V *y) {
+  lsolve_v<T, V>(fac_view(P), lu, y);
+}
+
+template <typename T, typename V>
+__device__ void usolve(const DevProg &P, const T *lu, V *y) {
+  usolve_v<T, V>(fac_view(P), lu, y);
 }
 
 }  // namespace krets

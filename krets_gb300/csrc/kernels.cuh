@@ -108,12 +108,48 @@ __device__ __forceinline__ void warm_l1(const OpWarm &w) {
       asm volatile("prefetch.global.L1 [%0];" ::"l"(w.ptr[a] + off));
 }
 
+// ============================================================== program staging
+// A single-CTA solve whose workspace leaves room copies the factorisation and solve arrays
+// into shared memory behind the workspace (byte `off` of the dynamic shared memory) before
+// its first factorisation.  Array a goes to off + at[a] (16-byte aligned) as n16[a]
+// 16-byte words: the program image keeps every array at a 16-byte aligned offset, so the
+// words a copy rounds up to stay inside the image.  Order: lev_ptr, lev_rows, piv_ptr,
+// lu_diag, lu_rowptr, lu_col, ulev_ptr, ulev_rows, piv, upd.
+struct OpStage {
+  int on, off;
+  int at[10], n16[10];
+};
+
+__device__ __forceinline__ void stage_fac(const OpStage &S, char *smem, FacView &F) {
+  if (!S.on) return;
+  const void *src[10] = {F.lev_ptr,   F.lev_rows, F.piv_ptr,  F.lu_diag,   F.lu_rowptr,
+                         F.lu_col,    F.ulev_ptr, F.ulev_rows, F.piv,      F.upd};
+  char *dst = smem + S.off;
+#pragma unroll
+  for (int a = 0; a < 10; ++a) {
+    const int4 *s4 = reinterpret_cast<const int4 *>(src[a]);
+    int4 *d4 = reinterpret_cast<int4 *>(dst + S.at[a]);
+    for (int i = threadIdx.x; i < S.n16[a]; i += blockDim.x) d4[i] = s4[i];
+  }
+  __syncthreads();
+  F.lev_ptr = reinterpret_cast<const int *>(dst + S.at[0]);
+  F.lev_rows = reinterpret_cast<const int *>(dst + S.at[1]);
+  F.piv_ptr = reinterpret_cast<const int *>(dst + S.at[2]);
+  F.lu_diag = reinterpret_cast<const int *>(dst + S.at[3]);
+  F.lu_rowptr = reinterpret_cast<const int *>(dst + S.at[4]);
+  F.lu_col = reinterpret_cast<const int *>(dst + S.at[5]);
+  F.ulev_ptr = reinterpret_cast<const int *>(dst + S.at[6]);
+  F.ulev_rows = reinterpret_cast<const int *>(dst + S.at[7]);
+  F.piv = reinterpret_cast<const int4 *>(dst + S.at[8]);
+  F.upd = reinterpret_cast<const int2 *>(dst + S.at[9]);
+}
+
 // ============================================================== k_op
 // Newton OP in FP64.  guess0 (optional, original numbering) warm-starts the iteration
 // as the DC sweep does; step_key >= 0 adds the "step" key to the convergence test.
-__device__ int newton_dc(const DevProg &P, const KCfg &cfg, const double *vals, double *lu, double *b, double *x,
-                         double *guess, double *ca, double *cb, int *status, bool guess_empty, double step_key,
-                         int *iters_out) {
+__device__ int newton_dc(const DevProg &P, const FacView &F, const KCfg &cfg, const double *vals, double *lu,
+                         double *b, double *x, double *guess, double *ca, double *cb, int *status, bool guess_empty,
+                         double step_key, int *iters_out) {
   PassCtx c{};
   c.mode = 0;
   c.guess = guess;
@@ -126,12 +162,12 @@ __device__ int newton_dc(const DevProg &P, const KCfg &cfg, const double *vals, 
     stamp_lu<double>(P, lu, ca, nullptr);
     for (int k = threadIdx.x; k < P.n; k += blockDim.x) b[k] = sum_rhs(P, k, cb);
     __syncthreads();
-    factor<double>(P, lu, status);
+    factor_v<double>(F, lu, status);
     if (*status & (KS_SINGULAR | KS_NONFINITE | KS_NOTIMPL)) break;
     for (int k = threadIdx.x; k < P.n; k += blockDim.x) x[k] = b[k];
     __syncthreads();
-    lsolve<double, double>(P, lu, x);
-    usolve<double, double>(P, lu, x);
+    lsolve_v<double, double>(F, lu, x);
+    usolve_v<double, double>(F, lu, x);
     if (!P.nonlinear) break;
     bool conv = !c.guess_empty && converged(P, cfg, guess, x, step_key >= 0.0, prev_step, step_key);
     if (conv) break;
@@ -149,10 +185,12 @@ __device__ int newton_dc(const DevProg &P, const KCfg &cfg, const double *vals, 
 }
 
 __global__ void k_op(DevProg P, KCfg cfg, Lay L, char *gws, const double *values, double *x_out,
-                     size_t out_stride, int *inst_status, int *iters, int n_inst, OpWarm warm) {
+                     size_t out_stride, int *inst_status, int *iters, int n_inst, OpWarm warm, OpStage stage) {
   extern __shared__ __align__(16) char smem[];
   char *base = gws ? gws + (size_t)blockIdx.x * L.bytes : smem;
   warm_l1(warm);
+  FacView F = fac_view(P);
+  stage_fac(stage, smem, F);
   ARR(double, lu, 0);
   ARR(double, b, 1);
   ARR(double, x, 2);
@@ -164,7 +202,7 @@ __global__ void k_op(DevProg P, KCfg cfg, Lay L, char *gws, const double *values
     if (threadIdx.x == 0) *status = 0;
     __syncthreads();
     const double *vals = values ? values + (size_t)inst * P.ne : nullptr;
-    newton_dc(P, cfg, vals, lu, b, x, guess, ca, cb, status, true, -1.0, iters ? iters + inst : nullptr);
+    newton_dc(P, F, cfg, vals, lu, b, x, guess, ca, cb, status, true, -1.0, iters ? iters + inst : nullptr);
     for (int k = threadIdx.x; k < P.n; k += blockDim.x) x_out[(size_t)inst * out_stride + P.q[k]] = x[k];
     if (threadIdx.x == 0 && inst_status) inst_status[inst] = *status;
     __syncthreads();
@@ -177,10 +215,12 @@ __global__ void k_op(DevProg P, KCfg cfg, Lay L, char *gws, const double *values
 // and stops at its first failing point, as dc::solve returns on the first error.
 __global__ void k_dc_sweep(DevProg P, KCfg cfg, Lay L, char *gws, int sweep_elem, double start, double step,
                            int n_points, const double *values, int n_inst, size_t inst_stride, double *x_out,
-                           int *out_status, OpWarm warm) {
+                           int *out_status, OpWarm warm, OpStage stage) {
   extern __shared__ __align__(16) char smem[];
   char *base = gws ? gws + (size_t)blockIdx.x * L.bytes : smem;
   warm_l1(warm);
+  FacView F = fac_view(P);
+  stage_fac(stage, smem, F);
   ARR(double, lu, 0);
   ARR(double, b, 1);
   ARR(double, x, 2);
@@ -200,7 +240,7 @@ __global__ void k_dc_sweep(DevProg P, KCfg cfg, Lay L, char *gws, int sweep_elem
       // warm start from the previous point's solution (dc.rs:167)
       for (int k = threadIdx.x; k < P.n; k += blockDim.x) guess[k] = x[k];
       __syncthreads();
-      newton_dc(P, cfg, vals, lu, b, x, guess, ca, cb, status, i == 0, (double)i, nullptr);
+      newton_dc(P, F, cfg, vals, lu, b, x, guess, ca, cb, status, i == 0, (double)i, nullptr);
       for (int k = threadIdx.x; k < P.n; k += blockDim.x) out[(size_t)i * P.n + P.q[k]] = x[k];
       __syncthreads();
       if (*status) break;
