@@ -155,6 +155,9 @@ struct krets_circuit {
   void *scratch = nullptr;
   size_t scratch_bytes = 0;
   int *d_small = nullptr;  // counters / status words
+  // status words of single solves in mapped pinned host memory (host and device address):
+  // the kernel writes them where the host reads them, so a call needs no copy for them
+  int *h_small = nullptr, *h_small_dev = nullptr;
   unsigned long long *d_hist = nullptr;
   long long hist[8] = {};
   int fallbacks = 0;
@@ -179,6 +182,7 @@ struct krets_circuit {
     if (d_el) cudaFree(d_el);
     if (scratch) cudaFree(scratch);
     if (d_small) cudaFree(d_small);
+    if (h_small) cudaFreeHost(h_small);
     if (d_hist) cudaFree(d_hist);
     if (l2buf) cudaFree(l2buf);
     for (auto &e : ev)
@@ -442,6 +446,39 @@ Lay layout_ac(const DevProg &P, bool mixed) {
   return B.done();
 }
 
+// Resident CTAs per SM of a kernel at a block size and dynamic shared memory, with the
+// kernel's shared-memory limit raised to that size.  Both runtime queries cost
+// microseconds, which a single-solve call would pay every time, so the answers are kept
+// per (device, kernel, block size, shared memory); the limit is only ever raised.
+template <typename K>
+krets_status kernel_fit(K kernel, int threads, size_t smem, int &per_sm) {
+  struct Fit { int dev; const void *k; int threads; size_t smem; int per_sm; };
+  struct Limit { int dev; const void *k; size_t smem; };
+  static std::mutex mu;
+  static std::vector<Fit> fits;
+  static std::vector<Limit> limits;
+  int dev = 0;
+  CU(cudaGetDevice(&dev));
+  const void *k = reinterpret_cast<const void *>(kernel);
+  std::lock_guard<std::mutex> lock(mu);
+  for (const Fit &f : fits)
+    if (f.dev == dev && f.k == k && f.threads == threads && f.smem == smem) {
+      per_sm = f.per_sm;
+      return KRETS_OK;
+    }
+  Limit *lim = nullptr;
+  for (Limit &l : limits)
+    if (l.dev == dev && l.k == k) lim = &l;
+  if (!lim || lim->smem < smem) {
+    CU(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (lim) lim->smem = smem;
+    else limits.push_back(Limit{dev, k, smem});
+  }
+  CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
+  fits.push_back(Fit{dev, k, threads, smem, per_sm});
+  return KRETS_OK;
+}
+
 // Decide shared vs global placement and the grid for a per-CTA workspace.
 template <typename K>
 krets_status plan_launch(krets_circuit *c, K kernel, const Lay &L, int threads, int items, int &grid,
@@ -449,9 +486,9 @@ krets_status plan_launch(krets_circuit *c, K kernel, const Lay &L, int threads, 
   if (L.bytes <= max_smem_optin()) {
     smem = L.bytes;
     gws = nullptr;
-    CU(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
+    krets_status s = kernel_fit(kernel, threads, smem, per_sm);
+    if (s != KRETS_OK) return s;
     if (per_sm < 1) per_sm = 1;
     grid = std::max(1, std::min(items, per_sm * device_sm_count()));
   } else {
@@ -740,18 +777,25 @@ krets_status krets_op(krets_circuit *c, double *x_out, int32_t *iters_out) {
   if (s != KRETS_OK) return s == KRETS_ERR_DECOMPOSITION_FAILED ? KRETS_ERR_MATRIX_DECOMPOSITION : s;
   DevBuf tx;
   void *dx;
+  if (!c->h_small) {
+    void *hp = nullptr, *dp = nullptr;
+    CU(cudaHostAlloc(&hp, 64, cudaHostAllocMapped));
+    c->h_small = static_cast<int *>(hp);
+    CU(cudaHostGetDevicePointer(&dp, hp, 0));
+    c->h_small_dev = static_cast<int *>(dp);
+  }
+  // the previous call on this stream has finished (it synchronised), so nothing writes these
+  volatile int *h = c->h_small;
+  h[0] = 0;
+  h[1] = 0;
   CU(cudaEventRecord(c->ev[0], c->stream));
   s = dev_view(x_out, sizeof(double) * c->n, false, c->stream, tx, &dx);
   if (s) return s;
-  int *d_status = c->d_small, *d_iters = c->d_small + 1;
-  CU(cudaMemsetAsync(c->d_small, 0, 16, c->stream));
   CU(cudaEventRecord(c->ev[2], c->stream));
-  s = run_op(c, D, 1, nullptr, (double *)dx, c->n, d_status, d_iters, plain_threads(D->view));
+  s = run_op(c, D, 1, nullptr, (double *)dx, c->n, c->h_small_dev, c->h_small_dev + 1, plain_threads(D->view));
   if (s) return s;
   CU(cudaEventRecord(c->ev[3], c->stream));
   if (tx.p) CU(cudaMemcpyAsync(x_out, dx, sizeof(double) * c->n, cudaMemcpyDeviceToHost, c->stream));
-  int h[2];
-  CU(cudaMemcpyAsync(h, c->d_small, sizeof h, cudaMemcpyDeviceToHost, c->stream));
   CU(cudaEventRecord(c->ev[1], c->stream));
   CU(cudaStreamSynchronize(c->stream));
   cudaEventElapsedTime(&c->kernel_ms, c->ev[2], c->ev[3]);
