@@ -381,14 +381,33 @@ __device__ __forceinline__ void factor_v(const FacView &F, T *lu, int *status) {
     int r0 = F.lev_ptr[l], r1 = F.lev_ptr[l + 1];
     for (int t = r0 + threadIdx.x; t < r1; t += blockDim.x) {
       int k = F.lev_rows[t];
-      for (int pi = F.piv_ptr[k]; pi < F.piv_ptr[k + 1]; ++pi) {
-        int4 pv = F.piv[pi];
-        T l_kj = lu[pv.x] * lu[F.lu_diag[pv.y]];
+      // A row's pivots run one after another.  What a pivot needs besides its own entry —
+      // its record, the reciprocal pivot of row j (final: an earlier level) and its first
+      // update pair — is loaded one pivot ahead, before the stores that the compiler must
+      // otherwise assume they alias, so each step of the chain waits only on its entry.
+      const int p0 = F.piv_ptr[k], p1 = F.piv_ptr[k + 1];
+      int4 pv = p0 < p1 ? F.piv[p0] : make_int4(0, 0, 0, 0);
+      T rd = p0 < p1 ? lu[F.lu_diag[pv.y]] : T(0);
+      int2 d = p0 < p1 && pv.z < pv.w ? F.upd[pv.z] : make_int2(0, 0);
+      for (int pi = p0; pi < p1; ++pi) {
+        int4 pn = pv;
+        T rn = rd;
+        int2 dn0 = d;
+        if (pi + 1 < p1) {
+          pn = F.piv[pi + 1];
+          rn = lu[F.lu_diag[pn.y]];
+          if (pn.z < pn.w) dn0 = F.upd[pn.z];
+        }
+        const T l_kj = lu[pv.x] * rd;
         lu[pv.x] = l_kj;
         for (int u = pv.z; u < pv.w; ++u) {
-          int2 d = F.upd[u];
+          const int2 dn = u + 1 < pv.w ? F.upd[u + 1] : d;
           lu[d.x] = lu[d.x] - l_kj * lu[d.y];
+          d = dn;
         }
+        pv = pn;
+        rd = rn;
+        d = dn0;
       }
       const int dg = F.lu_diag[k];
       T dk = lu[dg];
