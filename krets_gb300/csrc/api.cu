@@ -428,7 +428,32 @@ Lay layout_adaptive(const DevProg &P) {
   return B.done();
 }
 
+// MIXED: the stamping pass's coefficient arrays (slots 6, 7, 8) are dead once the
+// complex128 matrix and the rhs are summed, so the complex64 LU, the correction and the
+// solution (slots 2, 5, 3) reuse their bytes; the element values (slot 0) are read from
+// the caller's array.  That keeps a CTA of the 500-section ladder near 68 KB, three per SM.
 Lay layout_ac(const DevProg &P, bool mixed) {
+  if (mixed) {
+    LayBuilder B;
+    B.add(1, 16 * (size_t)P.nnz_a);
+    B.add(4, 16 * (size_t)P.n);
+    B.add(9, sizeof(double) * P.n);
+    B.add(10, sizeof(double) * 32);
+    B.add(11, sizeof(int) * 4);
+    B.add(12, sizeof(int) * 4);
+    const size_t r0 = B.cur;
+    B.add(6, sizeof(double) * P.n_coef);
+    B.add(7, sizeof(double) * P.n_coef);
+    B.add(8, sizeof(double) * P.ne);
+    const size_t r1 = B.cur;
+    B.cur = r0;
+    B.add(2, 8 * (size_t)P.nnz_lu);
+    B.add(5, 8 * (size_t)P.n);
+    B.add(3, 16 * (size_t)P.n);
+    B.cur = std::max(B.cur, r1);
+    B.L.off[0] = -1;
+    return B.done();
+  }
   LayBuilder B;
   B.add(0, sizeof(double) * P.ne);
   B.add(1, mixed ? 16 * (size_t)P.nnz_a : 0);

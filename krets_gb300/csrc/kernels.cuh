@@ -729,7 +729,7 @@ __global__ void k_ac_batch(DevProg P, Lay L, char *gws, const double *values, co
   char *base = gws ? gws + (size_t)blockIdx.x * L.bytes : smem;
   using C64 = cx<double>;
   using C32 = cx<float>;
-  ARR(double, vals, 0);
+  double *vals = MIXED ? nullptr : reinterpret_cast<double *>(base + L.off[0]);  // MIXED: caller's values
   ARR(C64, a128, 1);
   ARR(C64, x, 3);
   ARR(C64, b, 4);
@@ -751,8 +751,9 @@ __global__ void k_ac_batch(DevProg P, Lay L, char *gws, const double *values, co
     if (it_idx >= total) break;
     int inst = it_idx / n_freq, fi = it_idx % n_freq;
     if (threadIdx.x == 0) *status = 0;
-    for (int e = threadIdx.x; e < P.ne; e += blockDim.x)
-      vals[e] = values ? values[(size_t)inst * P.ne + e] : P.el[e].value;
+    if (!MIXED)
+      for (int e = threadIdx.x; e < P.ne; e += blockDim.x)
+        vals[e] = values ? values[(size_t)inst * P.ne + e] : P.el[e].value;
     for (int k = threadIdx.x; k < P.n; k += blockDim.x) opx[k] = op_x[(size_t)inst * P.n + P.q[k]];
     __syncthreads();
     PassCtx c{};
@@ -760,7 +761,7 @@ __global__ void k_ac_batch(DevProg P, Lay L, char *gws, const double *values, co
     c.freq = freqs[fi];
     c.guess = opx;
     c.guess_empty = false;
-    coef_pass(P, vals, c, ca_re, ca_im, cb, status);
+    coef_pass(P, MIXED ? (values ? values + (size_t)inst * P.ne : nullptr) : vals, c, ca_re, ca_im, cb, status);
     __syncthreads();
     for (int k = threadIdx.x; k < P.n; k += blockDim.x) b[k] = C64(sum_rhs(P, k, cb), 0.0);
     if (MIXED) {
