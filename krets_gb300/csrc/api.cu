@@ -1059,7 +1059,10 @@ krets_status krets_batch_ac(krets_circuit *c, int32_t n_inst, const double *valu
   if (s) return s;
   bool mixed = precision == KRETS_PREC_MIXED;
   Lay L = layout_ac(Dac->view, mixed);
-  int threads = 128, grid;
+  // one complex system per CTA, latency bound: 256 threads (for n >= 256; measured on the
+  // 500-section ladder, three CTAs per SM: 128 threads 2.61e6, 256 2.87e6, 384 2.91e6, 512
+  // 2.60e6 points/s)
+  int threads = Dac->view.n >= 256 ? 256 : 128, grid;
   size_t smem;
   char *gws;
   auto kern = mixed ? k_ac_batch<1> : k_ac_batch<0>;
