@@ -38,12 +38,55 @@ struct TranState {
 
 #define ARR(T, name, idx) T *name = reinterpret_cast<T *>(base + L.off[idx])
 
+// One contribution of an A entry (packed slot << 2 | unit << 1 | neg), signed.
+template <typename T>
+__device__ __forceinline__ T contrib_value(int code, const double *ca_re, const double *ca_im);
+template <>
+__device__ __forceinline__ double contrib_value<double>(int code, const double *ca_re, const double *) {
+  const double v = (code & 2) ? 1.0 : ca_re[code >> 2];
+  return (code & 1) ? -v : v;
+}
+template <>
+__device__ __forceinline__ cx<double> contrib_value<cx<double>>(int code, const double *ca_re, const double *ca_im) {
+  double vr = (code & 2) ? 1.0 : ca_re[code >> 2];
+  double vi = (code & 2) ? 0.0 : ca_im[code >> 2];
+  if (code & 1) { vr = -vr; vi = -vi; }
+  return cx<double>(vr, vi);
+}
+
 // Stamp every LU slot (A entries summed in emission order, fill slots zero) and return.
+// Four slots per thread at a time, so their chains of dependent loads (slot -> A entry ->
+// contribution range -> contributions) are in flight together; each slot's sum keeps the
+// emission order of sum_entry, so the values are the same bits.
 template <typename T>
 __device__ __forceinline__ void stamp_lu(const DevProg &P, T *lu, const double *ca_re, const double *ca_im) {
-  for (int s = threadIdx.x; s < P.nnz_lu; s += blockDim.x) {
-    int t = P.lu_src[s];
-    lu[s] = t < 0 ? T(0) : sum_entry<T>(P, t, ca_re, ca_im);
+  const int nb = blockDim.x;
+  for (int s0 = threadIdx.x; s0 < P.nnz_lu; s0 += 4 * nb) {
+    int t[4], u[4], ue[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) t[q] = s0 + q * nb < P.nnz_lu ? P.lu_src[s0 + q * nb] : -1;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      u[q] = t[q] >= 0 ? P.a_cptr[t[q]] : 0;
+      ue[q] = t[q] >= 0 ? P.a_cptr[t[q] + 1] : 0;
+    }
+    T acc[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[q] = T(0);
+    bool more = true;
+    while (more) {
+      more = false;
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (u[q] < ue[q]) {
+          acc[q] = acc[q] + contrib_value<T>(P.a_contrib[u[q]], ca_re, ca_im);
+          ++u[q];
+          more = more || u[q] < ue[q];
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (s0 + q * nb < P.nnz_lu) lu[s0 + q * nb] = acc[q];
   }
 }
 
