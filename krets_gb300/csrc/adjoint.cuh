@@ -174,6 +174,8 @@ __device__ __forceinline__ void adj_forward_step(const DevProg &P, const SProg &
 // mode 0: forward pass only (loss), mode 1: loss and gradient, mode 2: gradient only, the
 // forward pass having run on the double-float engine (k_tran_dfd with AdjFwd: per-instance
 // checkpoints and the loss); the last segment is then recomputed from its checkpoint.
+// ck_cb (mode 2, trapezoidal rule): the checkpoints hold the capacitors' companion values
+// (the forward pass ran the direct right-hand-side step) instead of their currents.
 // adj: per element {kind, row position of p, row position of m, row position of branch}
 // cc_ptr/cc_op: per column position, the rhs contributions of C^T lambda: range
 //       [cc_ptr[j], cc_ptr[j+1]) of (dyn index << 1 | neg) entries.
@@ -192,7 +194,8 @@ template <int RK, int RD, int RE>
 __global__ void __launch_bounds__(kAdjThreads, 1)
     k_adjoint_dfd(DevProg P, AdjLay L, const double *values, int n_inst, double h, int n_steps, int method, int K,
                   int out_pos, const int4 *adj, const int *cc_ptr, const int *cc_op, df *ckpt, df *seg, df *hist,
-                  double *loss_out, double *grad_out, int *inst_status, int *queue, int mode, WaveTab wt) {
+                  double *loss_out, double *grad_out, int *inst_status, int *queue, int mode, WaveTab wt,
+                  int ck_cb) {
   constexpr int GF = kAdjThreads, GH = kAdjHalf;
   extern __shared__ __align__(16) char smem[];
   const int tid = threadIdx.x;
@@ -336,11 +339,20 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
         x[k] = ck[k];
         last_seg[k] = ck[k];
       }
-      for (int d = tid; d < P.ncap; d += GF) icap[d] = ck[n + d];
-      gsync<GF>(0);
-      for (int s = last0 + 1; s <= n_steps; ++s) {
-        adj_forward_step<GF, GF>(P, S, lu, x, cdyn, cb, icap, vals, method, s, h, wt, tid, 0);
-        for (int k = tid; k < n; k += GF) last_seg[(size_t)(s - last0) * n + k] = x[k];
+      if (tr && ck_cb) {
+        for (int d = tid; d < P.ncap; d += GF) cb[d] = ck[n + d];
+        gsync<GF>(0);
+        for (int s = last0 + 1; s <= n_steps; ++s) {
+          adj_forward_step<GF, GF, true>(P, S, lu, x, cdyn, cb, icap, vals, method, s, h, wt, tid, 0);
+          for (int k = tid; k < n; k += GF) last_seg[(size_t)(s - last0) * n + k] = x[k];
+        }
+      } else {
+        for (int d = tid; d < P.ncap; d += GF) icap[d] = ck[n + d];
+        gsync<GF>(0);
+        for (int s = last0 + 1; s <= n_steps; ++s) {
+          adj_forward_step<GF, GF>(P, S, lu, x, cdyn, cb, icap, vals, method, s, h, wt, tid, 0);
+          for (int k = tid; k < n; k += GF) last_seg[(size_t)(s - last0) * n + k] = x[k];
+        }
       }
       gsync<GF>(0);
     }
@@ -470,10 +482,10 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
             }
             for (int d = hl; d < P.ncap; d += GH) icap[d] = ck[n + d];
             gsync<GH>(2);
-            if (tr) {  // companion currents of step s0 from the checkpoint's currents
+            if (tr) {  // companion currents of step s0 (the checkpoint's, or from its currents)
               for (int d = hl; d < P.ncap; d += GH) {
                 const int4 dd = S.dyn[d];
-                cb[d] = df_sub(df_mul(cdyn[d], df_sub(df_at(x, dd.y), df_at(x, dd.z))), icap[d]);
+                cb[d] = ck_cb ? icap[d] : df_sub(df_mul(cdyn[d], df_sub(df_at(x, dd.y), df_at(x, dd.z))), icap[d]);
               }
               for (int s = s0 + 1; s <= s1; ++s) {
                 adj_forward_step<GH, GH, true>(P, S, lu, x, cdyn, cb, icap, vals, method, s, h, wt, hl, 2);

@@ -1897,16 +1897,41 @@ krets_status krets_adjoint_tran(krets_circuit *c, int32_t n_inst, const double *
   DevBuf tstf;
   CU(cudaMalloc(&tstf.p, sizeof(int) * n_inst));
   CU(cudaMemsetAsync(tstf.p, 0, sizeof(int) * n_inst, c->stream));
+  // The forward pass takes the transient engine's configuration for this circuit (group
+  // size and place of the factors from the autotuner, whose trial runs start from the
+  // zero operating points in top; the direct right-hand-side step when it applies, whose
+  // checkpoints then hold the capacitors' companion values: ck_cb).
+  DfdLaunch Lf;
+  DfdLay DLf{};
+  df *lu_glob = nullptr;
+  int fgrid = 1, fopts = 0, ck_cb = 0;
+  if (split) {
+    const char *oenv = getenv("KRETS_DFD_OPTS");
+    fopts = oenv ? atoi(oenv) : kDfdDefaultOpts;
+    int G = 128, how = 0;
+    bool lug = false;
+    s = dfd_pick(c, Dtr, (const double *)dv, nullptr, 0, n_inst, h, n_steps, method, 0, queue, fopts, wt,
+                 Probe{nullptr, 0, (const double *)top.p}, G, lug, how);
+    if (s != KRETS_OK) return s;
+    if (!dfd_layout(P, DLf, lug, G, method, fopts)) {
+      G = 128;
+      lug = false;
+      if (!dfd_layout(P, DLf, false, G, method, fopts)) return fail(KRETS_ERR_INVALID_ARGUMENT, "double-float layout does not fit");
+    }
+    s = dfd_config(G, lug, DLf, Lf);
+    if (s != KRETS_OK) return s;
+    fgrid = std::max(1, std::min((n_inst + Lf.W - 1) / Lf.W, Lf.per_sm * device_sm_count()));
+    s = dfd_lu_buffer(c, Lf, fgrid, P, &lu_glob);
+    if (s != KRETS_OK) return s;
+    ck_cb = DLf.lean && method == KRETS_METHOD_TR;
+    CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
+  }
   CU(cudaEventRecord(c->ev[2], c->stream));
   if (split) {
-    DfdLaunch Lf;
-    s = dfd_config(128, false, DL, Lf);
-    if (s != KRETS_OK) return s;
-    const int fgrid = std::max(1, std::min((n_inst + Lf.W - 1) / Lf.W, Lf.per_sm * device_sm_count()));
     const AdjFwd af{(df *)tck.p, K, P.n + P.ncap, H.qinv[out_unknown], (double *)d_loss};
-    Lf.kd<<<fgrid, 128 * Lf.W, Lf.smem, c->stream>>>(P, c->cfg, DL, (const double *)dv, n_inst, h, n_steps, method,
-                                                     0, nullptr, (int *)tstf.p, queue, 0, wt,
-                                                     Probe{nullptr, 0, nullptr}, af, kWholeRun, nullptr);
+    Lf.kd<<<fgrid, Lf.G * Lf.W, Lf.smem, c->stream>>>(P, c->cfg, DLf, (const double *)dv, n_inst, h, n_steps,
+                                                      method, 0, nullptr, (int *)tstf.p, queue, fopts, wt,
+                                                      Probe{nullptr, 0, nullptr}, af, kWholeRun, lu_glob);
     g_launches++;
     CU(cudaGetLastError());
     CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
@@ -1915,7 +1940,7 @@ krets_status krets_adjoint_tran(krets_circuit *c, int32_t n_inst, const double *
     ka<<<grid, kAdjThreads, smem, c->stream>>>(P, AL, (const double *)dv, n_inst, h, n_steps, method, K,
                                                H.qinv[out_unknown], (const int4 *)d_adj, d_ccp, d_cco, (df *)tck.p,
                                                (df *)tseg.p, d_hist, (double *)d_loss, (double *)d_grad,
-                                               (int *)tst.p, queue, split ? 2 : (gradient ? 1 : 0), wt);
+                                               (int *)tst.p, queue, split ? 2 : (gradient ? 1 : 0), wt, ck_cb);
     g_launches++;
     CU(cudaGetLastError());
   }

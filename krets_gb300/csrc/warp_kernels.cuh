@@ -1657,16 +1657,20 @@ __device__ __forceinline__ int dfd_steps(const DevProg &P, const SProg &S, const
 // the companion values a previous call left; on return the companion values).  Every
 // value is formed with the same operations in the same order as dfd_steps with the
 // gather (a row fed by one element takes 0 + v = v exactly), so the results are
-// bit-identical to it.
-template <int G, bool TR>
+// bit-identical to it.  As an adjoint forward pass (ADJ, af.ck set) it writes no
+// waveforms: every K steps the state goes to a checkpoint (x, then the capacitor companion
+// values) and sum_n x_n[out_pos]^2 accumulates in double-float into *af.loss.  (A separate
+// instantiation, so the waveform step keeps its registers.)
+template <int G, bool TR, bool ADJ = false>
 __device__ __forceinline__ int dfd_steps_lean(const DevProg &P, const int4 *lrec, const int *zrow, const int *qinv,
                                               const IlProg &I, df *&x, df *&b, const df *cdyn, df *cb,
                                               const double *vals, double h, int n_steps, int lag, double *out, int gl,
                                               int gid, WaveTab wt, Probe pr, int s_begin, int row_base,
-                                              bool cvt64) {
+                                              bool cvt64, AdjFwd af = AdjFwd{nullptr, 1, 0, 0, nullptr}) {
   const int n_out = pr.n ? pr.n : P.n;
   const int ncap = P.ncap, nlc = P.ncap + P.n_ind, nd = P.ndyn, nz = P.n_zrow;
   int st = 0;
+  df loss{0.f, 0.f};  // adjoint forward pass: lane 0 of the group accumulates
   int pf_d = -1;  // first tabulated source of this thread: next value loaded a step ahead
   size_t pf_base = 0;
   double pf_val = 0.0;
@@ -1684,6 +1688,11 @@ __device__ __forceinline__ int dfd_steps_lean(const DevProg &P, const int4 *lrec
       cb[d] = df_sub(df_mul(cdyn[d], df_sub(x[r.x], x[r.y])), cb[d]);
     }
   for (int s = s_begin; s <= n_steps; ++s) {
+    if (ADJ && (s - 1) % af.K == 0) {  // x final (the last solve level synced); cb: this thread's
+      df *ck = af.ck + (size_t)((s - 1) / af.K) * af.ck_words;
+      for (int k = gl; k < P.n; k += G) ck[k] = x[k];
+      for (int d = gl; d < ncap; d += G) ck[P.n + d] = cb[d];
+    }
     for (int d = gl; d < ncap; d += G) {
       const int4 r = lrec[d];
       const df vprev = df_sub(x[r.x], x[r.y]);
@@ -1728,14 +1737,17 @@ __device__ __forceinline__ int dfd_steps_lean(const DevProg &P, const int4 *lrec
     for (int i = gl; i < nz; i += G) b[zrow[i]] = df{0.f, 0.f};
     gsync<G>(gid);  // b assembled (and every read of x done)
     il_solve<G>(I, b, gl, gid);
-    double *row = out + (size_t)(s - row_base) * n_out;
-    if (cvt64) {  // conversions and the add on the FP64 pipe (same value as df_out)
+    if (ADJ) {
+      if (gl == 0) loss = df_fma(b[af.out_pos], b[af.out_pos], loss);
+    } else if (cvt64) {
+      double *row = out + (size_t)(s - row_base) * n_out;  // conversions and the add on the FP64 pipe (same value as df_out)
       for (int j = gl; j < n_out; j += G) {
         const double v = df_to_double(b[qinv[pr.n ? pr.idx[j] : j]]);
         if ((__double2hiint(v) & 0x7ff00000) == 0x7ff00000) st |= KS_NONFINITE;
         __stcs(row + j, v);
       }
     } else {
+      double *row = out + (size_t)(s - row_base) * n_out;
       for (int j = gl; j < n_out; j += G) __stcs(row + j, df_out(b[qinv[pr.n ? pr.idx[j] : j]], st));
     }
     // no barrier: the next step reads b (final since the last solve level) and writes the
@@ -1744,6 +1756,7 @@ __device__ __forceinline__ int dfd_steps_lean(const DevProg &P, const int4 *lrec
     x = b;
     b = t;
   }
+  if (ADJ && gl == 0) *af.loss = df_to_double(loss);
   return st;
 }
 
@@ -1770,7 +1783,7 @@ struct Span {
 // so up to 14 instances share an SM (each step's critical path is a chain of level
 // barriers; more instances per SM hide it, and fewer waves of instances are needed).
 template <int G, bool LUG = false>
-__global__ void __launch_bounds__(896, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay L, const double *values, int n_inst,
+__global__ void __launch_bounds__(896) __maxnreg__(LUG ? 64 : 72) k_tran_dfd(DevProg P, KCfg cfg, DfdLay L, const double *values, int n_inst,
                                                      double h, int n_steps, int method, int lag, double *x_out,
                                                      int *inst_status, int *queue, int opts, WaveTab wt, Probe pr,
                                                      AdjFwd af, Span sp, df *lu_glob) {
@@ -1844,10 +1857,13 @@ __global__ void __launch_bounds__(896, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
     while (unar < S.nulev && S.ulev_ptr[unar + 1] - S.ulev_ptr[unar] <= 64) ++unar;
   }
   const bool int_cvt = (opts & 2) != 0;
-  // bit 2: trapezoidal capacitor history carried as the companion current (no adjoint pass)
+  // bit 2: trapezoidal capacitor history carried as the companion current (the gather
+  // step keeps currents in an adjoint forward pass: its checkpoints hold currents)
   const bool cbrec = (opts & 4) != 0 && method == KRETS_METHOD_TR && !af.ck;
-  // the direct right-hand-side step runs TR with companion currents, or BE
-  const bool lean_ok = lean && !af.ck && (cbrec || method == KRETS_METHOD_BE);
+  // the direct right-hand-side step runs TR with companion currents (its adjoint
+  // checkpoints hold companion values), or BE
+  const bool tr_lean = (opts & 4) != 0 && method == KRETS_METHOD_TR;
+  const bool lean_ok = lean && (tr_lean || method == KRETS_METHOD_BE);
   char *base = smem + L.sprog_bytes + (size_t)gid * L.bytes;
   // global-memory factors: per group the CSR factors, then (interleaved solves) their
   // interleaved copy
@@ -1906,12 +1922,21 @@ __global__ void __launch_bounds__(896, 1) k_tran_dfd(DevProg P, KCfg cfg, DfdLay
     df *xfin = x;  // where the last solution is
     if (!fatal && lean) {
       df *xs = x, *bs = cb;
-      if (cbrec)
+      const bool c64 = (opts & 16) != 0;
+      if (a.ck) {
+        if (tr_lean)
+          st |= dfd_steps_lean<G, true, true>(P, lrec, zrow, qinv, I, xs, bs, cdyn, icap, vals, h, n_steps, lag, out,
+                                              gl, gid, wt, pr, sp.s_begin, sp.row_base, c64, a);
+        else
+          st |= dfd_steps_lean<G, false, true>(P, lrec, zrow, qinv, I, xs, bs, cdyn, icap, vals, h, n_steps, lag,
+                                               out, gl, gid, wt, pr, sp.s_begin, sp.row_base, c64, a);
+      } else if (tr_lean) {
         st |= dfd_steps_lean<G, true>(P, lrec, zrow, qinv, I, xs, bs, cdyn, icap, vals, h, n_steps, lag, out, gl,
-                                      gid, wt, pr, sp.s_begin, sp.row_base, (opts & 16) != 0);
-      else
+                                      gid, wt, pr, sp.s_begin, sp.row_base, c64);
+      } else {
         st |= dfd_steps_lean<G, false>(P, lrec, zrow, qinv, I, xs, bs, cdyn, icap, vals, h, n_steps, lag, out, gl,
-                                       gid, wt, pr, sp.s_begin, sp.row_base, (opts & 16) != 0);
+                                       gid, wt, pr, sp.s_begin, sp.row_base, c64);
+      }
       xfin = xs;
     } else if (!fatal) {
       if (cbrec)
