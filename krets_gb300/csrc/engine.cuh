@@ -308,6 +308,25 @@ __device__ __forceinline__ double block_max(double v, double *red) {
   return r;
 }
 
+// The same over floats (red: the same 32-double scratch).
+__device__ __forceinline__ float block_maxf(float v, double *red) {
+  float *rf = reinterpret_cast<float *>(red);
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) rf[w] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float t = threadIdx.x < (blockDim.x >> 5) ? rf[threadIdx.x] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) t = fmaxf(t, __shfl_xor_sync(0xffffffffu, t, o));
+    if (threadIdx.x == 0) rf[32] = t;
+  }
+  __syncthreads();
+  const float r = rf[32];
+  __syncthreads();
+  return r;
+}
+
 // ------------------------------------------------------------------ stamping
 // Sum of one A entry's contributions (emission order).
 template <typename T>

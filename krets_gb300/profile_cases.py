@@ -1,7 +1,7 @@
 """Small cases of the main kernels for profiler captures (one launch each, a few GB on
 the device at most), run as
 
-    python -m krets_gb300.profile_cases tran|multi|adjoint|kernels|op
+    python -m krets_gb300.profile_cases tran|multi|adjoint|kernels|op|ac|dense
 
   tran     k_tran_dfd: 2048 instances of the 200-section RLC ladder, TR 1 ps, 200 steps,
            the configuration the autotuner picks for it on GB300 (64 threads per instance,
@@ -16,6 +16,8 @@ the device at most), run as
            mixed, double-float; nonlinear FP64 and mixed), adaptive transient, 64 small
            uneven netlists
   op       k_op: the plain operating point of the 1001-unknown ladder, three times
+  ac       k_ac_batch<1>: the 4096-point AC sweep of the 500-section RC ladder (complex64
+           factor, complex128 refinement), twice
   dense    k_multi_tran set-up (operating point and transient factorisations) and 100 BE
            steps of one circuit whose LU is a dense block of m - 1 rows, m = 96 .. 352
 """
@@ -118,6 +120,19 @@ def op():
     return g.timing()
 
 
+def ac():
+    from .analyses import AcAnalysis, Decade, generate_frequencies
+    from .generators import rc_ladder_ac
+    from .table import element_table
+    c = rc_ladder_ac()
+    g = _lib.GpuCircuit(element_table(c), c.size)
+    f = np.array(generate_frequencies(AcAnalysis(Decade(455), 1.0, 1e9)))
+    out = _lib.DeviceArray((1, len(f), c.size, 2))
+    for _ in range(2):
+        g.batch_ac(None, f, precision=_lib.PREC_MIXED, out=out)
+    return g.timing()
+
+
 def dense():
     from .generators import dense_block_table
     rows = []
@@ -139,7 +154,7 @@ def dense():
     return rows[-1][2], rows[-1][2]
 
 
-CASES = {"tran": tran, "multi": multi, "adjoint": adjoint, "kernels": kernels, "op": op, "dense": dense}
+CASES = {"tran": tran, "multi": multi, "adjoint": adjoint, "kernels": kernels, "op": op, "ac": ac, "dense": dense}
 
 if __name__ == "__main__":
     k, c = CASES[sys.argv[1]]()
