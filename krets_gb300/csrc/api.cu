@@ -167,6 +167,9 @@ struct krets_circuit {
   // global-memory factors of the double-float engine's groups (k_tran_dfd<G, true>)
   void *lug = nullptr;
   size_t lug_bytes = 0;
+  // per-CTA coefficient cache of the batched AC sweep (k_ac_batch<1>)
+  void *accache = nullptr;
+  size_t accache_bytes = 0;
   // staged host output of the double-float engine: two staging buffers, a copy stream
   void *stage = nullptr;
   size_t stage_bytes = 0;
@@ -175,6 +178,7 @@ struct krets_circuit {
 
   ~krets_circuit() {
     if (lug) cudaFree(lug);
+    if (accache) cudaFree(accache);
     if (stage) cudaFree(stage);
     for (auto &e : sev)
       if (e) cudaEventDestroy(e);
@@ -1070,9 +1074,22 @@ krets_status krets_batch_ac(krets_circuit *c, int32_t n_inst, const double *valu
   if (s) return s;
   int *queue = c->d_small + 8;
   CU(cudaMemsetAsync(queue, 0, sizeof(int), c->stream));
+  // per-CTA cache of the frequency-independent coefficients (complex64 path), kept in the
+  // handle across calls
+  if (mixed) {
+    const size_t bytes = sizeof(double) * (size_t)grid * (2 * (size_t)Dac->view.n_coef + Dac->view.ne);
+    if (bytes > c->accache_bytes) {
+      if (c->accache) cudaFree(c->accache);
+      c->accache = nullptr;
+      c->accache_bytes = 0;
+      CU(cudaMalloc(&c->accache, bytes));
+      c->accache_bytes = bytes;
+    }
+  }
   CU(cudaEventRecord(c->ev[2], c->stream));
   kern<<<grid, threads, smem, c->stream>>>(Dac->view, L, gws, (const double *)dv, (const double *)top.p, n_inst,
-                                           (const double *)df, n_freq, (double *)dx, d_item_st, queue);
+                                           (const double *)df, n_freq, (double *)dx, d_item_st, queue,
+                                           mixed ? (double *)c->accache : nullptr);
   g_launches++;
   CU(cudaGetLastError());
   CU(cudaEventRecord(c->ev[3], c->stream));

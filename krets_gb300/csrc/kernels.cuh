@@ -765,9 +765,14 @@ __global__ void k_tran_batch(DevProg P, KCfg cfg, Lay L, char *gws, const double
 // ============================================================== k_ac_batch
 // Work item = (instance, frequency).  op_x: operating point per instance, original
 // numbering (used by the diode's small-signal conductance).
+// ccache (MIXED): per CTA 2 n_coef + ne doubles.  A CTA keeps there the coefficients of
+// its current instance that do not depend on the frequency — the real parts (1/R, diode
+// conductances), the C and L values, the rhs coefficients — and forms only
+// ca_im = 2 pi f value per point, with the operations of elem_coefs (the same bits).
 template <int MIXED>
 __global__ void k_ac_batch(DevProg P, Lay L, char *gws, const double *values, const double *op_x, int n_inst,
-                           const double *freqs, int n_freq, double *x_out, int *item_status, int *queue) {
+                           const double *freqs, int n_freq, double *x_out, int *item_status, int *queue,
+                           double *ccache) {
   extern __shared__ __align__(16) char smem[];
   char *base = gws ? gws + (size_t)blockIdx.x * L.bytes : smem;
   using C64 = cx<double>;
@@ -787,6 +792,10 @@ __global__ void k_ac_batch(DevProg P, Lay L, char *gws, const double *values, co
   C32 *lu32 = reinterpret_cast<C32 *>(base + L.off[2]);
   C64 *lu64 = reinterpret_cast<C64 *>(base + L.off[2]);
   const int total = n_inst * n_freq;
+  const bool cached = MIXED && ccache;
+  double *cre = cached ? ccache + (size_t)blockIdx.x * (2 * (size_t)P.n_coef + P.ne) : nullptr;
+  double *ccl = cre + P.n_coef, *ccb = ccl + P.n_coef;
+  if (threadIdx.x == 0) item[1] = -1;  // instance whose coefficients the cache holds
   while (true) {
     if (threadIdx.x == 0) *item = atomicAdd(queue, 1);
     __syncthreads();
@@ -794,21 +803,59 @@ __global__ void k_ac_batch(DevProg P, Lay L, char *gws, const double *values, co
     if (it_idx >= total) break;
     int inst = it_idx / n_freq, fi = it_idx % n_freq;
     if (threadIdx.x == 0) *status = 0;
-    if (!MIXED)
-      for (int e = threadIdx.x; e < P.ne; e += blockDim.x)
-        vals[e] = values ? values[(size_t)inst * P.ne + e] : P.el[e].value;
-    for (int k = threadIdx.x; k < P.n; k += blockDim.x) opx[k] = op_x[(size_t)inst * P.n + P.q[k]];
+    const double *ca_src = ca_re, *cb_src = cb;
+    if (cached) {
+      if (inst != item[1]) {
+        for (int k = threadIdx.x; k < P.n; k += blockDim.x) opx[k] = op_x[(size_t)inst * P.n + P.q[k]];
+        if (threadIdx.x == 0) item[2] = 0;
+        __syncthreads();
+        PassCtx c0{};
+        c0.mode = 1;
+        c0.guess = opx;
+        c0.guess_empty = false;
+        const double *iv = values ? values + (size_t)inst * P.ne : nullptr;
+        int err = 0;
+        for (int e = threadIdx.x; e < P.ne; e += blockDim.x) {
+          const krets_element &E = P.el[e];
+          const double val = iv ? iv[e] : E.value;
+          double ar, ai, bb, x0, x1;
+          elem_coefs(E, e, P.el_pos[e], val, c0, ar, ai, bb, x0, x1, err);
+          cre[e] = ar;
+          ccl[e] = (E.kind == KRETS_ELEM_C || E.kind == KRETS_ELEM_L) ? val : 0.0;
+          ccb[e] = bb;
+          const int xs = P.xslot[e];
+          if (xs >= 0) {
+            cre[xs] = x0;
+            cre[xs + 1] = x1;
+            ccl[xs] = ccl[xs + 1] = 0.0;
+          }
+        }
+        if (err) atomicOr(&item[2], err);
+        __syncthreads();
+        if (threadIdx.x == 0) item[1] = inst;  // read again only after the next item's barrier
+      }
+      if (threadIdx.x == 0) *status |= item[2];
+      const double w2f = 2.0 * kPiD * freqs[fi];
+      for (int e = threadIdx.x; e < P.n_coef; e += blockDim.x) ca_im[e] = w2f * ccl[e];
+      ca_src = cre;
+      cb_src = ccb;
+    } else {
+      if (!MIXED)
+        for (int e = threadIdx.x; e < P.ne; e += blockDim.x)
+          vals[e] = values ? values[(size_t)inst * P.ne + e] : P.el[e].value;
+      for (int k = threadIdx.x; k < P.n; k += blockDim.x) opx[k] = op_x[(size_t)inst * P.n + P.q[k]];
+      __syncthreads();
+      PassCtx c{};
+      c.mode = 1;
+      c.freq = freqs[fi];
+      c.guess = opx;
+      c.guess_empty = false;
+      coef_pass(P, MIXED ? (values ? values + (size_t)inst * P.ne : nullptr) : vals, c, ca_re, ca_im, cb, status);
+    }
     __syncthreads();
-    PassCtx c{};
-    c.mode = 1;
-    c.freq = freqs[fi];
-    c.guess = opx;
-    c.guess_empty = false;
-    coef_pass(P, MIXED ? (values ? values + (size_t)inst * P.ne : nullptr) : vals, c, ca_re, ca_im, cb, status);
-    __syncthreads();
-    for (int k = threadIdx.x; k < P.n; k += blockDim.x) b[k] = C64(sum_rhs(P, k, cb), 0.0);
+    for (int k = threadIdx.x; k < P.n; k += blockDim.x) b[k] = C64(sum_rhs(P, k, cb_src), 0.0);
     if (MIXED) {
-      for (int t = threadIdx.x; t < P.nnz_a; t += blockDim.x) a128[t] = sum_entry<C64>(P, t, ca_re, ca_im);
+      for (int t = threadIdx.x; t < P.nnz_a; t += blockDim.x) a128[t] = sum_entry<C64>(P, t, ca_src, ca_im);
       __syncthreads();
       for (int s = threadIdx.x; s < P.nnz_lu; s += blockDim.x) {
         int t = P.lu_src[s];
