@@ -167,6 +167,41 @@ def test_batched_ac_sweep_matches_oracle(oracle_lib, precision):
         assert rel_err(z[i], ref[i], mask) < TOL, (i, f[i])
 
 
+AC_DIODE = """* diode clamp biased at its operating point, AC source
+V1 in 0 dc 0.7 AC 1
+R1 in a 100
+D1 a 0 DMOD
+C1 a 0 10n
+R2 a b 1000
+C2 b 0 1n
+.model DMOD D (is=1e-12)
+"""
+
+
+@pytest.mark.parametrize("precision", [_lib.PREC_FP64, _lib.PREC_MIXED])
+@pytest.mark.parametrize("case", ["ladder", "diode"])
+def test_batched_ac_monte_carlo_instances(oracle_lib, precision, case):
+    """Several parameter sets in one batched sweep: the work items of the instances
+    interleave on the CTAs, which keep each instance's frequency-independent coefficients
+    (conductances, C and L values, the diode's small-signal conductance at that
+    instance's operating point) between points.  Every (instance, point) against the
+    oracle's sweep with that instance's values."""
+    from krets_gb300.analyses import AcAnalysis, Decade
+    c = rc_ladder_ac(60, seed=5) if case == "ladder" else parse_circuit_description(AC_DIODE)
+    t = element_table(c)
+    f = np.array(generate_frequencies(AcAnalysis(Decade(7), 10.0, 1e8)))
+    vals = monte_carlo_values(c, 12, seed=8)
+    g = _lib.GpuCircuit(t, c.size)
+    z = g.batch_ac(vals, f, precision=precision)
+    mask = is_current_mask(c)
+    for i in range(len(vals)):
+        ti = t.copy()
+        ti["value"] = vals[i]
+        ref = oracle_lib.ac(ti, c.size, f)
+        for k in range(len(f)):
+            assert rel_err(z[i, k], ref[k], mask) < TOL, (i, k, f[k])
+
+
 def test_batch_op_monte_carlo(oracle_lib):
     c = config1_circuit()
     t = element_table(c)
