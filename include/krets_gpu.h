@@ -190,7 +190,9 @@ krets_status krets_batch_tran_probe(krets_circuit *c, int32_t n_inst, const doub
 /* Batched AC over frequency points of one instance (values NULL) or of several
  * instances: each work item is one (instance, frequency) complex system.
  * precision: FP64 = complex128 factor; MIXED = complex64 factor + complex128 refinement.
- * x_out: [n_inst][n_freq][n][2]; frequencies must be > 0. */
+ * x_out: [n_inst][n_freq][n][2]; frequencies must be > 0.  MIXED keeps a device buffer in
+ * the handle (per CTA of the launch: the frequency-independent coefficients of the
+ * instance it is working on), reused by later calls and freed with the handle. */
 krets_status krets_batch_ac(krets_circuit *c, int32_t n_inst, const double *values, const double *freqs,
                             int32_t n_freq, int32_t precision, double *x_out, int32_t *item_status);
 
