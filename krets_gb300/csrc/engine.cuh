@@ -45,6 +45,14 @@ template <typename R> __device__ __forceinline__ cx<R> operator/(cx<R> a, cx<R> 
   return {(a.re * r + a.im) / d, (a.im * r - a.re) / d};
 }
 
+// 1 / x, correctly rounded: the reciprocal instructions (rcp.rn) round to nearest as the
+// division 1.0 / x does, so the value is the same bits with fewer FP64 instructions (the
+// FP64 pipe issues at 1/64 of the FP32 rate on this GPU).  Complex values divide.
+__device__ __forceinline__ double recip(double x) { return __drcp_rn(x); }
+__device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
+template <typename R>
+__device__ __forceinline__ cx<R> recip(cx<R> x) { return cx<R>(R(1)) / x; }
+
 template <typename T> struct scal;
 template <> struct scal<double> {
   using real = double;
@@ -226,7 +234,7 @@ __device__ __forceinline__ void elem_coefs(const krets_element &E, int e, int4 p
   x1 = 0.0;
   switch (E.kind) {
     case KRETS_ELEM_R:
-      ca_re = (E.flags & KRETS_FLAG_G2) ? val : 1.0 / val;
+      ca_re = (E.flags & KRETS_FLAG_G2) ? val : recip(val);
       break;
     case KRETS_ELEM_C:
       if (c.mode == 1) {
@@ -432,7 +440,7 @@ __device__ __forceinline__ void factor_v(const FacView &F, T *lu, int *status) {
       T dk = lu[dg];
       if (!(scal<T>::mag(dk) > 0)) bad |= KS_SINGULAR;
       else if (!scal<T>::finite(dk)) bad |= KS_NONFINITE;
-      lu[dg] = T(1) / dk;
+      lu[dg] = recip(dk);
     }
     __syncthreads();
   }

@@ -158,7 +158,7 @@ __device__ int w_factor(const DevProg &P, T *lu, int lane) {
   }
   for (int k = lane; k < P.n; k += 32) {
     const int s = P.lu_diag[k];
-    lu[s] = T(1) / lu[s];
+    lu[s] = recip(lu[s]);
   }
   __syncwarp();
   return (int)__reduce_or_sync(kFull, (unsigned)bad);
@@ -175,7 +175,7 @@ __device__ __forceinline__ int w_coef_pass(const DevProg &P, const double *value
     const double val = values ? values[e] : E.value;
     double c = 0.0;
     switch (E.kind) {
-      case KRETS_ELEM_R: c = (E.flags & KRETS_FLAG_G2) ? val : 1.0 / val; break;
+      case KRETS_ELEM_R: c = (E.flags & KRETS_FLAG_G2) ? val : recip(val); break;
       case KRETS_ELEM_C: c = method == KRETS_METHOD_TR ? 2.0 * val / h : val / h; break;
       case KRETS_ELEM_L: c = method == KRETS_METHOD_TR ? 2.0 * val / h : val / h; break;
       case KRETS_ELEM_V:
@@ -674,7 +674,7 @@ __device__ int g_coef_pass(const DevProg &P, const double *values, double h, int
     const double val = values ? values[e] : E.value;
     double c = 0.0;
     switch (E.kind) {
-      case KRETS_ELEM_R: c = (E.flags & KRETS_FLAG_G2) ? val : 1.0 / val; break;
+      case KRETS_ELEM_R: c = (E.flags & KRETS_FLAG_G2) ? val : recip(val); break;
       case KRETS_ELEM_C: c = method == KRETS_METHOD_TR ? 2.0 * val / h : val / h; break;
       case KRETS_ELEM_L: c = method == KRETS_METHOD_TR ? 2.0 * val / h : val / h; break;
       case KRETS_ELEM_V:
@@ -830,7 +830,7 @@ __device__ int g_factor64_warp(const DevProg &P, double *lu, int gl, int gid, do
         const double d = lu[dk];
         if (!(fabs(d) > 0)) bad |= KS_SINGULAR;
         else if (!isfinite(d)) bad |= KS_NONFINITE;
-        lu[dk] = 1.0 / d;
+        lu[dk] = recip(d);
       }
     }
     gsync<G>(gid);
@@ -891,7 +891,7 @@ __device__ int g_factor64_warp(const DevProg &P, double *lu, int gl, int gid, do
   }
   for (int k = (m ? t0 : P.n) + gl; k < P.n; k += G) {  // pivots of the dense block
     const int sl = P.lu_diag[k];
-    lu[sl] = 1.0 / lu[sl];
+    lu[sl] = recip(lu[sl]);
   }
   gsync<G>(gid);
   return bad;
@@ -959,7 +959,7 @@ __device__ int g_factor64_merge(const DevProg &P, double *lu, int gl, int gid) {
   }
   for (int k = gl; k < P.n; k += G) {
     const int sl = P.lu_diag[k];
-    lu[sl] = 1.0 / lu[sl];
+    lu[sl] = recip(lu[sl]);
   }
   gsync<G>(gid);
   return bad;
@@ -989,7 +989,7 @@ __device__ int g_factor64(const DevProg &P, double *lu, int gl, int gid) {
   }
   for (int k = gl; k < P.n; k += G) {
     const int sl = P.lu_diag[k];
-    lu[sl] = 1.0 / lu[sl];
+    lu[sl] = recip(lu[sl]);
   }
   gsync<G>(gid);
   return bad;
