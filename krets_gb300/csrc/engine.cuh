@@ -401,11 +401,41 @@ __device__ __forceinline__ FacView fac_view(const DevProg &P) {
 // is a chain of about ten instructions on a pipe that issues at 1/64 of the FP32 rate,
 // and a factorisation's deepest rows run one pivot after another.  Rows of one level read
 // only the diagonals of earlier levels, so a row inverts its own pivot when it finishes.
+// Levels with at most one row per warp (the deepest ones) take a warp per row: the
+// pivots still run one after another, but a pivot's updates are spread over the lanes, so
+// they cost one FP64 instruction instead of one each (a single thread issues each of them
+// on a pipe that takes 64 cycles per warp instruction).  Same operations, same bits.
 template <typename T>
 __device__ __forceinline__ void factor_v(const FacView &F, T *lu, int *status) {
   int bad = 0;
+  const int nwarp = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int l = 0; l < F.nlev; ++l) {
     int r0 = F.lev_ptr[l], r1 = F.lev_ptr[l + 1];
+    if (r1 - r0 <= nwarp) {
+      if (warp < r1 - r0) {
+        const int k = F.lev_rows[r0 + warp];
+        for (int pi = F.piv_ptr[k]; pi < F.piv_ptr[k + 1]; ++pi) {
+          const int4 pv = F.piv[pi];
+          const T l_kj = lu[pv.x] * lu[F.lu_diag[pv.y]];
+          __syncwarp();  // every lane has read the entry before it is overwritten
+          for (int u = pv.z + lane; u < pv.w; u += 32) {
+            const int2 d = F.upd[u];
+            lu[d.x] = lu[d.x] - l_kj * lu[d.y];
+          }
+          if (lane == 0) lu[pv.x] = l_kj;
+          __syncwarp();  // the row's new values before the next pivot reads them
+        }
+        if (lane == 0) {
+          const int dg = F.lu_diag[k];
+          T dk = lu[dg];
+          if (!(scal<T>::mag(dk) > 0)) bad |= KS_SINGULAR;
+          else if (!scal<T>::finite(dk)) bad |= KS_NONFINITE;
+          lu[dg] = recip(dk);
+        }
+      }
+      __syncthreads();
+      continue;
+    }
     for (int t = r0 + threadIdx.x; t < r1; t += blockDim.x) {
       int k = F.lev_rows[t];
       // A row's pivots run one after another.  What a pivot needs besides its own entry —
