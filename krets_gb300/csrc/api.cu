@@ -2275,24 +2275,26 @@ krets_status krets_multi_create(int32_t n_circuits, const krets_element *elems, 
           return fail(KRETS_ERR_INVALID_ARGUMENT, "circuit " + std::to_string(c) + ": unknown index out of range");
     }
   }
+  // f(j) for j = 0 .. count-1 on all host threads (a shared counter hands out the jobs)
+  auto parallel_for = [](int count, const auto &f) {
+    std::atomic<int> next{0};
+    const int nt = std::max(1, std::min({(int)std::thread::hardware_concurrency(), 64, count}));
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&]() {
+        for (int j; (j = next.fetch_add(1)) < count;) f(j);
+      });
+    for (auto &t : th) t.join();
+  };
   // host symbolic pass of every circuit (DC and TRAN programs), on all host threads
   std::vector<Program> progs(2 * (size_t)N);
   std::vector<int> pst(2 * (size_t)N, 0);
   std::vector<std::string> pmsg(2 * (size_t)N);
-  {
-    std::atomic<int> next{0};
-    const int nt = std::max(1, std::min((int)std::thread::hardware_concurrency(), 64));
-    std::vector<std::thread> th;
-    for (int t = 0; t < nt; ++t)
-      th.emplace_back([&]() {
-        for (int j; (j = next.fetch_add(1)) < 2 * N;) {
-          const int c = j / 2, mode = (j & 1) ? MODE_TRAN : MODE_DC;
-          pst[j] = build_program(elems + m->el_off[c], m->ne[c], m->n[c], mode, method, h, 0.0, -1, progs[j], pmsg[j],
-                                 false, true);
-        }
-      });
-    for (auto &t : th) t.join();
-  }
+  parallel_for(2 * N, [&](int j) {
+    const int c = j / 2, mode = (j & 1) ? MODE_TRAN : MODE_DC;
+    pst[j] = build_program(elems + m->el_off[c], m->ne[c], m->n[c], mode, method, h, 0.0, -1, progs[j], pmsg[j],
+                           false, true);
+  });
   for (int j = 0; j < 2 * N; ++j) {
     if (pst[j] != KRETS_OK) return fail(pst[j], "circuit " + std::to_string(j / 2) + ": " + pmsg[j]);
     bool nonlinear = false;
@@ -2309,22 +2311,22 @@ krets_status krets_multi_create(int32_t n_circuits, const krets_element *elems, 
   const long long ne_total = m->el_off[N];
   CU(cudaMalloc(&m->d_el, sizeof(krets_element) * std::max(1ll, ne_total)));
   CU(cudaMemcpy(m->d_el, elems, sizeof(krets_element) * ne_total, cudaMemcpyHostToDevice));
+  // The image of all programs (GBs for a large batch) is built on all host threads; its
+  // staging copy is not zeroed first, since no kernel reads the padding between arrays.
   std::vector<ProgramImage> X(2 * (size_t)N);
   std::vector<size_t> off(2 * (size_t)N + 1, 0);
-  for (int j = 0; j < 2 * N; ++j) {
-    image_extras(progs[j], X[j]);
-    off[j + 1] = off[j] + program_bytes(progs[j], X[j]);
-  }
+  parallel_for(2 * N, [&](int j) { image_extras(progs[j], X[j]); });
+  for (int j = 0; j < 2 * N; ++j) off[j + 1] = off[j] + program_bytes(progs[j], X[j]);
   CU(cudaMalloc(&m->d_image, off[2 * N]));
   std::vector<DevProg> views(2 * (size_t)N);
   {
-    std::vector<char> staging(off[2 * N], 0);
-    for (int j = 0; j < 2 * N; ++j) {
+    std::unique_ptr<char[]> staging(new char[std::max<size_t>(off[2 * N], 1)]);
+    parallel_for(2 * N, [&](int j) {
       const int c = j / 2;
       place_program(progs[j], X[j], elems + m->el_off[c], m->d_el + m->el_off[c], (char *)m->d_image + off[j],
-                    staging.data() + off[j], views[j]);
-    }
-    CU(cudaMemcpy(m->d_image, staging.data(), off[2 * N], cudaMemcpyHostToDevice));
+                    staging.get() + off[j], views[j]);
+    });
+    CU(cudaMemcpy(m->d_image, staging.get(), off[2 * N], cudaMemcpyHostToDevice));
   }
   CU(cudaMalloc(&m->d_views, sizeof(DevProg) * views.size()));
   CU(cudaMemcpy(m->d_views, views.data(), sizeof(DevProg) * views.size(), cudaMemcpyHostToDevice));
