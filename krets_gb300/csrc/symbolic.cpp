@@ -328,7 +328,7 @@ int gp_factor(int n, const std::vector<int> &ap, const std::vector<int> &ai, con
     std::vector<int> piv_row(c), orig(c), where(c);
     std::iota(orig.begin(), orig.end(), 0);
     std::iota(where.begin(), where.end(), 0);
-    std::vector<T> lcol(c);
+    std::vector<T> L4((size_t)4 * c, T(0));  // the multipliers of the current group of four pivots
     for (int j = 0; j < c; ++j) {
       const int k = kd + j, col = q[k];
       T *cj = S.data() + (size_t)j * c;
@@ -347,17 +347,60 @@ int gp_factor(int n, const std::vector<int> &ap, const std::vector<int> &ai, con
       F.pinv[R[orig[ip]]] = k;
       if (ip != j) {
         for (int jj = j; jj < c; ++jj) std::swap(S[(size_t)jj * c + ip], S[(size_t)jj * c + j]);
+        for (int t = 0; t < (j & 3); ++t)  // the group's earlier multipliers follow their rows
+          std::swap(L4[(size_t)t * c + ip], L4[(size_t)t * c + j]);
         std::swap(orig[ip], orig[j]);
         where[orig[ip]] = ip;
         where[orig[j]] = j;
       }
-      for (int i = j + 1; i < c; ++i) lcol[i] = cj[i] / piv;
-      const T *__restrict__ lc = lcol.data();
-      for (int jj = j + 1; jj < c; ++jj) {
+      T *__restrict__ lc = L4.data() + (size_t)(j & 3) * c;
+      for (int i = j + 1; i < c; ++i) lc[i] = cj[i] / piv;
+      // Columns inside the current group of four are updated at once (their next pivot
+      // is chosen from them); the columns after the group take the group's four updates
+      // in one pass when the group is complete (or the block ends), in pivot order with
+      // the same operations per element, so the values are those of one update at a time
+      // (an update whose multiplier u is zero is skipped, as there).
+      const int g0 = j & ~3, g1 = std::min(g0 + 4, c);
+      for (int jj = j + 1; jj < g1; ++jj) {
         T *__restrict__ cc = S.data() + (size_t)jj * c;
         const T u = cc[j];
         if (u == T(0)) continue;
         for (int i = j + 1; i < c; ++i) cc[i] -= lc[i] * u;
+      }
+      if (j + 1 == g1) {  // the group's pivots g0 .. j are known: update the columns after it
+        const int np = j + 1 - g0;
+        for (int jj = g1; jj < c; ++jj) {
+          T *__restrict__ cc = S.data() + (size_t)jj * c;
+          T u[4];
+          bool all = true;
+          for (int t = 0; t < np; ++t) {  // the pivot rows' values after the earlier pivots
+            const int pr = g0 + t;
+            T v = cc[pr];
+            for (int t2 = 0; t2 < t; ++t2)
+              if (u[t2] != T(0)) v -= L4[(size_t)t2 * c + pr] * u[t2];
+            u[t] = v;
+            all = all && v != T(0);
+          }
+          if (all && np == 4) {
+            const T *__restrict__ l0 = L4.data(), *__restrict__ l1 = l0 + c, *__restrict__ l2 = l1 + c,
+                                  *__restrict__ l3 = l2 + c;
+            for (int t = 1; t < 4; ++t) cc[g0 + t] = u[t];
+            for (int i = g1; i < c; ++i) {
+              T x = cc[i];
+              x -= l0[i] * u[0];
+              x -= l1[i] * u[1];
+              x -= l2[i] * u[2];
+              x -= l3[i] * u[3];
+              cc[i] = x;
+            }
+          } else {
+            for (int t = 0; t < np; ++t) {
+              if (u[t] == T(0)) continue;
+              const T *__restrict__ lt = L4.data() + (size_t)t * c;
+              for (int i = g0 + t + 1; i < c; ++i) cc[i] -= lt[i] * u[t];
+            }
+          }
+        }
       }
     }
     // patterns: U column k = the sparse pivots it reaches, every earlier block pivot and
