@@ -402,9 +402,10 @@ __device__ __forceinline__ FacView fac_view(const DevProg &P) {
 // and a factorisation's deepest rows run one pivot after another.  Rows of one level read
 // only the diagonals of earlier levels, so a row inverts its own pivot when it finishes.
 // Levels with at most one row per warp (the deepest ones) take a warp per row: the
-// pivots still run one after another, but a pivot's updates are spread over the lanes, so
-// they cost one FP64 instruction instead of one each (a single thread issues each of them
-// on a pipe that takes 64 cycles per warp instruction).  Same operations, same bits.
+// pivots still run one after another, but a pivot's updates are spread over the lanes
+// (one warp instruction for all of them instead of one each on a single thread).  The
+// operations are the same (FP64: the same bits; the compiler may contract a complex
+// product differently, a last-bit difference).
 template <typename T>
 __device__ __forceinline__ void factor_v(const FacView &F, T *lu, int *status) {
   int bad = 0;
