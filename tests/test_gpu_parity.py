@@ -140,6 +140,20 @@ def test_nonlinear_transient_newton(oracle_lib):
             assert rel_err(x[i], ref, mask) < TOL, prec
 
 
+@pytest.mark.parametrize("sections", [60, 1000, 1500, 4000])
+def test_plain_op_program_placements(oracle_lib, sections):
+    """The plain OP with its factorisation and solve arrays copied into shared memory (60,
+    1000 sections), read from global memory beside a shared-memory workspace (1500), and
+    with the workspace itself in global memory (4000), each against the oracle."""
+    from krets_gb300.generators import resistor_ladder_netlist
+    c = parse_circuit_description(resistor_ladder_netlist(sections, shunts=True))
+    t = element_table(c)
+    g = _lib.GpuCircuit(t, c.size)
+    x, it = g.op()
+    assert it == 1
+    assert rel_err(x, oracle_lib.op(t, c.size), is_current_mask(c)) < TOL
+
+
 def test_reference_rectifier_runs():
     """The reference's rectifier test is smoke only (test_transient.rs:163-178): its
     ground-anode diodes always see the 0.5 V default guess (diode.rs:26-30), and the
